@@ -1,0 +1,314 @@
+"""Benchmark of the GB300 MUSCL time step (one JSON line on rank 0).
+
+Workload (the accreting mid-size configuration): icosphere_hex(7)
+(163,842 faces), MUSCL_HLLCplus, dim 5, gam3d 4/3, omega_ns 0, accretion on
+(rate 1e-2, e_acc 0.5, omega_acc 0.5, tilt 0.2, width 0.1, friction on,
+alpha 1e-6), initial Sigma = Pi = 1 with 1e-3 uniform noise (seed 1), zero
+velocity, dt0 = 2e-4.  Synthetic inputs; there is no dataset.
+
+A "step" is one do_step(dt0): two RK stages over every face.  value is
+face-updates/s (faces x steps / device time) with the state resident in
+HBM; e2e is the same metric through the C ABI with host buffers (state
+uploaded and read back every step).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import platform
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+PKG = REPO / "muscl-scheme-on-spherical-mesh-wip_gb300"
+for _p in (str(PKG), str(REPO)):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "face-updates/s"
+LEVEL = 7
+DT0 = 2e-4
+PARAMS = dict(accretion_rate=1e-2, e_acc=0.5, omega_acc_abs=0.5, tilt_angle=0.2, acc_width=0.1,
+              alpha=1e-6, friction_on=True)
+
+
+def peaks():
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def workload_config(n_faces, precision_name):
+    return {"workload": f"icosphere_hex({LEVEL}) MUSCL_HLLCplus dim5 accretion_on quiet-noise seed1",
+            "n_faces": n_faces, "solver": "HLLCplus", "dt0": DT0, "precision": precision_name,
+            "l2": "per-step working set larger than the 129 MB L2 (see working_set_mb)"}
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.proc = None
+        self.tmp = tempfile.NamedTemporaryFile(prefix="clocks_", suffix=".csv", delete=False)
+        self.device = device
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.tmp, stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        self.tmp.close()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in Path(self.tmp.name).read_text().splitlines():
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        finally:
+            os.unlink(self.tmp.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+# ------------------------------------------------------------------ helpers
+def build_case(sg):
+    mesh = sg.icosphere_hex(LEVEL)
+    geom = sg.Geometry(mesh)
+    gam = sg.initial_conditions.gam2d(4 / 3)
+    U0 = sg.initial_conditions.quiet_noise(geom.unit_face_centers(), gam, seed=1)
+    return mesh, geom, gam, U0
+
+
+def time_device(sg, torch, solver, n_faces, steps, warmup):
+    """Device time of `steps` graph replays on the solver's stream."""
+    stream = torch.cuda.ExternalStream(solver.stream())
+    for _ in range(warmup):
+        solver.do_step(DT0)
+    solver.synchronize()
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    start.record(stream)
+    solver.do_steps(steps, DT0)
+    end.record(stream)
+    end.synchronize()
+    torch.cuda.synchronize()
+    return start.elapsed_time(end) / 1e3
+
+
+def time_e2e(sg, solver, U_host, steps):
+    """Through the C ABI with host buffers: set_state (H2D), do_step, get_state (D2H)."""
+    out = np.empty_like(U_host)
+    solver.set_state(U_host)
+    solver.do_step(DT0)
+    solver.get_state(out)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        solver.set_state(U_host)
+        solver.do_step(DT0)
+        solver.get_state(out)
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(geom, U0, gam, budget_s=15.0):
+    """The CPU oracle (restatement of the reference, OpenMP, all host cores)
+    on a bounded sample of the same workload."""
+    import splash_gb300 as sg
+    from oracle.oracle import Oracle
+
+    cores = os.cpu_count() or 1
+    o = Oracle(geom, U0, gam, 0.0, True, sg.SolverParams(**PARAMS).as_list(), 3, threads=cores)
+    o.do_step(DT0)  # warm-up
+    t0 = time.perf_counter()
+    n = 0
+    while n < 50:
+        o.do_step(DT0)
+        n += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": geom.n_faces * n / dt, "unit": METRIC, "cores": cores, "kind": "port",
+            "sample": f"{n} do_step calls of the full workload after 1 warm-up "
+                      f"({dt:.1f} s, OpenMP {cores} threads, {platform.machine()})"}
+
+
+def algorithmic_bytes(geom, kernel: str) -> float:
+    """Compulsory bytes per launch of one kernel of the FP64 path.
+
+    reconstruct: read W (5 x 8 B per face), per slot 4 int32 stencil ids +
+      4 betas + H+, H-, BM + edge centre (3) + |ec| + normal (3) + Courant
+      factor + 2 eta (8 B each except ids) ; write U+ (5 x 8 B per slot).
+    flux_update: read U+ (5 x 8 B per slot, each read once algorithmically),
+      per slot edge centre, |ec|, normal, n x R, chord (11 x 8 B) + reverse
+      index (4 B); per face W, U0, unit centre, area, accretion source
+      (5+5+3+1+1 doubles) ; write U (or W1) and W (10 x 8 B).
+    """
+    F = geom.n_faces
+    S = geom.n_slots
+    if kernel == "reconstruct":
+        return F * 40 + S * (16 + 8 * (4 + 3 + 3 + 1 + 3 + 1 + 2)) + S * 40
+    return S * 40 + S * (11 * 8 + 4) + F * 8 * (5 + 5 + 3 + 1 + 1) + F * 80
+
+
+# ------------------------------------------------------------------ arms
+def run_ours(args):
+    import torch
+
+    import splash_gb300 as sg
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    mesh, geom, gam, U0 = build_case(sg)
+    params = sg.SolverParams(**PARAMS)
+    prec = sg.PREC_FP64
+    prec_name = "fp64"
+    solver = sg.MUSCL_HLLCplus(mesh, U0, 5, gam, 0.0, True, params=params, precision=prec,
+                               device=local)
+    F = geom.n_faces
+    # one replica per GPU (the step does not shard)
+    with ClockSampler(local) as clocks:
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        secs = time_device(sg, torch, solver, F, args.steps, args.warmup)
+        if world > 1:
+            t = torch.tensor([secs], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            secs = float(t.item())
+    clk = clocks.summary()
+    value = F * args.steps * world / secs
+    # per-kernel device times (un-captured launches, CUDA events on the solver stream)
+    ms = solver.kernel_times(max(3, min(20, args.steps)), DT0)
+    names = ["dt_reduce", "reconstruct", "flux_update", "reconstruct", "flux_update"]
+    per_kernel = {"dt_reduce": ms[0], "reconstruct": (ms[1] + ms[3]) / 2,
+                  "flux_update": (ms[2] + ms[4]) / 2}
+    dom = max(("reconstruct", "flux_update"), key=lambda k: per_kernel[k])
+    hbm, src = peaks()
+    ach = algorithmic_bytes(geom, dom) / (per_kernel[dom] * 1e-3) / 1e9
+    geo_b, st_b = solver.memory()
+    # end to end through the C ABI with host buffers
+    U_host = solver.get_state()
+    e2e_steps = max(3, min(args.steps, 50))
+    e2e_secs = time_e2e(sg, solver, U_host, e2e_steps)
+    bytes_io = F * 5 * 8
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {**workload_config(F, prec_name), "parallelism": f"replicas{world}",
+                   "working_set_mb": round((geo_b + st_b) / 2**20, 1)},
+        "gpu_launches": 5 * args.steps,
+        "e2e": {"value": F * e2e_steps / e2e_secs, "unit": METRIC, "h2d_bytes_per_step": bytes_io,
+                "d2h_bytes_per_step": bytes_io},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm,
+                     "unit": "GB/s", "frac": ach / hbm, "traffic": None,
+                     "peak_source": f"{src} MEASURED_PEAKS.json hbm_gbs" if src == "measured" else src,
+                     "kernel_ms": per_kernel},
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(geom, U0, gam)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    solver.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_reference(args):
+    """The reference's CPU path on the host cores: the reference itself cannot
+    travel to the GPU host (its x86 build is not portable and its sources are
+    not shipped), so its restatement in oracle/ (bit-identical to the
+    reference on x86-64) runs with all host threads on the same workload."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import splash_gb300 as sg
+
+    mesh, geom, gam, U0 = build_case(sg)
+    from oracle.oracle import Oracle
+
+    cores = os.cpu_count() or 1
+    o = Oracle(geom, U0, gam, 0.0, True, sg.SolverParams(**PARAMS).as_list(), 3, threads=cores)
+    for _ in range(min(args.warmup, 1)):
+        o.do_step(DT0)
+    n = max(1, min(args.steps, 10))
+    t0 = time.perf_counter()
+    o.do_steps(n, DT0)
+    secs = time.perf_counter() - t0
+    value = geom.n_faces * n / secs
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 0,
+        "steps": n, "warmup": min(args.warmup, 1), "ms_per_step": secs / n * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": workload_config(geom.n_faces, "fp64"),
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": "port",
+                         "sample": f"{n} do_step calls of the full workload, OpenMP {cores} "
+                                   f"threads ({platform.machine()})"},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

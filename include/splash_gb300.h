@@ -1,0 +1,197 @@
+/*
+ * splash_gb300.h — C ABI of the GB300 (sm_103a) MUSCL time step of SPLASH.
+ *
+ * The reference exposes its solver only as header-only C++ classes
+ * (Riemann_solvers/{HLLE_p,HLLC,HLLCplus}.hpp on top of physics/adiabatic.hpp
+ * and MUSCL_base/MUSCL_base.hpp); it has no FFI.  Each entry point below
+ * replaces one member of that class API, cited per function, so that a
+ * C++ wrapper (include/splash_muscl.hpp), a ctypes binding or any other FFI
+ * can drive the GPU solver with plain pointers and sizes.
+ *
+ * Conventions
+ *   - Every function returns an int status: SPLASH_OK (0) or one of the
+ *     SPLASH_E_* codes; splash_last_error() returns a message for the calling
+ *     thread's most recent failure.
+ *   - Conserved state arrays are row-major [n_faces][dim] float64 in the
+ *     reference face order (the order of pmp's face iterator, i.e. the order
+ *     test.cpp reads input/input.dat).  Renumbering to the internal
+ *     space-filling-curve order happens inside the library.
+ *   - A solver handle is driven by one host thread at a time (the reference
+ *     object is not re-entrant either).  splash_do_step() is asynchronous on
+ *     the solver's CUDA stream; every call that returns host data
+ *     synchronises that stream.
+ *   - Physics problems never abort: like the reference they latch the stop
+ *     flag (MUSCL_base.hpp:17,232-235), readable with splash_stop_check()
+ *     and, bit by bit, with splash_error_word().
+ */
+#ifndef SPLASH_GB300_H
+#define SPLASH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define SPLASH_OK 0
+#define SPLASH_E_INVALID 1     /* bad argument (null pointer, size, enum) */
+#define SPLASH_E_CUDA 2        /* CUDA runtime failure */
+#define SPLASH_E_MESH 3        /* mesh violates a reference assumption */
+#define SPLASH_E_NOMEM 4       /* host or device allocation failed */
+#define SPLASH_E_UNSUPPORTED 5 /* combination not implemented */
+
+/* ---- stop-flag bits (device error word) ------------------------------ */
+#define SPLASH_STOP_NAN_FLUX 1u       /* MUSCL_base.hpp:264-268 */
+#define SPLASH_STOP_NAN_WAVESPEED 2u  /* physics/adiabatic.hpp:671-676 */
+#define SPLASH_STOP_WAVE_ORDER 4u     /* HLLE_p.hpp:50-55, HLLC.hpp:234-239, HLLCplus.hpp:169-174 */
+#define SPLASH_STOP_NEG_EXTRA_DT 8u   /* physics/adiabatic.hpp:573-577 */
+
+/* ---- enums ------------------------------------------------------------ */
+typedef enum splash_mesh_kind {
+  SPLASH_MESH_ICOSPHERE_HEX = 0, /* geometry/sph_gen.h:278-284 */
+  SPLASH_MESH_QUAD_SPHERE = 1,   /* geometry/sph_gen.h:286-295 */
+  SPLASH_MESH_ICOSPHERE = 2      /* geometry/sph_gen.h:267-276 */
+} splash_mesh_kind;
+
+typedef enum splash_solver_kind {
+  SPLASH_SOLVER_HLLE_P = 1,  /* MUSCL_HLLE_p   Riemann_solvers/HLLE_p.hpp:6-59 */
+  SPLASH_SOLVER_HLLC = 2,    /* MUSCL_HLLC     Riemann_solvers/HLLC.hpp:6-122 */
+  SPLASH_SOLVER_HLLCPLUS = 3 /* MUSCL_HLLCplus Riemann_solvers/HLLCplus.hpp:6-177 */
+} splash_solver_kind;
+
+typedef enum splash_precision {
+  SPLASH_PREC_FP64 = 0, /* the reference method in FP64 */
+  SPLASH_PREC_MIXED = 1 /* FP32 reconstruction + Riemann, FP64 state/accumulation */
+} splash_precision;
+
+/* Mesh description.  If `vertices` is NULL the mesh is generated from
+ * (kind, level) exactly as the reference generators number it; otherwise
+ * the caller supplies a closed polygonal sphere mesh in its own order. */
+typedef struct splash_mesh_desc {
+  int kind;  /* splash_mesh_kind, used when vertices == NULL */
+  int level; /* subdivision level, used when vertices == NULL */
+  int n_vertices;
+  const double* vertices; /* [n_vertices][3] */
+  int n_faces;
+  const int* face_offsets;  /* [n_faces + 1] CSR offsets into face_vertices */
+  const int* face_vertices; /* corner ids, counter-clockwise seen from outside */
+} splash_mesh_desc;
+
+/* The keys the adiabatic constructor reads from input/parameters.json
+ * (physics/adiabatic.hpp:59-68). */
+typedef struct splash_params {
+  double accretion_rate;
+  double e_acc;
+  double omega_acc_abs;
+  double tilt_angle;
+  double acc_width;
+  double alpha;
+  int friction_on;
+} splash_params;
+
+typedef struct splash_solver splash_solver;
+typedef struct splash_geometry splash_geometry;
+
+/* ---- library ---------------------------------------------------------- */
+/* Message of the calling thread's last failure ("" if none). */
+const char* splash_last_error(void);
+/* Library version string. */
+const char* splash_version(void);
+
+/* ---- solver lifetime ---------------------------------------------------- */
+/* Replaces the constructors MUSCL_HLLE_p / MUSCL_HLLC / MUSCL_HLLCplus
+ * (Riemann_solvers/HLLE_p.hpp:11-13, HLLC.hpp:11-13, HLLCplus.hpp:11-13)
+ * with the adiabatic and base constructors they chain to
+ * (physics/adiabatic.hpp:18-91, MUSCL_base/MUSCL_base.hpp:20-95,
+ * geometry/MUSCL_geometry.hpp:43-225).  `U_in` is [n_faces][dim] in the
+ * reference face order; `params` replaces the parameters.json read.
+ * `device` selects the CUDA device; `threads` sizes host-side helpers
+ * (geometry precompute) only, 0 = all cores.  dim != 5 is rejected with
+ * SPLASH_E_UNSUPPORTED: the reference prints "check dim", latches
+ * stop_check and then indexes past the state vector
+ * (physics/adiabatic.hpp:26-30, Riemann_solvers/HLLC.hpp:208). */
+int splash_create(const splash_mesh_desc* mesh, const double* U_in, int dim, double gam,
+                  double omega_ns, int accretion_on, const splash_params* params,
+                  int solver_kind, int precision, int device, int threads,
+                  splash_solver** out);
+int splash_destroy(splash_solver* s);
+
+/* ---- the hot path ------------------------------------------------------ */
+/* Replaces MUSCL_base::do_step(double dt0) (MUSCL_base.hpp:97-225): one RK2
+ * midpoint step with dt = min(dt0, 0.1 h0 / max_vel, extra_dt_constr()).
+ * Asynchronous: enqueues one CUDA-graph replay on the solver's stream. */
+int splash_do_step(splash_solver* s, double dt0);
+/* `n` consecutive do_step(dt0) calls without returning to the host. */
+int splash_do_steps(splash_solver* s, int n, double dt0);
+/* Blocks until all enqueued steps have finished. */
+int splash_synchronize(splash_solver* s);
+
+/* The cudaStream_t the solver launches on (as void*), so a caller can
+ * order its own work or record CUDA events against the step. */
+int splash_stream(splash_solver* s, void** stream);
+/* Runs `reps` un-captured steps with CUDA events around every launch and
+ * returns the mean device time per launch in milliseconds:
+ * ms[0] dt reduction, ms[1] reconstruct (stage 1), ms[2] flux+update
+ * (stage 1), ms[3] reconstruct (stage 2), ms[4] flux+update (stage 2).
+ * The steps advance the state like do_step(dt0). */
+int splash_kernel_times(splash_solver* s, int reps, double dt0, double ms[5]);
+/* Device bytes held by the solver: out[0] geometry, out[1] state + scratch. */
+int splash_memory(splash_solver* s, int64_t out[2]);
+
+/* ---- accessors ---------------------------------------------------------- */
+int splash_time(splash_solver* s, double* t);               /* MUSCL_base.hpp:227-230 */
+int splash_stop_check(splash_solver* s, int* stop);         /* MUSCL_base.hpp:232-235 */
+int splash_error_word(splash_solver* s, uint32_t* bits);    /* SPLASH_STOP_* bits */
+int splash_last_dt(splash_solver* s, double* dt);           /* the clipped dt of the last step */
+int splash_steps(splash_solver* s, int64_t* steps);         /* MUSCL_base::steps */
+int splash_n_faces(splash_solver* s, int* n_faces);
+int splash_dim(splash_solver* s, int* dim);
+/* [n_faces][dim] conserved state, reference order (MUSCL_base::U). */
+int splash_get_state(splash_solver* s, double* U);
+int splash_set_state(splash_solver* s, const double* U);
+/* Per-step diagnostics of MUSCL_base.hpp:187-214 for the current state:
+ * out[0] = sum Sigma*A, out[1..3] = sum l*A, out[4] = sum E*A. */
+int splash_diagnostics(splash_solver* s, double out[5]);
+/* Internal (space-filling-curve) position -> reference face id, [n_faces]. */
+int splash_get_permutation(splash_solver* s, int* internal_to_ref);
+
+/* ---- writers (physics/adiabatic.hpp:101-348) ---------------------------- */
+/* Each appends one line "t  v0 v1 ... " to `path` with the reference's
+ * default stream formatting (6 significant digits). */
+int splash_write_t_rho(splash_solver* s, const char* path);     /* adiabatic.hpp:101-111 */
+int splash_write_t_p(splash_solver* s, const char* path);       /* adiabatic.hpp:113-133 */
+int splash_write_t_curl(splash_solver* s, const char* path);    /* adiabatic.hpp:135-177 */
+int splash_write_t_omega_z(splash_solver* s, const char* path); /* adiabatic.hpp:195-226 */
+/* three files, Lx/Ly/Lz (adiabatic.hpp:179-193) */
+int splash_write_t_L(splash_solver* s, const char* path_x, const char* path_y,
+                     const char* path_z);
+/* out[4] = flux towards observers at 0, 45, 90, 180 deg (adiabatic.hpp:228-333) */
+int splash_get_light_curves(splash_solver* s, double out[4]);
+/* [n_faces] lines of dim values (adiabatic.hpp:335-348) */
+int splash_write_final_state(splash_solver* s, const char* path);
+
+/* ---- geometry (host, reference numbering) ------------------------------ */
+/* Builds the reference geometry (geometry/MUSCL_geometry.hpp:43-575) for a
+ * mesh description; used by the drop-in classes' geometry writers
+ * (MUSCL_geometry.hpp:1069-1117) and by the test-suite. */
+int splash_geometry_build(const splash_mesh_desc* mesh, int threads, splash_geometry** out);
+int splash_geometry_free(splash_geometry* g);
+/* sizes[0..3] = n_vertices, n_faces, n_slots, max_slots;
+ * scalars[0..1] = h0, round_diff */
+int splash_geometry_info(const splash_geometry* g, int64_t sizes[4], double scalars[2]);
+/* Copies the named array into dst (capacity `bytes`).  Names: vertices,
+ * face_off, face_vtx, nbr_off, nbr, nbr_edge, face_centers, normals, area,
+ * edge_normals, bm_dist, h_plus, h_minus, ff_plus, ff_minus, beta_plus,
+ * beta_minus, and hilbert_order (internal position -> reference face id,
+ * the numbering splash_create uses).  *written receives the byte count
+ * (may be NULL). */
+int splash_geometry_get(const splash_geometry* g, const char* name, void* dst, size_t bytes,
+                        size_t* written);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* SPLASH_GB300_H */

@@ -1,0 +1,870 @@
+// C ABI of the GB300 MUSCL step (include/splash_gb300.h).
+//
+// Host side of the drop-in: it reproduces the reference constructor chain
+// (Riemann_solvers/*.hpp ctor -> physics/adiabatic.hpp:18-91 ->
+// MUSCL_base/MUSCL_base.hpp:20-95 -> geometry/MUSCL_geometry.hpp:43-225),
+// renumbers faces along a Hilbert curve, uploads the slot-plane geometry
+// once, captures one do_step as a CUDA graph, and implements the accessors
+// and writers of the reference class API on top of device state.
+#include "splash_gb300.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "geometry.hpp"
+#include "hilbert.hpp"
+#include "kernels.hpp"
+#include "layout.hpp"
+#include "mesh.hpp"
+#include "solver.hpp"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+#define SPLASH_CUDA(call)                                                                   \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess)                                                                  \
+      return fail(SPLASH_E_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_),    \
+                  __FILE__, __LINE__);                                                      \
+  } while (0)
+
+}  // namespace
+
+struct splash_geometry {
+  splash::RefGeometry g;
+};
+
+namespace splash {
+
+int Solver::check_cuda(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) return fail(SPLASH_E_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  return SPLASH_OK;
+}
+
+Solver::~Solver() {
+  if (device >= 0) cudaSetDevice(device);
+  if (graph_exec) cudaGraphExecDestroy(graph_exec);
+  if (graph) cudaGraphDestroy(graph);
+  for (void* p : dev_allocs) cudaFree(p);
+  if (h_stage) cudaFreeHost(h_stage);
+  if (stream) cudaStreamDestroy(stream);
+}
+
+template <typename T>
+T* Solver::dalloc(size_t n) {
+  void* p = nullptr;
+  if (cudaMalloc(&p, n * sizeof(T) > 0 ? n * sizeof(T) : 16) != cudaSuccess) throw std::bad_alloc();
+  dev_allocs.push_back(p);
+  return static_cast<T*>(p);
+}
+
+template <typename T>
+T* Solver::upload(const std::vector<T>& h) {
+  T* d = dalloc<T>(h.size());
+  if (!h.empty() && cudaMemcpy(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess)
+    throw std::runtime_error("cudaMemcpy upload failed");
+  return d;
+}
+
+}  // namespace splash
+
+namespace {
+
+using splash::RefGeometry;
+using splash::Solver;
+
+// Mesh from a descriptor: generated with the reference numbering, or given.
+splash::MeshArrays mesh_from_desc(const splash_mesh_desc* d) {
+  if (d->vertices == nullptr) {
+    return splash::mesh_arrays(splash::build_mesh(d->kind, d->level));
+  }
+  if (d->n_vertices <= 0 || d->n_faces <= 0 || !d->face_offsets || !d->face_vertices)
+    throw std::runtime_error("incomplete mesh arrays");
+  splash::MeshArrays a;
+  a.vertices.assign(d->vertices, d->vertices + 3 * (size_t)d->n_vertices);
+  a.face_off.assign(d->face_offsets, d->face_offsets + d->n_faces + 1);
+  if (a.face_off[0] != 0 || a.face_off[d->n_faces] <= 0) throw std::runtime_error("bad face offsets");
+  a.face_vtx.assign(d->face_vertices, d->face_vertices + a.face_off[d->n_faces]);
+  return a;
+}
+
+struct V3 {
+  double x, y, z;
+};
+inline V3 vadd(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline V3 vsub(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline V3 vdiv(V3 a, double s) { return {a.x / s, a.y / s, a.z / s}; }
+inline double vnorm(V3 a) {
+  double s = 0.0;
+  s += a.x * a.x;
+  s += a.y * a.y;
+  s += a.z * a.z;
+  return std::sqrt(s);
+}
+inline V3 vcross(V3 a, V3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline double vdot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline V3 at3(const std::vector<double>& v, size_t i) { return {v[3 * i], v[3 * i + 1], v[3 * i + 2]}; }
+
+// std::max / std::min semantics
+inline double smax(double a, double b) { return (a < b) ? b : a; }
+
+}  // namespace
+
+namespace splash {
+
+// Host precompute of every slot-plane array; see layout.hpp.
+void Solver::build_device_geometry(const RefGeometry& g) {
+  const int nf = g.n_faces;
+  n_faces = nf;
+  max_slots = g.max_slots;
+  fpad = (nf + 31) / 32 * 32;
+  const size_t PS = (size_t)max_slots * fpad;
+
+  perm = hilbert_order(g.face_centers.data(), nf);
+  iperm.assign(nf, 0);
+  for (int i = 0; i < nf; ++i) iperm[perm[i]] = i;
+
+  // reference-order reverse slot (std::find of MUSCL_base.hpp:383-384)
+  std::vector<int> j0_of(g.n_slots, -1);
+  for (int f = 0; f < nf; ++f) {
+    for (int s = g.face_off[f]; s < g.face_off[f + 1]; ++s) {
+      const int nb = g.nbr_edge[s];
+      int j0 = -1;
+      for (int q = g.face_off[nb]; q < g.face_off[nb + 1]; ++q)
+        if (g.nbr_edge[q] == f) {
+          j0 = q - g.face_off[nb];
+          break;
+        }
+      if (j0 < 0) throw std::runtime_error("edge neighbour relation is not symmetric");
+      j0_of[s] = j0;
+    }
+  }
+
+  std::vector<int8_t> h_nslots(fpad, 0);
+  std::vector<double> h_fcn(3 * (size_t)fpad, 0.0), h_area(fpad, 1.0), h_acc(fpad, 0.0);
+  std::vector<int> h_sten(4 * PS, 0), h_rev(PS, 0);
+  std::vector<double> h_beta(4 * PS, 0.0), h_hpm(2 * PS, 1.0), h_bm(PS, 1.0), h_eta(2 * PS, 1.0),
+      h_arc(PS, 0.0), h_ec(3 * PS, 0.0), h_ecn(PS, 1.0), h_en(3 * PS, 0.0), h_nxr(3 * PS, 0.0),
+      h_chord(PS, 0.0);
+
+  const double sigma = par.acc_width / 2.355;
+  const double mu = M_PI / 2;
+  for (int i = 0; i < nf; ++i) {
+    const int r = perm[i];
+    const int n = g.face_off[r + 1] - g.face_off[r];
+    h_nslots[i] = (int8_t)n;
+    V3 fc = at3(g.face_centers, r);
+    const V3 fcn = vdiv(fc, vnorm(fc));
+    h_fcn[i] = fcn.x;
+    h_fcn[fpad + i] = fcn.y;
+    h_fcn[2 * (size_t)fpad + i] = fcn.z;
+    h_area[i] = g.area[r];
+    if (accretion_on) {
+      // res[0] of physics/adiabatic.hpp:428-436 (depends on geometry only)
+      const double theta_acc = std::acos(fcn.y * std::sin(par.tilt_angle) + fcn.z * std::cos(par.tilt_angle));
+      h_acc[i] = 1 / area_coeff * par.accretion_rate / std::sqrt(2 * M_PI * sigma * sigma) *
+                 std::exp(-(theta_acc - mu) * (theta_acc - mu) / (2 * sigma * sigma));
+    }
+    for (int j = 0; j < n; ++j) {
+      const int sr = g.face_off[r] + j;
+      const size_t s = (size_t)j * fpad + i;
+      h_sten[s] = iperm[g.ff_plus[2 * (size_t)sr]];
+      h_sten[PS + s] = iperm[g.ff_plus[2 * (size_t)sr + 1]];
+      h_sten[2 * PS + s] = iperm[g.ff_minus[2 * (size_t)sr]];
+      h_sten[3 * PS + s] = iperm[g.ff_minus[2 * (size_t)sr + 1]];
+      h_beta[s] = g.beta_plus[2 * (size_t)sr];
+      h_beta[PS + s] = g.beta_plus[2 * (size_t)sr + 1];
+      h_beta[2 * PS + s] = g.beta_minus[2 * (size_t)sr];
+      h_beta[3 * PS + s] = g.beta_minus[2 * (size_t)sr + 1];
+      h_hpm[s] = g.h_plus[sr];
+      h_hpm[PS + s] = g.h_minus[sr];
+      h_bm[s] = g.bm_dist[sr];
+      h_eta[s] = g.h_plus[sr] / g.bm_dist[sr];
+      h_eta[PS + s] = g.h_minus[sr] / g.bm_dist[sr];
+      const int va = g.face_vtx[sr];
+      const int vb = g.face_vtx[g.face_off[r] + ((j + 1 == n) ? 0 : j + 1)];
+      const V3 A = at3(g.vertices, va), B = at3(g.vertices, vb);
+      h_arc[s] = great_circle(&g.vertices[3 * (size_t)va], &g.vertices[3 * (size_t)vb]) / g.area[r];
+      V3 ec = vdiv(vadd(A, B), 2.);
+      ec = vdiv(ec, vnorm(ec));
+      const double ecn = vnorm(ec);
+      h_ec[s] = ec.x;
+      h_ec[PS + s] = ec.y;
+      h_ec[2 * PS + s] = ec.z;
+      h_ecn[s] = ecn;
+      const V3 en = at3(g.edge_normals, sr);
+      h_en[s] = en.x;
+      h_en[PS + s] = en.y;
+      h_en[2 * PS + s] = en.z;
+      const V3 nxr = vcross(en, vdiv(ec, ecn));
+      h_nxr[s] = nxr.x;
+      h_nxr[PS + s] = nxr.y;
+      h_nxr[2 * PS + s] = nxr.z;
+      h_chord[s] = vnorm(vsub(A, B));
+      const int nb = g.nbr_edge[sr];
+      h_rev[s] = j0_of[sr] * fpad + iperm[nb];
+    }
+    // unused slots of low-valence faces point at themselves (never read)
+    for (int j = n; j < max_slots; ++j) {
+      const size_t s = (size_t)j * fpad + i;
+      for (int q = 0; q < 4; ++q) h_sten[q * PS + s] = i;
+      h_rev[s] = (int)s;
+    }
+  }
+  // padding faces
+  for (int i = nf; i < fpad; ++i) {
+    for (int j = 0; j < max_slots; ++j) {
+      const size_t s = (size_t)j * fpad + i;
+      for (int q = 0; q < 4; ++q) h_sten[q * PS + s] = 0;
+      h_rev[s] = 0;
+    }
+  }
+
+  G.n_faces = nf;
+  G.fpad = fpad;
+  G.max_slots = max_slots;
+  G.nslots = upload(h_nslots);
+  G.fcn = upload(h_fcn);
+  G.area = upload(h_area);
+  G.acc_src = upload(h_acc);
+  G.sten = upload(h_sten);
+  G.beta = upload(h_beta);
+  G.hpm = upload(h_hpm);
+  G.bm = upload(h_bm);
+  G.eta = upload(h_eta);
+  G.arc_a = upload(h_arc);
+  G.ec = upload(h_ec);
+  G.ecn = upload(h_ecn);
+  G.en = upload(h_en);
+  G.nxr = upload(h_nxr);
+  G.chord = upload(h_chord);
+  G.rev = upload(h_rev);
+  geometry_bytes = 0;
+  geometry_bytes += h_nslots.size() + 8 * (h_fcn.size() + h_area.size() + h_acc.size());
+  geometry_bytes += 4 * (h_sten.size() + h_rev.size());
+  geometry_bytes += 8 * (h_beta.size() + h_hpm.size() + h_bm.size() + h_eta.size() + h_arc.size() +
+                         h_ec.size() + h_ecn.size() + h_en.size() + h_nxr.size() + h_chord.size());
+
+  // keep what the writers need, in reference order
+  wr_vertices = g.vertices;
+  wr_face_off = g.face_off;
+  wr_face_vtx = g.face_vtx;
+  wr_face_centers = g.face_centers;
+  wr_area = g.area;
+}
+
+int Solver::upload_state(const double* U_ref) {
+  std::memcpy(h_stage, U_ref, (size_t)n_faces * kDim * sizeof(double));
+  SPLASH_CUDA(cudaMemcpyAsync(d_stage, h_stage, (size_t)n_faces * kDim * sizeof(double),
+                              cudaMemcpyHostToDevice, stream));
+  SPLASH_CUDA(fp64_scatter_state(d_stage, d_perm, S.U, n_faces, fpad, stream));
+  SPLASH_CUDA(fp64_prepare(G, S, P, stream));
+  return SPLASH_OK;
+}
+
+int Solver::download_state(double* U_ref) {
+  SPLASH_CUDA(fp64_gather_state(S.U, d_perm, d_stage, n_faces, fpad, stream));
+  SPLASH_CUDA(cudaMemcpyAsync(h_stage, d_stage, (size_t)n_faces * kDim * sizeof(double),
+                              cudaMemcpyDeviceToHost, stream));
+  SPLASH_CUDA(cudaStreamSynchronize(stream));
+  std::memcpy(U_ref, h_stage, (size_t)n_faces * kDim * sizeof(double));
+  return SPLASH_OK;
+}
+
+int Solver::read_scalars(double* out) {
+  SPLASH_CUDA(cudaMemcpyAsync(out, S.scal, kScCount * sizeof(double), cudaMemcpyDeviceToHost, stream));
+  SPLASH_CUDA(cudaStreamSynchronize(stream));
+  return SPLASH_OK;
+}
+
+int Solver::capture_graph() {
+  SPLASH_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t le = fp64_step(G, S, P, stream);
+  cudaGraph_t g = nullptr;
+  cudaError_t ce = cudaStreamEndCapture(stream, &g);
+  if (le != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return fail(SPLASH_E_CUDA, "step launch during capture: %s", cudaGetErrorString(le));
+  }
+  SPLASH_CUDA(ce);
+  graph = g;
+  SPLASH_CUDA(cudaGraphInstantiate(&graph_exec, graph, 0));
+  return SPLASH_OK;
+}
+
+int Solver::step(double dt0) {
+  SPLASH_CUDA(fp64_set_dt0(S, dt0, stream));
+  SPLASH_CUDA(cudaGraphLaunch(graph_exec, stream));
+  ++steps;
+  return SPLASH_OK;
+}
+
+}  // namespace splash
+
+// ============================ C ABI ======================================
+extern "C" {
+
+const char* splash_last_error(void) { return g_last_error.c_str(); }
+const char* splash_version(void) { return "splash_gb300 1.0 (sm_103a)"; }
+
+int splash_create(const splash_mesh_desc* mesh, const double* U_in, int dim, double gam,
+                  double omega_ns, int accretion_on, const splash_params* params, int solver_kind,
+                  int precision, int device, int threads, splash_solver** out) {
+  if (!out) return fail(SPLASH_E_INVALID, "out is NULL");
+  *out = nullptr;
+  if (!mesh || !U_in || !params) return fail(SPLASH_E_INVALID, "mesh, U_in and params must be non-NULL");
+  if (dim != splash::kDim)
+    return fail(SPLASH_E_UNSUPPORTED,
+                "dim=%d: the adiabatic solvers need dim=5 (the reference latches stop_check and "
+                "then indexes out of bounds, physics/adiabatic.hpp:26-30)",
+                dim);
+  if (solver_kind < SPLASH_SOLVER_HLLE_P || solver_kind > SPLASH_SOLVER_HLLCPLUS)
+    return fail(SPLASH_E_INVALID, "unknown solver kind %d", solver_kind);
+  if (precision != SPLASH_PREC_FP64 && precision != SPLASH_PREC_MIXED)
+    return fail(SPLASH_E_INVALID, "unknown precision %d", precision);
+  if (precision == SPLASH_PREC_MIXED && !splash::mixed_available())
+    return fail(SPLASH_E_UNSUPPORTED, "mixed precision path not built");
+  if (!(gam > 1.0 && gam < 2.0)) return fail(SPLASH_E_INVALID, "gam=%g must lie in (1, 2)", gam);
+
+  std::unique_ptr<Solver> s(new (std::nothrow) Solver());
+  if (!s) return fail(SPLASH_E_NOMEM, "host allocation failed");
+  try {
+    splash::MeshArrays arrays = mesh_from_desc(mesh);
+    RefGeometry g = splash::build_ref_geometry(arrays, threads);
+    s->par = *params;
+    s->accretion_on = accretion_on != 0;
+    s->precision = precision;
+    s->solver_kind = solver_kind;
+    s->device = device;
+    // adiabatic ctor: area_coeff (loop counter taken to start at 0) and
+    // total_mass (physics/adiabatic.hpp:70-90)
+    {
+      double ac = 0;
+      const double mu = M_PI / 2;
+      const double sigma = params->acc_width / 2.355;
+      for (int n = 0; n < g.n_faces; ++n) {
+        const V3 c = at3(g.face_centers, n);
+        const double theta = std::acos(c.z / vnorm(c));
+        ac += g.area[n] / std::sqrt(2 * M_PI * sigma * sigma) *
+              std::exp(-(theta - mu) * (theta - mu) / (2 * sigma * sigma));
+      }
+      ac /= 4 * M_PI;
+      s->area_coeff = ac;
+      double tm = 0;
+      for (int n = 0; n < g.n_faces; ++n) tm += U_in[(size_t)n * dim] * g.area[n];
+      s->total_mass = tm;
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+      return fail(SPLASH_E_CUDA, "no CUDA device available");
+    if (device < 0 || device >= ndev) return fail(SPLASH_E_INVALID, "device %d out of range", device);
+    SPLASH_CUDA(cudaSetDevice(device));
+    SPLASH_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+
+    s->build_device_geometry(g);
+    splash::PhysParams& P = s->P;
+    P.gam = gam;
+    P.omega_ns = omega_ns;
+    P.e_acc = params->e_acc;
+    P.omega_acc_x = 0;
+    P.omega_acc_y = std::sin(params->tilt_angle) * params->omega_acc_abs;
+    P.omega_acc_z = std::cos(params->tilt_angle) * params->omega_acc_abs;
+    P.alpha = params->alpha;
+    P.acc_rate = params->accretion_rate;
+    P.total_mass = s->total_mass;
+    P.h0 = g.h0;
+    P.round_diff = g.round_diff;
+    P.accretion_on = accretion_on ? 1 : 0;
+    P.friction_on = params->friction_on ? 1 : 0;
+    P.solver = solver_kind;
+
+    const size_t fp = (size_t)s->fpad;
+    const size_t PS = (size_t)s->max_slots * fp;
+    splash::DevState& S = s->S;
+    S.U = s->dalloc<double>(splash::kDim * fp);
+    S.W0 = s->dalloc<double>(splash::kDim * fp);
+    S.W1 = s->dalloc<double>(splash::kDim * fp);
+    S.uplus = s->dalloc<double>(splash::kDim * PS);
+    s->n_partials = splash::fp64_partial_blocks(s->n_faces);
+    S.partial = s->dalloc<double>((size_t)s->n_partials * splash::kPartialStride);
+    S.scal = s->dalloc<double>(splash::kScCount);
+    S.err = s->dalloc<unsigned int>(4);
+    s->d_stage = s->dalloc<double>((size_t)s->n_faces * splash::kDim);
+    s->d_perm = s->upload(s->perm);
+    SPLASH_CUDA(cudaMemset(S.U, 0, splash::kDim * fp * sizeof(double)));
+    SPLASH_CUDA(cudaMemset(S.W0, 0, splash::kDim * fp * sizeof(double)));
+    SPLASH_CUDA(cudaMemset(S.W1, 0, splash::kDim * fp * sizeof(double)));
+    SPLASH_CUDA(cudaMemset(S.uplus, 0, splash::kDim * PS * sizeof(double)));
+    SPLASH_CUDA(cudaMemset(S.scal, 0, splash::kScCount * sizeof(double)));
+    SPLASH_CUDA(cudaMemset(S.err, 0, 4 * sizeof(unsigned int)));
+    SPLASH_CUDA(cudaMallocHost(&s->h_stage, (size_t)s->n_faces * splash::kDim * sizeof(double)));
+
+    int rc = s->upload_state(U_in);
+    if (rc) return rc;
+    rc = s->capture_graph();
+    if (rc) return rc;
+    SPLASH_CUDA(cudaStreamSynchronize(s->stream));
+  } catch (const std::bad_alloc&) {
+    return fail(SPLASH_E_NOMEM, "allocation failed while building the solver");
+  } catch (const std::exception& e) {
+    return fail(SPLASH_E_MESH, "%s", e.what());
+  }
+  *out = reinterpret_cast<splash_solver*>(s.release());
+  return SPLASH_OK;
+}
+
+int splash_destroy(splash_solver* h) {
+  delete reinterpret_cast<Solver*>(h);
+  return SPLASH_OK;
+}
+
+#define GET_SOLVER(h)                                                   \
+  Solver* s = reinterpret_cast<Solver*>(h);                             \
+  if (!s) return fail(SPLASH_E_INVALID, "solver handle is NULL");      \
+  SPLASH_CUDA(cudaSetDevice(s->device))
+
+int splash_do_step(splash_solver* h, double dt0) {
+  GET_SOLVER(h);
+  return s->step(dt0);
+}
+
+int splash_do_steps(splash_solver* h, int n, double dt0) {
+  GET_SOLVER(h);
+  if (n < 0) return fail(SPLASH_E_INVALID, "n < 0");
+  for (int i = 0; i < n; ++i) {
+    const int rc = s->step(dt0);
+    if (rc) return rc;
+  }
+  return SPLASH_OK;
+}
+
+int splash_stream(splash_solver* h, void** stream) {
+  Solver* s = reinterpret_cast<Solver*>(h);
+  if (!s || !stream) return fail(SPLASH_E_INVALID, "NULL argument");
+  *stream = (void*)s->stream;
+  return SPLASH_OK;
+}
+
+int splash_kernel_times(splash_solver* h, int reps, double dt0, double ms[5]) {
+  GET_SOLVER(h);
+  if (reps <= 0 || !ms) return fail(SPLASH_E_INVALID, "reps must be > 0 and ms non-NULL");
+  cudaEvent_t ev[6];
+  for (auto& e : ev) SPLASH_CUDA(cudaEventCreate(&e));
+  double acc[5] = {0, 0, 0, 0, 0};
+  int rc = SPLASH_OK;
+  for (int r = 0; r < reps && rc == SPLASH_OK; ++r) {
+    cudaError_t e = splash::fp64_set_dt0(s->S, dt0, s->stream);
+    if (e == cudaSuccess) e = splash::fp64_step(s->G, s->S, s->P, s->stream, ev);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ev[5]);
+    if (e != cudaSuccess) {
+      rc = fail(SPLASH_E_CUDA, "kernel timing: %s", cudaGetErrorString(e));
+      break;
+    }
+    for (int k = 0; k < 5; ++k) {
+      float t = 0;
+      cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+      acc[k] += t;
+    }
+    ++s->steps;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  if (rc) return rc;
+  for (int k = 0; k < 5; ++k) ms[k] = acc[k] / reps;
+  return SPLASH_OK;
+}
+
+int splash_memory(splash_solver* h, int64_t out[2]) {
+  Solver* s = reinterpret_cast<Solver*>(h);
+  if (!s || !out) return fail(SPLASH_E_INVALID, "NULL argument");
+  const size_t fp = (size_t)s->fpad, PS = (size_t)s->max_slots * fp;
+  out[0] = (int64_t)s->geometry_bytes;
+  out[1] = (int64_t)(8 * (3 * splash::kDim * fp + splash::kDim * PS) +
+                     8 * (size_t)s->n_partials * splash::kPartialStride);
+  return SPLASH_OK;
+}
+
+int splash_synchronize(splash_solver* h) {
+  GET_SOLVER(h);
+  SPLASH_CUDA(cudaStreamSynchronize(s->stream));
+  return SPLASH_OK;
+}
+
+int splash_time(splash_solver* h, double* t) {
+  GET_SOLVER(h);
+  if (!t) return fail(SPLASH_E_INVALID, "t is NULL");
+  double sc[splash::kScCount];
+  const int rc = s->read_scalars(sc);
+  if (rc) return rc;
+  *t = sc[splash::kScTime];
+  return SPLASH_OK;
+}
+
+int splash_last_dt(splash_solver* h, double* dt) {
+  GET_SOLVER(h);
+  if (!dt) return fail(SPLASH_E_INVALID, "dt is NULL");
+  double sc[splash::kScCount];
+  const int rc = s->read_scalars(sc);
+  if (rc) return rc;
+  *dt = sc[splash::kScDt];
+  return SPLASH_OK;
+}
+
+int splash_error_word(splash_solver* h, uint32_t* bits) {
+  GET_SOLVER(h);
+  if (!bits) return fail(SPLASH_E_INVALID, "bits is NULL");
+  unsigned int e = 0;
+  SPLASH_CUDA(cudaMemcpyAsync(&e, s->S.err, sizeof e, cudaMemcpyDeviceToHost, s->stream));
+  SPLASH_CUDA(cudaStreamSynchronize(s->stream));
+  *bits = e;
+  return SPLASH_OK;
+}
+
+int splash_stop_check(splash_solver* h, int* stop) {
+  if (!stop) return fail(SPLASH_E_INVALID, "stop is NULL");
+  uint32_t bits = 0;
+  const int rc = splash_error_word(h, &bits);
+  if (rc) return rc;
+  *stop = bits != 0;
+  return SPLASH_OK;
+}
+
+int splash_steps(splash_solver* h, int64_t* steps) {
+  Solver* s = reinterpret_cast<Solver*>(h);
+  if (!s || !steps) return fail(SPLASH_E_INVALID, "NULL argument");
+  *steps = s->steps;
+  return SPLASH_OK;
+}
+
+int splash_n_faces(splash_solver* h, int* n) {
+  Solver* s = reinterpret_cast<Solver*>(h);
+  if (!s || !n) return fail(SPLASH_E_INVALID, "NULL argument");
+  *n = s->n_faces;
+  return SPLASH_OK;
+}
+
+int splash_dim(splash_solver* h, int* d) {
+  Solver* s = reinterpret_cast<Solver*>(h);
+  if (!s || !d) return fail(SPLASH_E_INVALID, "NULL argument");
+  *d = splash::kDim;
+  return SPLASH_OK;
+}
+
+int splash_get_state(splash_solver* h, double* U) {
+  GET_SOLVER(h);
+  if (!U) return fail(SPLASH_E_INVALID, "U is NULL");
+  return s->download_state(U);
+}
+
+int splash_set_state(splash_solver* h, const double* U) {
+  GET_SOLVER(h);
+  if (!U) return fail(SPLASH_E_INVALID, "U is NULL");
+  const int rc = s->upload_state(U);
+  if (rc) return rc;
+  SPLASH_CUDA(cudaStreamSynchronize(s->stream));
+  return SPLASH_OK;
+}
+
+int splash_diagnostics(splash_solver* h, double out[5]) {
+  GET_SOLVER(h);
+  if (!out) return fail(SPLASH_E_INVALID, "out is NULL");
+  std::vector<double> U((size_t)s->n_faces * splash::kDim);
+  int rc = s->download_state(U.data());
+  if (rc) return rc;
+  double m = 0, l1 = 0, l2 = 0, l3 = 0, e = 0;
+  for (int i = 0; i < s->n_faces; ++i) {
+    const double* u = &U[(size_t)i * splash::kDim];
+    m += u[0] * s->wr_area[i];
+    l1 += u[1] * s->wr_area[i];
+    l2 += u[2] * s->wr_area[i];
+    l3 += u[3] * s->wr_area[i];
+    e += u[4] * s->wr_area[i];
+  }
+  out[0] = m;
+  out[1] = l1;
+  out[2] = l2;
+  out[3] = l3;
+  out[4] = e;
+  return SPLASH_OK;
+}
+
+int splash_get_permutation(splash_solver* h, int* internal_to_ref) {
+  Solver* s = reinterpret_cast<Solver*>(h);
+  if (!s || !internal_to_ref) return fail(SPLASH_E_INVALID, "NULL argument");
+  std::copy(s->perm.begin(), s->perm.end(), internal_to_ref);
+  return SPLASH_OK;
+}
+
+// ---------------- writers (physics/adiabatic.hpp:101-348) ----------------
+static int open_append(std::ofstream& os, const char* path) {
+  if (!path) return fail(SPLASH_E_INVALID, "path is NULL");
+  os.open(path, std::ios::out | std::ios::app);
+  if (!os) return fail(SPLASH_E_INVALID, "cannot open %s", path);
+  return SPLASH_OK;
+}
+
+int splash_write_t_rho(splash_solver* h, const char* path) {
+  GET_SOLVER(h);
+  std::ofstream os;
+  int rc = open_append(os, path);
+  if (rc) return rc;
+  std::vector<double> U((size_t)s->n_faces * splash::kDim);
+  if ((rc = s->download_state(U.data()))) return rc;
+  double t;
+  if ((rc = splash_time(h, &t))) return rc;
+  os << t << "  ";
+  for (int i = 0; i < s->n_faces; ++i) os << U[(size_t)i * splash::kDim] << " ";
+  os << "\n";
+  return SPLASH_OK;
+}
+
+int splash_write_t_p(splash_solver* h, const char* path) {
+  GET_SOLVER(h);
+  std::ofstream os;
+  int rc = open_append(os, path);
+  if (rc) return rc;
+  std::vector<double> U((size_t)s->n_faces * splash::kDim);
+  if ((rc = s->download_state(U.data()))) return rc;
+  double t;
+  if ((rc = splash_time(h, &t))) return rc;
+  os << t << "  ";
+  for (int i = 0; i < s->n_faces; ++i) {
+    const double* u = &U[(size_t)i * splash::kDim];
+    const V3 fc = at3(s->wr_face_centers, i);
+    V3 vel = vcross(vdiv(fc, vnorm(fc)), V3{u[1], u[2], u[3]});
+    vel = vdiv(vel, -u[0]);
+    const double n = vnorm(vel);
+    os << smax(1e-16, (u[4] - u[0] * (n * n) / 2) * (s->P.gam - 1)) << " ";
+  }
+  os << "\n";
+  return SPLASH_OK;
+}
+
+int splash_write_t_curl(splash_solver* h, const char* path) {
+  GET_SOLVER(h);
+  std::ofstream os;
+  int rc = open_append(os, path);
+  if (rc) return rc;
+  std::vector<double> U((size_t)s->n_faces * splash::kDim);
+  if ((rc = s->download_state(U.data()))) return rc;
+  // U_plus of the last stage, slot planes -> host
+  const size_t PS = (size_t)s->max_slots * s->fpad;
+  std::vector<double> up(splash::kDim * PS);
+  SPLASH_CUDA(cudaMemcpy(up.data(), s->S.uplus, up.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  double t;
+  if ((rc = splash_time(h, &t))) return rc;
+  os << t << "  ";
+  for (int r = 0; r < s->n_faces; ++r) {
+    const int i = s->iperm[r];
+    const int n = s->wr_face_off[r + 1] - s->wr_face_off[r];
+    double vort = 0;
+    for (int j = 0; j < n; ++j) {
+      const size_t sl = (size_t)j * s->fpad + i;
+      const V3 l{up[PS + sl], up[2 * PS + sl], up[3 * PS + sl]};
+      const int va = s->wr_face_vtx[s->wr_face_off[r] + j];
+      const int vb = s->wr_face_vtx[s->wr_face_off[r] + ((j + 1 == n) ? 0 : j + 1)];
+      V3 ec = vdiv(vadd(at3(s->wr_vertices, va), at3(s->wr_vertices, vb)), 2.);
+      ec = vdiv(ec, vnorm(ec));
+      V3 vel = vcross(ec, l);
+      vel = vdiv(vel, -U[(size_t)r * splash::kDim]);
+      const V3 rr = vsub(at3(s->wr_vertices, va), at3(s->wr_vertices, vb));
+      vort += vdot(vel, rr);
+    }
+    os << vort / s->wr_area[r] << " ";
+  }
+  os << "\n";
+  return SPLASH_OK;
+}
+
+int splash_write_t_L(splash_solver* h, const char* px, const char* py, const char* pz) {
+  GET_SOLVER(h);
+  std::vector<double> U((size_t)s->n_faces * splash::kDim);
+  int rc;
+  if ((rc = s->download_state(U.data()))) return rc;
+  double t;
+  if ((rc = splash_time(h, &t))) return rc;
+  const char* paths[3] = {px, py, pz};
+  for (int k = 0; k < 3; ++k) {
+    std::ofstream os;
+    if ((rc = open_append(os, paths[k]))) return rc;
+    os << t << "  ";
+    for (int i = 0; i < s->n_faces; ++i) os << U[(size_t)i * splash::kDim + k + 1] << " ";
+    os << "\n";
+  }
+  return SPLASH_OK;
+}
+
+int splash_write_t_omega_z(splash_solver* h, const char* path) {
+  GET_SOLVER(h);
+  std::ofstream os;
+  int rc = open_append(os, path);
+  if (rc) return rc;
+  std::vector<double> U((size_t)s->n_faces * splash::kDim);
+  if ((rc = s->download_state(U.data()))) return rc;
+  double t;
+  if ((rc = splash_time(h, &t))) return rc;
+  os << t << "  ";
+  for (int i = 0; i < s->n_faces; ++i) {
+    const double* u = &U[(size_t)i * splash::kDim];
+    const V3 fc = at3(s->wr_face_centers, i);
+    const double theta = std::acos(fc.z / vnorm(fc));
+    const V3 fcn = vdiv(fc, vnorm(fc));
+    V3 vel = vcross(fcn, V3{u[1], u[2], u[3]});
+    vel = vdiv(vel, -u[0]);
+    const V3 rxv = vcross(fcn, vel);
+    double om_z = rxv.z / (std::sin(theta) * std::sin(theta));
+    if (std::isnan(om_z) || std::isinf(om_z) || std::abs(om_z) > 1e4) om_z = 0;
+    os << om_z << " ";
+  }
+  os << "\n";
+  return SPLASH_OK;
+}
+
+int splash_get_light_curves(splash_solver* h, double out[4]) {
+  GET_SOLVER(h);
+  if (!out) return fail(SPLASH_E_INVALID, "out is NULL");
+  std::vector<double> U((size_t)s->n_faces * splash::kDim);
+  int rc;
+  if ((rc = s->download_state(U.data()))) return rc;
+  // observers of physics/adiabatic.hpp:233-245
+  const double D = 9.4 * 3 * 1e19 / 15000;
+  const V3 o0{D, 0, 0};
+  const V3 o45{std::sqrt(9.4 * 3 * 1e19 / 15000), 0, std::sqrt(9.4 * 3 * 1e19 / 15000)};
+  const V3 o90{0, 0, D};
+  const V3 o180{0, 0, -9.4 * 3 * 1e19 / 15000};
+  double f0 = 0, f45 = 0, f90 = 0, f180 = 0;
+  for (int i = 0; i < s->n_faces; ++i) {
+    const double* u = &U[(size_t)i * splash::kDim];
+    const V3 fc = at3(s->wr_face_centers, i);
+    const double phi_fc = std::atan2(fc.y / vnorm(fc), fc.x / vnorm(fc));
+    const double theta_fc = std::acos(fc.z / vnorm(fc));
+    const V3 fcn = vdiv(fc, vnorm(fc));
+    V3 vel = vcross(fcn, V3{u[1], u[2], u[3]});
+    vel = vdiv(vel, -u[0]);
+    const double vn = vnorm(vel);
+    const double PI = smax(1e-16, (u[4] - u[0] * (vn * vn) / 2) * (s->P.gam - 1));
+    const double area = s->wr_area[i];
+    if (phi_fc < M_PI / 2 && phi_fc > -M_PI / 2) f0 += PI * (std::abs(vdot(o0, fcn)) / vnorm(o0)) * area;
+    if (theta_fc < M_PI / 2) f90 += PI * (std::abs(vdot(o90, fcn)) / vnorm(o90)) * area;
+    if (vdot(o45, fcn) > 0) f45 += PI * (std::abs(vdot(o45, fcn)) / vnorm(o45)) * area;
+    if (theta_fc > M_PI / 2) f180 += PI * (std::abs(vdot(o180, fcn)) / vnorm(o180)) * area;
+  }
+  out[0] = f0;
+  out[1] = f45;
+  out[2] = f90;
+  out[3] = f180;
+  return SPLASH_OK;
+}
+
+int splash_write_final_state(splash_solver* h, const char* path) {
+  GET_SOLVER(h);
+  if (!path) return fail(SPLASH_E_INVALID, "path is NULL");
+  std::vector<double> U((size_t)s->n_faces * splash::kDim);
+  int rc;
+  if ((rc = s->download_state(U.data()))) return rc;
+  std::ofstream os(path, std::ios::out | std::ios::trunc);
+  if (!os) return fail(SPLASH_E_INVALID, "cannot open %s", path);
+  for (int i = 0; i < s->n_faces; ++i) {
+    for (int k = 0; k < splash::kDim; ++k) os << U[(size_t)i * splash::kDim + k] << " ";
+    os << "\n";
+  }
+  return SPLASH_OK;
+}
+
+// ---------------- geometry export ----------------
+int splash_geometry_build(const splash_mesh_desc* mesh, int threads, splash_geometry** out) {
+  if (!mesh || !out) return fail(SPLASH_E_INVALID, "NULL argument");
+  *out = nullptr;
+  try {
+    std::unique_ptr<splash_geometry> g(new splash_geometry());
+    g->g = splash::build_ref_geometry(mesh_from_desc(mesh), threads);
+    *out = g.release();
+  } catch (const std::bad_alloc&) {
+    return fail(SPLASH_E_NOMEM, "allocation failed");
+  } catch (const std::exception& e) {
+    return fail(SPLASH_E_MESH, "%s", e.what());
+  }
+  return SPLASH_OK;
+}
+
+int splash_geometry_free(splash_geometry* g) {
+  delete g;
+  return SPLASH_OK;
+}
+
+int splash_geometry_info(const splash_geometry* gh, int64_t sizes[4], double scalars[2]) {
+  if (!gh || !sizes || !scalars) return fail(SPLASH_E_INVALID, "NULL argument");
+  const RefGeometry& g = gh->g;
+  sizes[0] = g.n_vertices;
+  sizes[1] = g.n_faces;
+  sizes[2] = g.n_slots;
+  sizes[3] = g.max_slots;
+  scalars[0] = g.h0;
+  scalars[1] = g.round_diff;
+  return SPLASH_OK;
+}
+
+int splash_geometry_get(const splash_geometry* gh, const char* name, void* dst, size_t bytes,
+                        size_t* written) {
+  if (!gh || !name) return fail(SPLASH_E_INVALID, "NULL argument");
+  const RefGeometry& g = gh->g;
+  const void* src = nullptr;
+  size_t n = 0;
+  auto pick_d = [&](const std::vector<double>& v) { src = v.data(); n = v.size() * sizeof(double); };
+  auto pick_i = [&](const std::vector<int>& v) { src = v.data(); n = v.size() * sizeof(int); };
+  const std::string k(name);
+  if (k == "vertices") pick_d(g.vertices);
+  else if (k == "face_off") pick_i(g.face_off);
+  else if (k == "face_vtx") pick_i(g.face_vtx);
+  else if (k == "nbr_off") pick_i(g.nbr_off);
+  else if (k == "nbr") pick_i(g.nbr);
+  else if (k == "nbr_edge") pick_i(g.nbr_edge);
+  else if (k == "face_centers") pick_d(g.face_centers);
+  else if (k == "normals") pick_d(g.normals);
+  else if (k == "area") pick_d(g.area);
+  else if (k == "edge_normals") pick_d(g.edge_normals);
+  else if (k == "bm_dist") pick_d(g.bm_dist);
+  else if (k == "h_plus") pick_d(g.h_plus);
+  else if (k == "h_minus") pick_d(g.h_minus);
+  else if (k == "ff_plus") pick_i(g.ff_plus);
+  else if (k == "ff_minus") pick_i(g.ff_minus);
+  else if (k == "beta_plus") pick_d(g.beta_plus);
+  else if (k == "beta_minus") pick_d(g.beta_minus);
+  else if (k == "hilbert_order") {
+    // the internal face numbering a solver built on this mesh uses
+    static thread_local std::vector<int> order;
+    order = splash::hilbert_order(g.face_centers.data(), g.n_faces);
+    pick_i(order);
+  }
+  else return fail(SPLASH_E_INVALID, "unknown geometry array '%s'", name);
+  if (written) *written = n;
+  if (dst) {
+    if (bytes < n) return fail(SPLASH_E_INVALID, "buffer too small for '%s' (%zu < %zu)", name, bytes, n);
+    std::memcpy(dst, src, n);
+  }
+  return SPLASH_OK;
+}
+
+}  // extern "C"

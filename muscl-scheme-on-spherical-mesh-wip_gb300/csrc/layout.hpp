@@ -1,0 +1,88 @@
+// Device-resident data layout of one solver instance.
+//
+// Faces are stored in an internal order (a Hilbert curve through the unit
+// face centres) so that the neighbour gathers of a warp touch nearby memory.
+// Per-face arrays have length `fpad` (n_faces rounded up to a multiple of 32).
+// Per-slot arrays (one value per face edge) use "slot planes": the value of
+// slot j of internal face f lives at index j * fpad + f, so a warp of
+// consecutive faces reading slot j issues one coalesced access.  Faces with
+// fewer than max_slots edges (the 12 pentagons of an icosphere_hex mesh)
+// leave their last plane entries unused.
+//
+// Every geometric constant the time step needs is precomputed on the host
+// with the reference's own expression (so the device never re-derives a
+// transcendental of the geometry), converted to the slot-plane layout and
+// uploaded once.
+#pragma once
+
+#include <cstdint>
+
+namespace splash {
+
+constexpr int kDim = 5;          // conserved fields: Sigma, l_x, l_y, l_z, E
+constexpr int kMaxSlots = 6;     // hexagons (pentagons and quads use fewer)
+constexpr int kPartialStride = 8;  // doubles per block partial record
+
+// Physics constants of the adiabatic model (physics/adiabatic.hpp).
+struct PhysParams {
+  double gam;            // 2D adiabatic index (2 - 1/gam3d)
+  double omega_ns;       // star rotation, z axis
+  double e_acc;          // accreted specific energy
+  double omega_acc_x, omega_acc_y, omega_acc_z;  // (0, sin(tilt), cos(tilt)) * omega_acc_abs
+  double alpha;          // friction coefficient
+  double acc_rate;       // accretion rate (depletion without friction)
+  double total_mass;     // initial mass (depletion without friction)
+  double h0;             // minimum edge arc length
+  double round_diff;     // arc/chord of face 0 edge (1,2)
+  int accretion_on;
+  int friction_on;
+  int solver;            // 1 HLLE_p, 2 HLLC, 3 HLLC+
+};
+
+// FP64 geometry, slot planes of length max_slots * fpad unless noted.
+struct DevGeom {
+  int n_faces;
+  int fpad;
+  int max_slots;
+  // per face [fpad]
+  const int8_t* nslots;   // number of edges
+  const double* fcn;      // unit face centre, 3 planes of fpad (x | y | z)
+  const double* area;     // spherical excess
+  const double* acc_src;  // accretion mass source res[0] (0 when accretion is off)
+  // per slot
+  const int* sten;        // 4 planes: flux_faces_plus[0..1], flux_faces_minus[0..1] (internal ids)
+  const double* beta;     // 4 planes: betas_plus[0..1], betas_minus[0..1]
+  const double* hpm;      // 2 planes: H_plus, H_minus
+  const double* bm;       // BM_dist
+  const double* eta;      // 2 planes: H_plus/BM, H_minus/BM
+  const double* arc_a;    // great-circle edge length / face area (limiter Courant factor)
+  const double* ec;       // 3 planes: unit edge centre
+  const double* ecn;      // |ec| as evaluated in double
+  const double* en;       // 3 planes: outward edge normal
+  const double* nxr;      // 3 planes: cross(en, ec/|ec|)
+  const double* chord;    // straight edge length
+  const int* rev;         // slot-plane index of the same edge seen from the neighbour
+};
+
+// Solver state on the device.
+struct DevState {
+  double* U;      // conserved state, kDim planes of fpad
+  double* W0;     // (Sigma, l, Pi) of U, kDim planes
+  double* W1;     // (Sigma, l, Pi) after stage 1, kDim planes
+  double* uplus;  // reconstructed edge states, kDim * max_slots planes of fpad
+  double* partial;  // per-block partial records (kPartialStride doubles)
+  double* scal;   // device scalars, see ScalarSlot
+  unsigned int* err;  // stop bits
+};
+
+enum ScalarSlot : int {
+  kScDt = 0,       // dt of the current step (clipped)
+  kScTime = 1,     // simulation time after the current step
+  kScMaxVel = 2,   // max_vel of the step's input state
+  kScExtraDt = 3,  // extra_dt_constr of the step's input state
+  kScMass = 4,     // 4..8: sum Sigma A, l_x A, l_y A, l_z A, E A of the step's input state
+  kScDt0 = 9,      // dt0 requested by the caller
+  kScCount = 16
+};
+
+}  // namespace splash

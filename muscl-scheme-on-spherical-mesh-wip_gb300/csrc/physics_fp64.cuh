@@ -1,0 +1,238 @@
+// FP64 device physics of the MUSCL step: pressures, edge velocities, the
+// three Riemann solvers, the blended limiter and the accretion source.
+//
+// Each function restates one reference function (cited) with the
+// reference's operand order; the translation unit that includes this header
+// is compiled with -fmad=false so no multiply-add is fused, which keeps the
+// FP64 path within a few ulp of the reference per operation (library
+// transcendentals aside).
+#pragma once
+
+#include <cmath>
+
+#include "layout.hpp"
+
+namespace splash {
+namespace f64 {
+
+struct D3 {
+  double x, y, z;
+};
+
+__device__ __forceinline__ D3 d3(double x, double y, double z) { return D3{x, y, z}; }
+__device__ __forceinline__ D3 sub(D3 a, D3 b) { return D3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ D3 scal(D3 a, double s) { return D3{a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ D3 divs(D3 a, double s) { return D3{a.x / s, a.y / s, a.z / s}; }
+// vec3d.hpp:56-64 : sqrt(((0 + x^2) + y^2) + z^2)
+__device__ __forceinline__ double norm3(D3 a) {
+  double s = a.x * a.x;
+  s = s + a.y * a.y;
+  s = s + a.z * a.z;
+  return sqrt(s);
+}
+__device__ __forceinline__ D3 cross3(D3 a, D3 b) {
+  return D3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ double dot3(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+// std::max / std::min argument semantics
+__device__ __forceinline__ double smax(double a, double b) { return (a < b) ? b : a; }
+__device__ __forceinline__ double smin(double a, double b) { return (b < a) ? b : a; }
+
+// physics/adiabatic.hpp:582-592 (u[4] = energy, vel given)
+__device__ __forceinline__ double pressure(const double* u, double vn, double gam) {
+  return smax(1e-16, (u[4] - u[0] * (vn * vn) / 2) * (gam - 1));
+}
+
+// MUSCL_base.hpp:517-539 (u[4] = energy, r = unit face centre)
+__device__ __forceinline__ double pressure_fc(const double* u, D3 r, double gam) {
+  D3 vel = cross3(r, d3(u[1], u[2], u[3]));
+  vel = divs(vel, -u[0]);
+  const double n = norm3(vel);
+  return smax(1e-16, (u[4] - u[0] * (n * n) / 2) * (gam - 1));
+}
+
+// MUSCL_base.hpp:541-562 (u[4] = pressure, r = unit edge centre)
+__device__ __forceinline__ double energy_at_edge(const double* u, D3 r, double gam) {
+  D3 vel = cross3(r, d3(u[1], u[2], u[3]));
+  vel = divs(vel, -u[0]);
+  const double n = norm3(vel);
+  return 1 / (gam - 1) * u[4] + u[0] * (n * n) / 2;
+}
+
+// Geometry of one slot as the flux functions see it.
+struct SlotGeom {
+  D3 ec;      // unit edge centre
+  double ecn; // |ec|
+  D3 en;      // edge normal
+  D3 nxr;     // cross(en, ec/|ec|)
+};
+
+// velocity at the edge: cross(ec, l) / ((-u0) |ec|)   (adiabatic.hpp:375-376)
+__device__ __forceinline__ D3 edge_vel(const double* u, const SlotGeom& g) {
+  const D3 v = cross3(g.ec, d3(u[1], u[2], u[3]));
+  return divs(v, (-u[0]) * g.ecn);
+}
+
+// physics/adiabatic.hpp:352-392
+__device__ __forceinline__ void phys_flux(const double* u, const SlotGeom& g, double gam,
+                                          double* res) {
+  const D3 vel = edge_vel(u, g);
+  const double PI = pressure(u, norm3(vel), gam);
+  const double ndv = dot3(g.en, vel);
+  res[0] = u[0] * dot3(vel, g.en);
+  res[1] = (u[1] * ndv - g.nxr.x * PI);
+  res[2] = (u[2] * ndv - g.nxr.y * PI);
+  res[3] = (u[3] * ndv - g.nxr.z * PI);
+  res[4] = (u[4] + PI) * dot3(vel, g.en);
+}
+
+// physics/adiabatic.hpp:594-683 ; sets *nan_flag when a wave speed is NaN
+__device__ __forceinline__ void char_vel(const double* uL, const double* uR, const SlotGeom& g,
+                                         double gam, double& S_L, double& S_R, bool& nan_flag) {
+  const D3 vel_l = edge_vel(uL, g);
+  const D3 vel_r = edge_vel(uR, g);
+  const double p_L = pressure(uL, norm3(vel_l), gam);
+  const double p_R = pressure(uR, norm3(vel_r), gam);
+  const double a_L = sqrt(gam * p_L / uL[0]);
+  const double a_R = sqrt(gam * p_R / uR[0]);
+  const double p_pvrs = 1 / 2. * (p_L + p_R) -
+                        1 / 8. * (dot3(g.en, vel_r) - dot3(g.en, vel_l)) * (uL[0] + uR[0]) * (a_L + a_R);
+  const double p_star = smax(0., p_pvrs);
+  double q_R = 1, q_L = 1;
+  if (!(p_star <= p_R)) {
+    q_R = sqrt(1 + (gam + 1) / (2 * gam) * (p_star / p_R - 1));
+    if (isnan(q_R) || isinf(q_R)) q_R = 1;
+  }
+  if (!(p_star <= p_L)) {
+    q_L = sqrt(1 + (gam + 1) / (2 * gam) * (p_star / p_L - 1));
+    if (isnan(q_L) || isinf(q_L)) q_L = 1;
+  }
+  S_L = dot3(vel_l, g.en) - a_L * q_L;
+  S_R = dot3(vel_r, g.en) + a_R * q_R;
+  if (isnan(S_L) || isnan(S_R)) nan_flag = true;
+}
+
+// Riemann fluxes: HLLE_p.hpp:19-58 (solver 1), HLLC.hpp:138-242 (solver 2),
+// HLLCplus.hpp:17-177 (solver 3).  Returns stop bits (STOP_NAN_WAVESPEED,
+// STOP_WAVE_ORDER as in splash_gb300.h).
+__device__ __forceinline__ unsigned flux_star(const double* uL, const double* uR,
+                                              const SlotGeom& g, double gam, int solver,
+                                              double* F) {
+  unsigned bits = 0;
+  bool nan_ws = false;
+  double S_L, S_R;
+  char_vel(uL, uR, g, gam, S_L, S_R, nan_ws);
+  if (nan_ws) bits |= 2u;
+  double FL[kDim], FR[kDim];
+  phys_flux(uL, g, gam, FL);
+  phys_flux(uR, g, gam, FR);
+  if (solver == 1) {
+    if (S_L >= 0) {
+#pragma unroll
+      for (int i = 0; i < kDim; ++i) F[i] = FL[i];
+    } else if (S_L < 0 && S_R > 0) {
+#pragma unroll
+      for (int i = 0; i < kDim; ++i)
+        F[i] = (S_R * FL[i] - S_L * FR[i] + S_R * S_L * (uR[i] - uL[i])) / (S_R - S_L);
+    } else {
+      // S_R <= 0, or NaN wave speeds (reference prints and stops)
+      if (!(S_R <= 0)) bits |= 4u;
+#pragma unroll
+      for (int i = 0; i < kDim; ++i) F[i] = FR[i];
+    }
+    return bits;
+  }
+  const D3 vel_L = edge_vel(uL, g);
+  const D3 vel_R = edge_vel(uR, g);
+  const double rho_R = uR[0];
+  const double rho_L = uL[0];
+  const double p_L = pressure(uL, norm3(vel_L), gam);
+  const double p_R = pressure(uR, norm3(vel_R), gam);
+  const double V_L = dot3(g.en, vel_L);
+  const double V_R = dot3(g.en, vel_R);
+  double S_star = (p_R - p_L + rho_L * V_L * (S_L - V_L) - rho_R * V_R * (S_R - V_R)) /
+                  (rho_L * (S_L - V_L) - rho_R * (S_R - V_R));
+  if (isnan(S_star) || isinf(S_star)) S_star = (V_L + V_R) / 2;
+  const double D[kDim] = {0, -g.nxr.x, -g.nxr.y, -g.nxr.z, S_star};
+  const double P_LR = (p_L + p_R + uL[0] * (S_L - V_L) * (S_star - V_L) +
+                       uR[0] * (S_R - V_R) * (S_star - V_R)) /
+                      2;
+  // branch choice of HLLC.hpp:218-239 / HLLCplus.hpp:153-174
+  int side;  // 0: F_L, 1: F_L*, 2: F_R*, 3: F_R
+  if (S_L >= 0) {
+    side = 0;
+  } else if (S_L < 0 && S_star >= 0) {
+    side = 1;
+  } else if (S_star < 0 && S_R >= 0) {
+    side = 2;
+  } else {
+    if (!(S_R < 0)) bits |= 4u;
+    side = 3;
+  }
+  if (side == 0) {
+#pragma unroll
+    for (int i = 0; i < kDim; ++i) F[i] = FL[i];
+    return bits;
+  }
+  if (side == 3) {
+#pragma unroll
+    for (int i = 0; i < kDim; ++i) F[i] = FR[i];
+    return bits;
+  }
+  const double Sk = (side == 1) ? S_L : S_R;
+  const double* uk = (side == 1) ? uL : uR;
+  const double* Fk = (side == 1) ? FL : FR;
+#pragma unroll
+  for (int i = 0; i < kDim; ++i) F[i] = (S_star * (Sk * uk[i] - Fk[i]) + Sk * P_LR * D[i]) / (Sk - S_star);
+  if (solver == 3) {
+    F[0] = F[0] + 0.0;  // flux_fix[0] = 0 is added like the other fields
+    const double phi_L = uL[0] * (S_L - V_L);
+    const double phi_R = uR[0] * (S_R - V_R);
+    const double a_L = sqrt(gam * p_L / uL[0]);
+    const double a_R = sqrt(gam * p_R / uR[0]);
+    const double M = smin(1., smax(norm3(vel_L) / a_L, norm3(vel_R) / a_R));
+    int lambd_L = 0, lambd_R = 0;
+    if ((V_L - a_L) > 0 && (V_R - a_R) < 0) lambd_L = 1;
+    if ((V_L + a_L) > 0 && (V_R + a_R) < 0) lambd_L = 1;
+    if ((V_R - a_R) > 0 && (V_L - a_L) < 0) lambd_R = 1;
+    if ((V_R + a_R) > 0 && (V_L + a_L) < 0) lambd_R = 1;
+    double f_star = 1;
+    if (lambd_L == 0 && lambd_R == 0) f_star = M * sqrt(4 + (1 - M * M) * (1 - M * M)) / ((1 + M * M));
+    const double h = smin(p_L / p_R, p_R / p_L);
+    const double gsw = 1 - pow(h, M);
+    const double dV = V_R - V_L;
+    const D3 dv = sub(vel_R, vel_L);
+    const double cs = Sk / (Sk - S_star) * gsw;
+    const D3 vff = d3((f_star - 1) * dV * g.en.x + cs * (dv.x - dV * g.en.x),
+                      (f_star - 1) * dV * g.en.y + cs * (dv.y - dV * g.en.y),
+                      (f_star - 1) * dV * g.en.z + cs * (dv.z - dV * g.en.z));
+    const D3 am = cross3(g.ec, vff);
+    F[1] = F[1] + am.x * phi_L * phi_R / (phi_R - phi_L);
+    F[2] = F[2] + am.y * phi_L * phi_R / (phi_R - phi_L);
+    F[3] = F[3] + am.z * phi_L * phi_R / (phi_R - phi_L);
+    F[4] = F[4] + (f_star - 1) * (V_R - V_L) * S_star * phi_L * phi_R / (phi_R - phi_L);
+  }
+  return bits;
+}
+
+// h(r) switch of physics/adiabatic.hpp:692-702
+__device__ __forceinline__ double limiter_switch(double r) {
+  double o = 0;
+  if (r < 1 && r > 0) o = (1 - tanh(4 * (r * r) * pow(1 - r, 0.1)));
+  if (r >= 1) o = pow(tanh(10 * pow(r - 1, 3.0)), 6.0);
+  return o;
+}
+
+// physics/adiabatic.hpp:685-828 for one field: blend of the third-order
+// limiter and the irregular-grid superbee, NaN ratio -> 0.
+__device__ __forceinline__ double limiter_field(double r, double nu_plus, double eta_p,
+                                                double eta_m, double twoN) {
+  if (isnan(r)) return 0.0;
+  const double sb = smax(0., smax(smin(1., eta_m * r / (twoN * nu_plus)), smin(r, eta_p)));
+  const double to = smax(0., smin(sb, 1 + (1 + nu_plus) / 3 * (r - 1)));
+  const double hv = limiter_switch(r);
+  return ((1 - hv) * to + hv * sb);
+}
+
+}  // namespace f64
+}  // namespace splash

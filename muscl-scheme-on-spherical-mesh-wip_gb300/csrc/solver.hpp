@@ -1,0 +1,72 @@
+// One solver instance: the host mirror of the reference object
+// (MUSCL_base + adiabatic + a Riemann solver) with its device state.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+#include "geometry.hpp"
+#include "layout.hpp"
+#include "splash_gb300.h"
+
+namespace splash {
+
+// True when the FP32/FP64 mixed kernels are compiled into the library.
+bool mixed_available();
+
+struct Solver {
+  // configuration
+  splash_params par{};
+  bool accretion_on = false;
+  int precision = SPLASH_PREC_FP64;
+  int solver_kind = SPLASH_SOLVER_HLLCPLUS;
+  int device = -1;
+  double area_coeff = 0.0;
+  double total_mass = 0.0;
+
+  // sizes
+  int n_faces = 0;
+  int fpad = 0;
+  int max_slots = 0;
+  int n_partials = 0;
+  size_t geometry_bytes = 0;
+
+  // numbering: perm[internal] = reference face id, iperm = inverse
+  std::vector<int> perm, iperm;
+
+  // reference-order host copies used by the writers
+  std::vector<double> wr_vertices, wr_face_centers, wr_area;
+  std::vector<int> wr_face_off, wr_face_vtx;
+
+  // device
+  cudaStream_t stream = nullptr;
+  PhysParams P{};
+  DevGeom G{};
+  DevState S{};
+  double* d_stage = nullptr;  // [n_faces][5] reference-order staging
+  int* d_perm = nullptr;
+  double* h_stage = nullptr;  // pinned mirror of d_stage
+  std::vector<void*> dev_allocs;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  int64_t steps = 0;
+
+  ~Solver();
+
+  template <typename T>
+  T* dalloc(size_t n);
+  template <typename T>
+  T* upload(const std::vector<T>& h);
+
+  void build_device_geometry(const RefGeometry& g);
+  int upload_state(const double* U_ref);
+  int download_state(double* U_ref);
+  int read_scalars(double* out);
+  int capture_graph();
+  int step(double dt0);
+  static int check_cuda(cudaError_t e, const char* what);
+};
+
+}  // namespace splash

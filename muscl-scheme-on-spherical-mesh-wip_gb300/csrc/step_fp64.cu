@@ -1,0 +1,414 @@
+// FP64 kernels of the MUSCL time step (the reference method in FP64).
+//
+// One do_step(dt0) (MUSCL_base/MUSCL_base.hpp:97-225) is five launches on
+// one stream, captured once into a CUDA graph by the host:
+//
+//   dt_kernel          1 block  : reduce the previous launch's per-block
+//                                 partials -> max_vel, extra_dt, clipped dt,
+//                                 time; diagnostics sums
+//   reconstruct(W0)    per face : limited edge states of every slot
+//   flux_update(1)     per face : Riemann fluxes, source, res2d(dt/2) + U0
+//                                 -> W1 (Sigma, l, Pi)
+//   reconstruct(W1)    per face
+//   flux_update(2)     per face : res2d(dt) + U0 -> U, W0 for the next step,
+//                                 per-block partials of the new state
+//
+// Per-face threads loop over the face's slots in the reference slot order,
+// so the flux divergence accumulates in exactly the reference order.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "kernels.hpp"
+#include "physics_fp64.cuh"
+
+namespace splash {
+namespace f64 {
+namespace {
+
+constexpr int kBlock = 128;
+
+__device__ __forceinline__ D3 plane3(const double* p, int stride, int i) {
+  return D3{p[i], p[stride + i], p[2 * stride + i]};
+}
+
+// Warp + block reduction of one partial record; thread 0 of the block
+// writes it.  Fixed tree order, so the result is deterministic.
+__device__ void block_partials(double vmax, double dmin, const double sums[5], double* out) {
+  __shared__ double sm[kBlock / 32][7];
+  double v[7] = {vmax, dmin, sums[0], sums[1], sums[2], sums[3], sums[4]};
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double a = __shfl_down_sync(0xffffffffu, v[0], o);
+    const double b = __shfl_down_sync(0xffffffffu, v[1], o);
+    v[0] = fmax(v[0], a);
+    v[1] = fmin(v[1], b);
+#pragma unroll
+    for (int k = 2; k < 7; ++k) v[k] = v[k] + __shfl_down_sync(0xffffffffu, v[k], o);
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < 7; ++k) sm[warp][k] = v[k];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r[7];
+#pragma unroll
+    for (int k = 0; k < 7; ++k) r[k] = sm[0][k];
+    for (int w = 1; w < kBlock / 32; ++w) {
+      r[0] = fmax(r[0], sm[w][0]);
+      r[1] = fmin(r[1], sm[w][1]);
+#pragma unroll
+      for (int k = 2; k < 7; ++k) r[k] = r[k] + sm[w][k];
+    }
+#pragma unroll
+    for (int k = 0; k < 7; ++k) out[k] = r[k];
+  }
+}
+
+// Per-face contributions to the dt clip of the NEXT step and to the
+// diagnostics sums, for a conserved state u (u[4] = energy):
+// find_v_max (MUSCL_base.hpp:311-343) and extra_dt_constr
+// (physics/adiabatic.hpp:543-580).
+__device__ __forceinline__ void dt_candidates(const double* u, D3 r, double area,
+                                              const PhysParams& P, double& vmax,
+                                              double& dmin, double sums[5]) {
+  D3 vpos = cross3(r, d3(u[1], u[2], u[3]));
+  vpos = divs(vpos, u[0]);
+  const double vn = norm3(vpos);
+  const double p = pressure_fc(u, r, P.gam);
+  const double c_s = sqrt(P.gam * p / u[0]);
+  vmax = fmax(vn, c_s);
+  // extra_dt_constr
+  D3 vel = cross3(r, d3(u[1], u[2], u[3]));
+  vel = divs(vel, -u[0]);
+  const D3 omega0 = d3(0, 0, P.omega_ns);
+  const D3 vel0 = cross3(omega0, r);
+  const double nvel = norm3(vel);
+  const double press = pressure(u, nvel, P.gam);
+  const double gam3d = 1 / (2 - P.gam);
+  const double GM = 0.217909;
+  const double g_eff = GM - nvel * nvel;
+  const double rho = gam3d / (2 * gam3d - 1) * g_eff * u[0] * u[0] / press;
+  dmin = 0.01 * u[0] / (P.alpha * rho * norm3(sub(vel, vel0)));
+#pragma unroll
+  for (int k = 0; k < 5; ++k) sums[k] = u[k] * area;
+}
+
+// physics/adiabatic.hpp:396-541 ; w[4] is the pressure
+__device__ __forceinline__ void source_term(const double* w, D3 fcn, double acc0,
+                                            const PhysParams& P, double* res) {
+#pragma unroll
+  for (int i = 0; i < kDim; ++i) res[i] = 0;
+  if (!P.accretion_on) return;
+  D3 vel = cross3(fcn, d3(w[1], w[2], w[3]));
+  vel = divs(vel, -w[0]);
+  res[0] = acc0;
+  const D3 omega_acc = d3(P.omega_acc_x, P.omega_acc_y, P.omega_acc_z);
+  const D3 omxr = cross3(omega_acc, fcn);
+  D3 rxv = cross3(fcn, omxr);
+  res[1] = res[0] * rxv.x;
+  res[2] = res[0] * rxv.y;
+  res[3] = res[0] * rxv.z;
+  const double nd = norm3(sub(omxr, vel));
+  res[4] = res[0] * (P.e_acc + (nd * nd) / 2.);
+  rxv = cross3(fcn, vel);
+  const double nvel = norm3(vel);
+  if (!P.friction_on) {
+    const double fall_eff = 1;
+    const double dmdt = -(fall_eff * P.acc_rate * 4 * M_PI) / P.total_mass * w[0];
+    res[0] += dmdt;
+    res[1] += dmdt * rxv.x;
+    res[2] += dmdt * rxv.y;
+    res[3] += dmdt * rxv.z;
+    res[4] += dmdt * (P.gam / (P.gam - 1) * w[4] / w[0] + (nvel * nvel) / 2.);
+  }
+  const double GM = 0.217909;
+  const double g_eff = GM - nvel * nvel;
+  const double c_sigma = 4.85e36;
+  const double k_m = 1.6e-13;
+  const double kappa = 3.4e6;
+  const double C = 12. / 5 * k_m * w[0] / w[4] * pow(3. / 4 * c_sigma * g_eff * w[0], 1. / 4);
+  const double beta_switch = 0.736194670678821;
+  const double C_switch = -1 - 1 / (beta_switch - 1);
+  double beta;
+  if (C <= C_switch)
+    beta = 1 - 1 / (1 + C);
+  else
+    beta = 1 - pow(2 / C, 4.0);
+  const double beta_ceil = 1 - 1e-8, beta_floor = 1e-8;
+  if (beta < beta_floor || isnan(beta)) beta = beta_floor;
+  if (beta > beta_ceil) beta = beta_ceil;
+  res[4] -= g_eff / kappa * (1 - beta);
+  if (P.friction_on) {
+    const double gam3d = 1 / (2 - P.gam);
+    const double rho = gam3d / (2 * gam3d - 1) * g_eff * w[0] * w[0] / w[4];
+    const D3 omega0 = d3(0, 0, P.omega_ns);
+    const D3 vel0 = cross3(omega0, fcn);
+    const double dv = norm3(sub(vel, vel0));
+    const D3 wr = scal(sub(vel, vel0), -P.alpha * rho * dv);
+    const D3 l_fr = cross3(fcn, wr);
+    res[1] += l_fr.x;
+    res[2] += l_fr.y;
+    res[3] += l_fr.z;
+    res[4] += dot3(wr, vel0);
+    res[0] -= P.alpha * rho * dv;
+    res[1] -= P.alpha * rho * dv / w[0] * w[1];
+    res[2] -= P.alpha * rho * dv / w[0] * w[2];
+    res[3] -= P.alpha * rho * dv / w[0] * w[3];
+    res[4] -= P.alpha * rho * dv * (nvel * nvel / 2. + w[4] * P.gam / ((P.gam - 1) * w[0]));
+  }
+}
+
+// ---------------------------------------------------------------------
+// W = (Sigma, l, Pi) of the conserved state and the partials of it
+// (used once after the state is set; afterwards flux_update stage 2
+// produces both).
+__global__ void __launch_bounds__(kBlock) prepare_kernel(DevGeom G, DevState S, PhysParams P) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  double vmax = 0.0, dmin = 1e20, sums[5] = {0, 0, 0, 0, 0};
+  if (f < G.n_faces) {
+    double u[kDim];
+#pragma unroll
+    for (int k = 0; k < kDim; ++k) u[k] = S.U[k * G.fpad + f];
+    const D3 r = plane3(G.fcn, G.fpad, f);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) S.W0[k * G.fpad + f] = u[k] - 0.0;
+    S.W0[4 * G.fpad + f] = pressure_fc(u, r, P.gam) - 0.0;
+    dt_candidates(u, r, G.area[f], P, vmax, dmin, sums);
+  }
+  block_partials(vmax, dmin, sums, S.partial + (size_t)blockIdx.x * kPartialStride);
+}
+
+// dt = min(dt0, 0.1 h0 / max_vel, extra_dt)  (MUSCL_base.hpp:100-115)
+__global__ void __launch_bounds__(256) dt_kernel(DevState S, PhysParams P, int nblocks) {
+  __shared__ double sm[256][7];
+  double v[7] = {1e-8, 1e20, 0, 0, 0, 0, 0};
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+    const double* p = S.partial + (size_t)b * kPartialStride;
+    v[0] = fmax(v[0], p[0]);
+    v[1] = fmin(v[1], p[1]);
+#pragma unroll
+    for (int k = 2; k < 7; ++k) v[k] = v[k] + p[k];
+  }
+#pragma unroll
+  for (int k = 0; k < 7; ++k) sm[threadIdx.x][k] = v[k];
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      sm[threadIdx.x][0] = fmax(sm[threadIdx.x][0], sm[threadIdx.x + s][0]);
+      sm[threadIdx.x][1] = fmin(sm[threadIdx.x][1], sm[threadIdx.x + s][1]);
+#pragma unroll
+      for (int k = 2; k < 7; ++k) sm[threadIdx.x][k] = sm[threadIdx.x][k] + sm[threadIdx.x + s][k];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double max_vel = sm[0][0];
+    double extra = sm[0][1];
+    if (extra < 0) {
+      atomicOr(S.err, 8u);  // SPLASH_STOP_NEG_EXTRA_DT
+      extra = 1e20;
+    }
+    double dt = S.scal[kScDt0];
+    if (dt > P.h0 * 0.1 / max_vel) dt = P.h0 * 0.1 / max_vel;
+    if (dt > extra) dt = extra;
+    S.scal[kScDt] = dt;
+    S.scal[kScMaxVel] = max_vel;
+    S.scal[kScExtraDt] = extra;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) S.scal[kScMass + k] = sm[0][2 + k];
+    S.scal[kScTime] = S.scal[kScTime] + dt;
+  }
+}
+
+// find_U_edges (MUSCL_base.hpp:361-434) for every slot of one face.
+__global__ void __launch_bounds__(kBlock) reconstruct_kernel(DevGeom G, const double* __restrict__ W,
+                                                             double* __restrict__ uplus,
+                                                             const double* __restrict__ scal,
+                                                             PhysParams P) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= G.n_faces) return;
+  const int fp = G.fpad;
+  const int PS = G.max_slots * fp;  // one slot-plane set
+  const double dt = scal[kScDt];
+  double w[kDim];
+#pragma unroll
+  for (int k = 0; k < kDim; ++k) w[k] = W[k * fp + f];
+  const int n = G.nslots[f];
+  const double twoN = (double)(2 * n);
+  const double gam = P.gam;
+  for (int j = 0; j < n; ++j) {
+    const int s = j * fp + f;
+    const int ia = G.sten[s], ib = G.sten[PS + s], ic = G.sten[2 * PS + s], id = G.sten[3 * PS + s];
+    const double bp0 = G.beta[s], bp1 = G.beta[PS + s], bm0 = G.beta[2 * PS + s], bm1 = G.beta[3 * PS + s];
+    const double hp = G.hpm[s], hm = G.hpm[PS + s], bmd = G.bm[s];
+    double pp[kDim], r[kDim];
+#pragma unroll
+    for (int k = 0; k < kDim; ++k) {
+      const double* Wk = W + k * fp;
+      const double Up = bp0 * Wk[ia] + bp1 * Wk[ib];
+      pp[k] = (Up - w[k]) / hp;
+      const double Um = bm0 * Wk[ic] + bm1 * Wk[id];
+      const double pm = (-Um + w[k]) / hm;
+      r[k] = pm / pp[k];
+    }
+    // Courant factor of the limiter (adiabatic.hpp:741-758, 792-810)
+    const D3 ec = plane3(G.ec, PS, s);
+    const double ecn = G.ecn[s];
+    const D3 en = plane3(G.en, PS, s);
+    D3 vel = cross3(ec, d3(w[1], w[2], w[3]));
+    vel = divs(vel, (-w[0] - 0.0) * ecn);
+    const double p = w[4] + 0.0;
+    const double c = sqrt(gam * p / (w[0] + 0.0));
+    const double nu_plus = (c + dot3(vel, en)) * dt * G.arc_a[s];
+    const double eta_p = G.eta[s], eta_m = G.eta[PS + s];
+    double up[kDim];
+#pragma unroll
+    for (int k = 0; k < kDim; ++k) {
+      const double lim = limiter_field(r[k], nu_plus, eta_p, eta_m, twoN);
+      if (k == 0 || k == 4)
+        up[k] = w[k] + 0.0 + pp[k] * lim * bmd;
+      else
+        up[k] = w[k] + pp[k] * lim * bmd;
+    }
+    up[4] = energy_at_edge(up, ec, gam);  // Pi -> E at the edge centre
+#pragma unroll
+    for (int k = 0; k < kDim; ++k) uplus[k * PS + s] = up[k];
+  }
+}
+
+// find_flux_var + res2d + the RK combine with the density floor
+// (MUSCL_base.hpp:345-359, 238-276, 124-161).  stage 1: dt_here = dt/2,
+// writes W1; stage 2: dt_here = dt, writes U, W0 and the partials.
+template <int STAGE>
+__global__ void __launch_bounds__(kBlock) flux_update_kernel(DevGeom G, DevState S, PhysParams P) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  double vmax = 0.0, dmin = 1e20, sums[5] = {0, 0, 0, 0, 0};
+  if (f < G.n_faces) {
+    const int fp = G.fpad;
+    const int PS = G.max_slots * fp;
+    const double dt = S.scal[kScDt];
+    const double dt_here = (STAGE == 1) ? dt / 2 : dt;
+    const double* Win = (STAGE == 1) ? S.W0 : S.W1;
+    const D3 fcn = plane3(G.fcn, fp, f);
+    const double area = G.area[f];
+    double w[kDim], acc[kDim];
+#pragma unroll
+    for (int k = 0; k < kDim; ++k) w[k] = Win[k * fp + f];
+    source_term(w, fcn, G.acc_src[f], P, acc);
+#pragma unroll
+    for (int k = 0; k < kDim; ++k) acc[k] = dt_here * acc[k];
+    const double rd_dt = P.round_diff * dt_here;
+    const int n = G.nslots[f];
+    unsigned bits = 0;
+    for (int j = 0; j < n; ++j) {
+      const int s = j * fp + f;
+      const int rv = G.rev[s];
+      double uL[kDim], uR[kDim], F[kDim];
+#pragma unroll
+      for (int k = 0; k < kDim; ++k) {
+        uL[k] = S.uplus[k * PS + s];
+        uR[k] = S.uplus[k * PS + rv];
+      }
+      SlotGeom g;
+      g.ec = plane3(G.ec, PS, s);
+      g.ecn = G.ecn[s];
+      g.en = plane3(G.en, PS, s);
+      g.nxr = plane3(G.nxr, PS, s);
+      bits |= flux_star(uL, uR, g, P.gam, P.solver, F);
+      const double coef = rd_dt * G.chord[s] / area;
+#pragma unroll
+      for (int k = 0; k < kDim; ++k) {
+        if (isnan(F[k])) bits |= 1u;
+        acc[k] -= coef * F[k];
+      }
+    }
+    if (bits) atomicOr(S.err, bits);
+    double u[kDim];
+#pragma unroll
+    for (int k = 0; k < kDim; ++k) u[k] = acc[k] + S.U[k * fp + f];
+    if (u[0] < 1e-8) u[0] = 1e-8;
+    double* Wout = (STAGE == 1) ? S.W1 : S.W0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) Wout[k * fp + f] = u[k] - 0.0;
+    Wout[4 * fp + f] = pressure_fc(u, fcn, P.gam) - 0.0;
+    if (STAGE == 2) {
+#pragma unroll
+      for (int k = 0; k < kDim; ++k) S.U[k * fp + f] = u[k];
+      dt_candidates(u, fcn, area, P, vmax, dmin, sums);
+    }
+  }
+  if (STAGE == 2) block_partials(vmax, dmin, sums, S.partial + (size_t)blockIdx.x * kPartialStride);
+}
+
+__global__ void set_scalar_kernel(double* dst, double v) { *dst = v; }
+
+// reference order [F][dim] <-> internal planes
+__global__ void scatter_state_kernel(const double* __restrict__ aos, const int* __restrict__ perm,
+                                     double* __restrict__ U, int n_faces, int fpad) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_faces) return;
+  const int r = perm[i];
+#pragma unroll
+  for (int k = 0; k < kDim; ++k) U[k * fpad + i] = aos[(size_t)r * kDim + k];
+}
+__global__ void gather_state_kernel(const double* __restrict__ U, const int* __restrict__ perm,
+                                    double* __restrict__ aos, int n_faces, int fpad) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_faces) return;
+  const int r = perm[i];
+#pragma unroll
+  for (int k = 0; k < kDim; ++k) aos[(size_t)r * kDim + k] = U[k * fpad + i];
+}
+
+inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
+
+}  // namespace
+}  // namespace f64
+
+// ---- launchers (declared in kernels.hpp) --------------------------------
+int fp64_partial_blocks(int n_faces) { return f64::blocks_for(n_faces); }
+
+cudaError_t fp64_prepare(const DevGeom& G, const DevState& S, const PhysParams& P,
+                         cudaStream_t st) {
+  f64::prepare_kernel<<<f64::blocks_for(G.n_faces), f64::kBlock, 0, st>>>(G, S, P);
+  return cudaGetLastError();
+}
+
+cudaError_t fp64_set_dt0(const DevState& S, double dt0, cudaStream_t st) {
+  f64::set_scalar_kernel<<<1, 1, 0, st>>>(S.scal + kScDt0, dt0);
+  return cudaGetLastError();
+}
+
+cudaError_t fp64_step(const DevGeom& G, const DevState& S, const PhysParams& P, cudaStream_t st,
+                      cudaEvent_t* ev) {
+  const int nb = f64::blocks_for(G.n_faces);
+  if (ev) cudaEventRecord(ev[0], st);
+  f64::dt_kernel<<<1, 256, 0, st>>>(S, P, nb);
+  if (ev) cudaEventRecord(ev[1], st);
+  f64::reconstruct_kernel<<<nb, f64::kBlock, 0, st>>>(G, S.W0, S.uplus, S.scal, P);
+  if (ev) cudaEventRecord(ev[2], st);
+  f64::flux_update_kernel<1><<<nb, f64::kBlock, 0, st>>>(G, S, P);
+  if (ev) cudaEventRecord(ev[3], st);
+  f64::reconstruct_kernel<<<nb, f64::kBlock, 0, st>>>(G, S.W1, S.uplus, S.scal, P);
+  if (ev) cudaEventRecord(ev[4], st);
+  f64::flux_update_kernel<2><<<nb, f64::kBlock, 0, st>>>(G, S, P);
+  if (ev) cudaEventRecord(ev[5], st);
+  return cudaGetLastError();
+}
+
+cudaError_t fp64_scatter_state(const double* aos, const int* perm, double* U, int n_faces,
+                               int fpad, cudaStream_t st) {
+  f64::scatter_state_kernel<<<f64::blocks_for(n_faces), f64::kBlock, 0, st>>>(aos, perm, U, n_faces, fpad);
+  return cudaGetLastError();
+}
+
+cudaError_t fp64_gather_state(const double* U, const int* perm, double* aos, int n_faces,
+                              int fpad, cudaStream_t st) {
+  f64::gather_state_kernel<<<f64::blocks_for(n_faces), f64::kBlock, 0, st>>>(U, perm, aos, n_faces, fpad);
+  return cudaGetLastError();
+}
+
+}  // namespace splash
