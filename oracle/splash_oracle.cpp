@@ -544,14 +544,16 @@ struct Oracle {
     stop_check = stop_before || stop_check;
     if (dt > extra_dt) dt = extra_dt;
 
+    // stop bits as in include/splash_gb300.h: 1 NaN flux, 2 NaN wave
+    // speed, 4 wave ordering, 8 negative extra dt
     find_U_edges();
     int fb = find_flux_var();
-    if (res2d(dt / 2)) bits |= 16;
+    if (res2d(dt / 2)) bits |= 1;
     combine();
 
     find_U_edges();
     fb |= find_flux_var();
-    if (res2d(dt)) bits |= 16;
+    if (res2d(dt)) bits |= 1;
     combine();
 
     if (fb & 1) bits |= 2;

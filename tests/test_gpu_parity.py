@@ -102,13 +102,25 @@ def test_stop_flag_bits_negative_extra_dt():
     assert s.error_word() & sg.STOP_NEG_EXTRA_DT
 
 
-def test_nan_input_raises_stop_flag():
-    """A NaN planted in the host input state (never on the device) reaches
-    the flux and latches the NaN-flux bit, like MUSCL_base.hpp:264-268."""
+@pytest.mark.parametrize("field", [0, 4])
+def test_nan_input_stop_flag_matches_reference(field):
+    """A NaN planted in the host input state (never on the device).  In the
+    density it reaches the fluxes and latches the stop flag
+    (MUSCL_base.hpp:264-268, adiabatic.hpp:671-676); in the energy the
+    pressure floor swallows it (MUSCL_base.hpp:538) and the reference does not
+    stop.  The GPU error word must equal the oracle's stop bits."""
+    import splash_gb300 as sg
+
     c = load("state_hex3_hllc_acc.npz")
-    s = gpu_solver(c)
     U = c["U0"].copy()
-    U[5, 4] = np.nan
+    U[5, field] = np.nan
+    c2 = dict(c)
+    c2["U0"] = U
+    o = make_oracle(sg.Geometry(mesh_of("hex", 3)), c2)
+    bits = o.do_step(1e-3)
+    s = gpu_solver(c)
     s.set_state(U)
     s.do_step(1e-3)
-    assert s.get_stop_check()
+    assert s.error_word() == bits
+    assert s.get_stop_check() == (field == 0)
+    assert np.array_equal(np.isnan(s.get_state()), np.isnan(o.get_state()))
