@@ -170,6 +170,24 @@ def cpu_baseline(geom, U0, gam, budget_s=15.0):
                       f"({dt:.1f} s, OpenMP {cores} threads, {platform.machine()})"}
 
 
+def algorithmic_bytes_mixed(geom, kernel: str) -> float:
+    """Compulsory bytes per launch of one kernel of the mixed path.
+
+    reconstruct: read W32 (5 x 4 B per face); per slot 4 int32 stencil ids,
+      4 betas, 1/H+, 1/H-, BM, edge centre (3), normal (3), Courant factor,
+      2 eta (all FP32) ; write U+ (5 x 4 B per slot).
+    flux_update: read U+ (5 x 4 B per slot, once algorithmically); per slot
+      edge centre, normal, n x R (9 x 4 B), the FP64 flux coefficient and the
+      reverse index; per face W32, U0 (FP64), unit centre (FP32 + FP64), area,
+      accretion source ; write U (FP64) and W32.
+    """
+    F = geom.n_faces
+    S = geom.n_slots
+    if kernel == "reconstruct":
+        return F * 20 + S * (16 + 4 * (4 + 2 + 1 + 3 + 3 + 1 + 2)) + S * 20
+    return S * 20 + S * (9 * 4 + 8 + 4) + F * (20 + 40 + 12 + 24 + 8 + 8) + F * (40 + 20)
+
+
 def algorithmic_bytes(geom, kernel: str) -> float:
     """Compulsory bytes per launch of one kernel of the FP64 path.
 
@@ -189,6 +207,12 @@ def algorithmic_bytes(geom, kernel: str) -> float:
 
 
 # ------------------------------------------------------------------ arms
+def l1_rel(a, b, area):
+    num = np.sum(area[:, None] * np.abs(a - b), axis=0)
+    den = np.sum(area[:, None] * np.abs(b), axis=0)
+    return num / np.where(den > 0, den, 1)
+
+
 def run_ours(args):
     import torch
 
@@ -204,57 +228,71 @@ def run_ours(args):
     torch.cuda.set_device(local)
     mesh, geom, gam, U0 = build_case(sg)
     params = sg.SolverParams(**PARAMS)
-    prec = sg.PREC_FP64
-    prec_name = "fp64"
-    solver = sg.MUSCL_HLLCplus(mesh, U0, 5, gam, 0.0, True, params=params, precision=prec,
-                               device=local)
     F = geom.n_faces
+    mixed = sg.MUSCL_HLLCplus(mesh, U0, 5, gam, 0.0, True, params=params, precision=sg.PREC_MIXED,
+                              device=local)
+    fp64 = sg.MUSCL_HLLCplus(mesh, U0, 5, gam, 0.0, True, params=params, precision=sg.PREC_FP64,
+                             device=local)
     # one replica per GPU (the step does not shard)
     with ClockSampler(local) as clocks:
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
-        secs = time_device(sg, torch, solver, F, args.steps, args.warmup)
+        secs = time_device(sg, torch, mixed, F, args.steps, args.warmup)
         if world > 1:
             t = torch.tensor([secs], device="cuda")
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             secs = float(t.item())
     clk = clocks.summary()
     value = F * args.steps * world / secs
+    secs64 = time_device(sg, torch, fp64, F, args.steps, args.warmup)
+    value64 = F * args.steps / secs64
+    # accuracy of the timed runs: both advanced warmup + steps from the same state
+    Um, U64 = mixed.get_state(), fp64.get_state()
+    acc = {"steps": args.warmup + args.steps, "l1_rel_per_field": l1_rel(Um, U64, geom["area"]).tolist(),
+           "linf_rel_per_field": (np.max(np.abs(Um - U64), axis=0) /
+                                  np.max(np.abs(U64), axis=0)).tolist(),
+           "reference": "GPU FP64 path (1e-10 of the reference on the golden states)"}
     # per-kernel device times (un-captured launches, CUDA events on the solver stream)
-    ms = solver.kernel_times(max(3, min(20, args.steps)), DT0)
-    names = ["dt_reduce", "reconstruct", "flux_update", "reconstruct", "flux_update"]
-    per_kernel = {"dt_reduce": ms[0], "reconstruct": (ms[1] + ms[3]) / 2,
-                  "flux_update": (ms[2] + ms[4]) / 2}
-    dom = max(("reconstruct", "flux_update"), key=lambda k: per_kernel[k])
+    reps = max(3, min(20, args.steps))
+    ms = mixed.kernel_times(reps, DT0)
+    ms64 = fp64.kernel_times(reps, DT0)
+    kern = {"dt_reduce": ms[0], "reconstruct": (ms[1] + ms[3]) / 2, "flux_update": (ms[2] + ms[4]) / 2}
+    kern64 = {"dt_reduce": ms64[0], "reconstruct": (ms64[1] + ms64[3]) / 2,
+              "flux_update": (ms64[2] + ms64[4]) / 2}
+    dom = max(("reconstruct", "flux_update"), key=lambda k: kern[k])
     hbm, src = peaks()
-    ach = algorithmic_bytes(geom, dom) / (per_kernel[dom] * 1e-3) / 1e9
-    geo_b, st_b = solver.memory()
+    ach = algorithmic_bytes_mixed(geom, dom) / (kern[dom] * 1e-3) / 1e9
+    geo_b, st_b = mixed.memory()
     # end to end through the C ABI with host buffers
-    U_host = solver.get_state()
+    U_host = mixed.get_state()
     e2e_steps = max(3, min(args.steps, 50))
-    e2e_secs = time_e2e(sg, solver, U_host, e2e_steps)
+    e2e_secs = time_e2e(sg, mixed, U_host, e2e_steps)
     bytes_io = F * 5 * 8
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {**workload_config(F, prec_name), "parallelism": f"replicas{world}",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {**workload_config(F, "mixed FP32/FP64"), "parallelism": f"replicas{world}",
                    "working_set_mb": round((geo_b + st_b) / 2**20, 1)},
         "gpu_launches": 5 * args.steps,
         "e2e": {"value": F * e2e_steps / e2e_secs, "unit": METRIC, "h2d_bytes_per_step": bytes_io,
                 "d2h_bytes_per_step": bytes_io},
+        "fp64": {"value": value64, "ms_per_step": secs64 / args.steps * 1e3, "kernel_ms": kern64},
+        "mixed_over_fp64": value / value64,
+        "accuracy": acc,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm,
                      "unit": "GB/s", "frac": ach / hbm, "traffic": None,
-                     "peak_source": f"{src} MEASURED_PEAKS.json hbm_gbs" if src == "measured" else src,
-                     "kernel_ms": per_kernel},
+                     "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)",
+                     "kernel_ms": kern},
         "clocks": clk,
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(geom, U0, gam)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    solver.close()
+    mixed.close()
+    fp64.close()
     if world > 1:
         torch.distributed.destroy_process_group()
 

@@ -243,6 +243,51 @@ void Solver::build_device_geometry(const RefGeometry& g) {
     }
   }
 
+  if (precision == SPLASH_PREC_MIXED) {
+    // FP32 slot planes; FP64 for the values feeding FP64 steps
+    auto tof = [](const std::vector<double>& v) { return std::vector<float>(v.begin(), v.end()); };
+    std::vector<float> h_invh(2 * PS, 1.0f);
+    std::vector<double> h_coef(PS, 0.0);
+    for (size_t q = 0; q < PS; ++q) {
+      h_invh[q] = (float)(1.0 / h_hpm[q]);
+      h_invh[PS + q] = (float)(1.0 / h_hpm[PS + q]);
+    }
+    for (int i = 0; i < nf; ++i)
+      for (int j = 0; j < (int)h_nslots[i]; ++j) {
+        const size_t q = (size_t)j * fpad + i;
+        h_coef[q] = g.round_diff * h_chord[q] / h_area[i];
+      }
+    GM.n_faces = nf;
+    GM.fpad = fpad;
+    GM.max_slots = max_slots;
+    GM.nslots = upload(h_nslots);
+    GM.fcn = upload(h_fcn);
+    GM.fcn32 = upload(tof(h_fcn));
+    GM.area = upload(h_area);
+    GM.acc_src = upload(h_acc);
+    GM.sten = upload(h_sten);
+    GM.beta = upload(tof(h_beta));
+    GM.inv_h = upload(h_invh);
+    GM.bm = upload(tof(h_bm));
+    GM.eta = upload(tof(h_eta));
+    GM.arc_a = upload(tof(h_arc));
+    GM.ec = upload(tof(h_ec));
+    GM.en = upload(tof(h_en));
+    GM.nxr = upload(tof(h_nxr));
+    GM.coef = upload(h_coef);
+    GM.rev = upload(h_rev);
+    geometry_bytes = h_nslots.size() + 8 * (h_fcn.size() + h_area.size() + h_acc.size() + h_coef.size()) +
+                     4 * (h_fcn.size() + h_sten.size() + h_rev.size() + h_beta.size() + h_invh.size() +
+                          h_bm.size() + h_eta.size() + h_arc.size() + h_ec.size() + h_en.size() +
+                          h_nxr.size());
+    wr_vertices = g.vertices;
+    wr_face_off = g.face_off;
+    wr_face_vtx = g.face_vtx;
+    wr_face_centers = g.face_centers;
+    wr_area = g.area;
+    return;
+  }
+
   G.n_faces = nf;
   G.fpad = fpad;
   G.max_slots = max_slots;
@@ -276,12 +321,21 @@ void Solver::build_device_geometry(const RefGeometry& g) {
   wr_area = g.area;
 }
 
+cudaError_t Solver::launch_prepare() {
+  return precision == SPLASH_PREC_MIXED ? mixed_prepare(GM, S, P, stream) : fp64_prepare(G, S, P, stream);
+}
+
+cudaError_t Solver::launch_step(cudaEvent_t* ev) {
+  return precision == SPLASH_PREC_MIXED ? mixed_step(GM, S, P, stream, ev)
+                                        : fp64_step(G, S, P, stream, ev);
+}
+
 int Solver::upload_state(const double* U_ref) {
   std::memcpy(h_stage, U_ref, (size_t)n_faces * kDim * sizeof(double));
   SPLASH_CUDA(cudaMemcpyAsync(d_stage, h_stage, (size_t)n_faces * kDim * sizeof(double),
                               cudaMemcpyHostToDevice, stream));
   SPLASH_CUDA(fp64_scatter_state(d_stage, d_perm, S.U, n_faces, fpad, stream));
-  SPLASH_CUDA(fp64_prepare(G, S, P, stream));
+  SPLASH_CUDA(launch_prepare());
   return SPLASH_OK;
 }
 
@@ -302,7 +356,7 @@ int Solver::read_scalars(double* out) {
 
 int Solver::capture_graph() {
   SPLASH_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-  cudaError_t le = fp64_step(G, S, P, stream);
+  cudaError_t le = launch_step(nullptr);
   cudaGraph_t g = nullptr;
   cudaError_t ce = cudaStreamEndCapture(stream, &g);
   if (le != cudaSuccess) {
@@ -407,8 +461,18 @@ int splash_create(const splash_mesh_desc* mesh, const double* U_in, int dim, dou
     S.U = s->dalloc<double>(splash::kDim * fp);
     S.W0 = s->dalloc<double>(splash::kDim * fp);
     S.W1 = s->dalloc<double>(splash::kDim * fp);
-    S.uplus = s->dalloc<double>(splash::kDim * PS);
-    s->n_partials = splash::fp64_partial_blocks(s->n_faces);
+    if (precision == SPLASH_PREC_MIXED) {
+      S.W32 = s->dalloc<float>(splash::kDim * fp);
+      S.uplus32 = s->dalloc<float>(splash::kDim * PS);
+      S.uplus = nullptr;
+      SPLASH_CUDA(cudaMemset(S.W32, 0, splash::kDim * fp * sizeof(float)));
+      SPLASH_CUDA(cudaMemset(S.uplus32, 0, splash::kDim * PS * sizeof(float)));
+      s->n_partials = splash::mixed_partial_blocks(s->n_faces);
+    } else {
+      S.uplus = s->dalloc<double>(splash::kDim * PS);
+      SPLASH_CUDA(cudaMemset(S.uplus, 0, splash::kDim * PS * sizeof(double)));
+      s->n_partials = splash::fp64_partial_blocks(s->n_faces);
+    }
     S.partial = s->dalloc<double>((size_t)s->n_partials * splash::kPartialStride);
     S.scal = s->dalloc<double>(splash::kScCount);
     S.err = s->dalloc<unsigned int>(4);
@@ -417,7 +481,6 @@ int splash_create(const splash_mesh_desc* mesh, const double* U_in, int dim, dou
     SPLASH_CUDA(cudaMemset(S.U, 0, splash::kDim * fp * sizeof(double)));
     SPLASH_CUDA(cudaMemset(S.W0, 0, splash::kDim * fp * sizeof(double)));
     SPLASH_CUDA(cudaMemset(S.W1, 0, splash::kDim * fp * sizeof(double)));
-    SPLASH_CUDA(cudaMemset(S.uplus, 0, splash::kDim * PS * sizeof(double)));
     SPLASH_CUDA(cudaMemset(S.scal, 0, splash::kScCount * sizeof(double)));
     SPLASH_CUDA(cudaMemset(S.err, 0, 4 * sizeof(unsigned int)));
     SPLASH_CUDA(cudaMallocHost(&s->h_stage, (size_t)s->n_faces * splash::kDim * sizeof(double)));
@@ -477,7 +540,7 @@ int splash_kernel_times(splash_solver* h, int reps, double dt0, double ms[5]) {
   int rc = SPLASH_OK;
   for (int r = 0; r < reps && rc == SPLASH_OK; ++r) {
     cudaError_t e = splash::fp64_set_dt0(s->S, dt0, s->stream);
-    if (e == cudaSuccess) e = splash::fp64_step(s->G, s->S, s->P, s->stream, ev);
+    if (e == cudaSuccess) e = s->launch_step(ev);
     if (e == cudaSuccess) e = cudaEventSynchronize(ev[5]);
     if (e != cudaSuccess) {
       rc = fail(SPLASH_E_CUDA, "kernel timing: %s", cudaGetErrorString(e));
@@ -501,8 +564,12 @@ int splash_memory(splash_solver* h, int64_t out[2]) {
   if (!s || !out) return fail(SPLASH_E_INVALID, "NULL argument");
   const size_t fp = (size_t)s->fpad, PS = (size_t)s->max_slots * fp;
   out[0] = (int64_t)s->geometry_bytes;
-  out[1] = (int64_t)(8 * (3 * splash::kDim * fp + splash::kDim * PS) +
-                     8 * (size_t)s->n_partials * splash::kPartialStride);
+  if (s->precision == SPLASH_PREC_MIXED)
+    out[1] = (int64_t)(8 * splash::kDim * fp + 4 * (splash::kDim * fp + splash::kDim * PS) +
+                       8 * (size_t)s->n_partials * splash::kPartialStride);
+  else
+    out[1] = (int64_t)(8 * (3 * splash::kDim * fp + splash::kDim * PS) +
+                       8 * (size_t)s->n_partials * splash::kPartialStride);
   return SPLASH_OK;
 }
 
@@ -672,7 +739,13 @@ int splash_write_t_curl(splash_solver* h, const char* path) {
   // U_plus of the last stage, slot planes -> host
   const size_t PS = (size_t)s->max_slots * s->fpad;
   std::vector<double> up(splash::kDim * PS);
-  SPLASH_CUDA(cudaMemcpy(up.data(), s->S.uplus, up.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  if (s->S.uplus) {
+    SPLASH_CUDA(cudaMemcpy(up.data(), s->S.uplus, up.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  } else {
+    std::vector<float> up32(splash::kDim * PS);
+    SPLASH_CUDA(cudaMemcpy(up32.data(), s->S.uplus32, up32.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    std::copy(up32.begin(), up32.end(), up.begin());
+  }
   double t;
   if ((rc = splash_time(h, &t))) return rc;
   os << t << "  ";

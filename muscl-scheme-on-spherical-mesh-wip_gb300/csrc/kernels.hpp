@@ -17,9 +17,18 @@ cudaError_t fp64_set_dt0(const DevState& S, double dt0, cudaStream_t st);
 // an event is recorded before the first and after every launch.
 cudaError_t fp64_step(const DevGeom& G, const DevState& S, const PhysParams& P, cudaStream_t st,
                       cudaEvent_t* ev = nullptr);
+// The dt clip (one block) shared by both paths.
+cudaError_t dt_reduce(const DevState& S, const PhysParams& P, int nblocks, cudaStream_t st);
 cudaError_t fp64_scatter_state(const double* aos, const int* perm, double* U, int n_faces, int fpad,
                                cudaStream_t st);
 cudaError_t fp64_gather_state(const double* U, const int* perm, double* aos, int n_faces, int fpad,
                               cudaStream_t st);
+
+// ---- FP32/FP64 mixed path (step_mixed.cu) ----
+cudaError_t mixed_prepare(const DevGeomMixed& G, const DevState& S, const PhysParams& P,
+                          cudaStream_t st);
+cudaError_t mixed_step(const DevGeomMixed& G, const DevState& S, const PhysParams& P,
+                       cudaStream_t st, cudaEvent_t* ev = nullptr);
+int mixed_partial_blocks(int n_faces);
 
 }  // namespace splash

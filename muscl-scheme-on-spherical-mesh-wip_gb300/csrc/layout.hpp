@@ -64,12 +64,39 @@ struct DevGeom {
   const int* rev;         // slot-plane index of the same edge seen from the neighbour
 };
 
+// Geometry of the FP32/FP64 mixed path: FP32 slot planes, FP64 where the
+// value feeds an FP64 step (unit centre for pressure recovery and the dt
+// clip, area, accretion mass source, flux coefficient).
+struct DevGeomMixed {
+  int n_faces;
+  int fpad;
+  int max_slots;
+  const int8_t* nslots;
+  const double* fcn;      // 3 planes, FP64 unit face centre
+  const float* fcn32;     // 3 planes, FP32 copy (source term)
+  const double* area;
+  const double* acc_src;  // accretion mass source, FP64
+  const int* sten;        // 4 planes
+  const float* beta;      // 4 planes
+  const float* inv_h;     // 2 planes: 1/H_plus, 1/H_minus
+  const float* bm;
+  const float* eta;       // 2 planes
+  const float* arc_a;
+  const float* ec;        // 3 planes, unit edge centre
+  const float* en;        // 3 planes
+  const float* nxr;       // 3 planes
+  const double* coef;     // round_diff * chord / area (FP64)
+  const int* rev;
+};
+
 // Solver state on the device.
 struct DevState {
   double* U;      // conserved state, kDim planes of fpad
   double* W0;     // (Sigma, l, Pi) of U, kDim planes
   double* W1;     // (Sigma, l, Pi) after stage 1, kDim planes
   double* uplus;  // reconstructed edge states, kDim * max_slots planes of fpad
+  float* W32;     // mixed path: (Sigma, l, Pi) in FP32, kDim planes
+  float* uplus32; // mixed path: edge states (Sigma, l, Pi) in FP32
   double* partial;  // per-block partial records (kPartialStride doubles)
   double* scal;   // device scalars, see ScalarSlot
   unsigned int* err;  // stop bits

@@ -234,5 +234,99 @@ __device__ __forceinline__ double limiter_field(double r, double nu_plus, double
   return ((1 - hv) * to + hv * sb);
 }
 
+// Per-face contributions to the dt clip of the NEXT step and to the
+// diagnostics sums, for a conserved state u (u[4] = energy):
+// find_v_max (MUSCL_base.hpp:311-343) and extra_dt_constr
+// (physics/adiabatic.hpp:543-580).
+__device__ __forceinline__ void dt_candidates(const double* u, D3 r, double area,
+                                              const PhysParams& P, double& vmax,
+                                              double& dmin, double sums[5]) {
+  D3 vpos = cross3(r, d3(u[1], u[2], u[3]));
+  vpos = divs(vpos, u[0]);
+  const double vn = norm3(vpos);
+  const double p = pressure_fc(u, r, P.gam);
+  const double c_s = sqrt(P.gam * p / u[0]);
+  vmax = fmax(vn, c_s);
+  // extra_dt_constr
+  D3 vel = cross3(r, d3(u[1], u[2], u[3]));
+  vel = divs(vel, -u[0]);
+  const D3 omega0 = d3(0, 0, P.omega_ns);
+  const D3 vel0 = cross3(omega0, r);
+  const double nvel = norm3(vel);
+  const double press = pressure(u, nvel, P.gam);
+  const double gam3d = 1 / (2 - P.gam);
+  const double GM = 0.217909;
+  const double g_eff = GM - nvel * nvel;
+  const double rho = gam3d / (2 * gam3d - 1) * g_eff * u[0] * u[0] / press;
+  dmin = 0.01 * u[0] / (P.alpha * rho * norm3(sub(vel, vel0)));
+#pragma unroll
+  for (int k = 0; k < 5; ++k) sums[k] = u[k] * area;
+}
+
+// physics/adiabatic.hpp:396-541 ; w[4] is the pressure
+__device__ __forceinline__ void source_term(const double* w, D3 fcn, double acc0,
+                                            const PhysParams& P, double* res) {
+#pragma unroll
+  for (int i = 0; i < kDim; ++i) res[i] = 0;
+  if (!P.accretion_on) return;
+  D3 vel = cross3(fcn, d3(w[1], w[2], w[3]));
+  vel = divs(vel, -w[0]);
+  res[0] = acc0;
+  const D3 omega_acc = d3(P.omega_acc_x, P.omega_acc_y, P.omega_acc_z);
+  const D3 omxr = cross3(omega_acc, fcn);
+  D3 rxv = cross3(fcn, omxr);
+  res[1] = res[0] * rxv.x;
+  res[2] = res[0] * rxv.y;
+  res[3] = res[0] * rxv.z;
+  const double nd = norm3(sub(omxr, vel));
+  res[4] = res[0] * (P.e_acc + (nd * nd) / 2.);
+  rxv = cross3(fcn, vel);
+  const double nvel = norm3(vel);
+  if (!P.friction_on) {
+    const double fall_eff = 1;
+    const double dmdt = -(fall_eff * P.acc_rate * 4 * M_PI) / P.total_mass * w[0];
+    res[0] += dmdt;
+    res[1] += dmdt * rxv.x;
+    res[2] += dmdt * rxv.y;
+    res[3] += dmdt * rxv.z;
+    res[4] += dmdt * (P.gam / (P.gam - 1) * w[4] / w[0] + (nvel * nvel) / 2.);
+  }
+  const double GM = 0.217909;
+  const double g_eff = GM - nvel * nvel;
+  const double c_sigma = 4.85e36;
+  const double k_m = 1.6e-13;
+  const double kappa = 3.4e6;
+  const double C = 12. / 5 * k_m * w[0] / w[4] * pow(3. / 4 * c_sigma * g_eff * w[0], 1. / 4);
+  const double beta_switch = 0.736194670678821;
+  const double C_switch = -1 - 1 / (beta_switch - 1);
+  double beta;
+  if (C <= C_switch)
+    beta = 1 - 1 / (1 + C);
+  else
+    beta = 1 - pow(2 / C, 4.0);
+  const double beta_ceil = 1 - 1e-8, beta_floor = 1e-8;
+  if (beta < beta_floor || isnan(beta)) beta = beta_floor;
+  if (beta > beta_ceil) beta = beta_ceil;
+  res[4] -= g_eff / kappa * (1 - beta);
+  if (P.friction_on) {
+    const double gam3d = 1 / (2 - P.gam);
+    const double rho = gam3d / (2 * gam3d - 1) * g_eff * w[0] * w[0] / w[4];
+    const D3 omega0 = d3(0, 0, P.omega_ns);
+    const D3 vel0 = cross3(omega0, fcn);
+    const double dv = norm3(sub(vel, vel0));
+    const D3 wr = scal(sub(vel, vel0), -P.alpha * rho * dv);
+    const D3 l_fr = cross3(fcn, wr);
+    res[1] += l_fr.x;
+    res[2] += l_fr.y;
+    res[3] += l_fr.z;
+    res[4] += dot3(wr, vel0);
+    res[0] -= P.alpha * rho * dv;
+    res[1] -= P.alpha * rho * dv / w[0] * w[1];
+    res[2] -= P.alpha * rho * dv / w[0] * w[2];
+    res[3] -= P.alpha * rho * dv / w[0] * w[3];
+    res[4] -= P.alpha * rho * dv * (nvel * nvel / 2. + w[4] * P.gam / ((P.gam - 1) * w[0]));
+  }
+}
+
 }  // namespace f64
 }  // namespace splash

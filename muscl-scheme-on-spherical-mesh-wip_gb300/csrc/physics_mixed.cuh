@@ -1,0 +1,221 @@
+// FP32 physics of the mixed-precision MUSCL step.
+//
+// Same formulas as the FP64 path (physics_fp64.cuh, citing the reference),
+// evaluated in FP32 with three deliberate differences that keep FP32 away
+// from cancellation:
+//   * edge states carry the pressure Pi, not the energy: the reference
+//     converts Pi -> E at the edge (MUSCL_base.hpp:541-562) and every flux
+//     routine converts back E -> Pi (physics/adiabatic.hpp:582-592), a round
+//     trip that is exact in real arithmetic but loses digits in FP32 when the
+//     kinetic energy dominates; the mixed path uses Pi directly and forms
+//     E = Pi/(gam-1) + Sigma |v|^2/2 (a sum of positive terms) where the flux
+//     needs it;
+//   * the unit edge centre is used without the |ec| ~ 1 rescale;
+//   * integer powers are multiplications and pow(1-r, 0.1) is exp(0.1 log).
+#pragma once
+
+#include <cmath>
+
+#include "layout.hpp"
+
+namespace splash {
+namespace mx {
+
+struct F3 {
+  float x, y, z;
+};
+
+__device__ __forceinline__ F3 f3(float x, float y, float z) { return F3{x, y, z}; }
+__device__ __forceinline__ F3 sub(F3 a, F3 b) { return F3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ F3 scal(F3 a, float s) { return F3{a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ float dot3(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float norm3(F3 a) { return sqrtf(dot3(a, a)); }
+__device__ __forceinline__ F3 cross3(F3 a, F3 b) {
+  return F3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ float smax(float a, float b) { return (a < b) ? b : a; }
+__device__ __forceinline__ float smin(float a, float b) { return (b < a) ? b : a; }
+
+struct SlotGeomF {
+  F3 ec;   // unit edge centre
+  F3 en;   // edge normal
+  F3 nxr;  // cross(en, ec)
+};
+
+// Primitive view of one edge state u = (Sigma, l, Pi).
+struct EdgeState {
+  float rho;
+  F3 vel;    // cross(ec, l) / (-Sigma)
+  float p;   // max(1e-16, Pi)   (pressure floor of adiabatic.hpp:586-591)
+  float E;   // Pi/(gam-1) + Sigma |v|^2/2
+  float vn;  // v . n
+};
+
+__device__ __forceinline__ EdgeState edge_state(const float* u, const SlotGeomF& g, float gam) {
+  EdgeState s;
+  s.rho = u[0];
+  const float inv = -1.0f / u[0];
+  s.vel = scal(cross3(g.ec, f3(u[1], u[2], u[3])), inv);
+  s.p = smax(1e-16f, u[4]);
+  s.E = u[4] / (gam - 1.0f) + 0.5f * u[0] * dot3(s.vel, s.vel);
+  s.vn = dot3(s.vel, g.en);
+  return s;
+}
+
+// physics/adiabatic.hpp:352-392 with u[4] = E supplied separately
+__device__ __forceinline__ void phys_flux(const float* u, const EdgeState& s, const SlotGeomF& g,
+                                          float* F) {
+  F[0] = s.rho * s.vn;
+  F[1] = u[1] * s.vn - g.nxr.x * s.p;
+  F[2] = u[2] * s.vn - g.nxr.y * s.p;
+  F[3] = u[3] * s.vn - g.nxr.z * s.p;
+  F[4] = (s.E + s.p) * s.vn;
+}
+
+// PVRS wave speeds, physics/adiabatic.hpp:594-683
+__device__ __forceinline__ void char_vel(const EdgeState& L, const EdgeState& R, float gam,
+                                         float& S_L, float& S_R, float& a_L, float& a_R) {
+  a_L = sqrtf(gam * L.p / L.rho);
+  a_R = sqrtf(gam * R.p / R.rho);
+  const float p_pvrs = 0.5f * (L.p + R.p) - 0.125f * (R.vn - L.vn) * (L.rho + R.rho) * (a_L + a_R);
+  const float p_star = smax(0.f, p_pvrs);
+  const float k = (gam + 1.0f) / (2.0f * gam);
+  float q_R = 1.f, q_L = 1.f;
+  if (!(p_star <= R.p)) {
+    q_R = sqrtf(1.f + k * (p_star / R.p - 1.f));
+    if (isnan(q_R) || isinf(q_R)) q_R = 1.f;
+  }
+  if (!(p_star <= L.p)) {
+    q_L = sqrtf(1.f + k * (p_star / L.p - 1.f));
+    if (isnan(q_L) || isinf(q_L)) q_L = 1.f;
+  }
+  S_L = L.vn - a_L * q_L;
+  S_R = R.vn + a_R * q_R;
+}
+
+// Riemann fluxes (HLLE_p.hpp:19-58, HLLC.hpp:138-242, HLLCplus.hpp:17-177).
+// Returns the stop bits of splash_gb300.h (2 NaN wave speed, 4 ordering).
+__device__ __forceinline__ unsigned flux_star(const float* uL, const float* uR, const SlotGeomF& g,
+                                              float gam, int solver, float* F) {
+  unsigned bits = 0;
+  const EdgeState L = edge_state(uL, g, gam);
+  const EdgeState R = edge_state(uR, g, gam);
+  float S_L, S_R, a_L, a_R;
+  char_vel(L, R, gam, S_L, S_R, a_L, a_R);
+  if (isnan(S_L) || isnan(S_R)) bits |= 2u;
+  float FL[kDim], FR[kDim];
+  phys_flux(uL, L, g, FL);
+  phys_flux(uR, R, g, FR);
+  const float qL[kDim] = {uL[0], uL[1], uL[2], uL[3], L.E};
+  const float qR[kDim] = {uR[0], uR[1], uR[2], uR[3], R.E};
+  if (solver == 1) {
+    if (S_L >= 0) {
+#pragma unroll
+      for (int i = 0; i < kDim; ++i) F[i] = FL[i];
+    } else if (S_L < 0 && S_R > 0) {
+      const float inv = 1.0f / (S_R - S_L);
+#pragma unroll
+      for (int i = 0; i < kDim; ++i) F[i] = (S_R * FL[i] - S_L * FR[i] + S_R * S_L * (qR[i] - qL[i])) * inv;
+    } else {
+      if (!(S_R <= 0)) bits |= 4u;
+#pragma unroll
+      for (int i = 0; i < kDim; ++i) F[i] = FR[i];
+    }
+    return bits;
+  }
+  const float V_L = L.vn, V_R = R.vn;
+  float S_star = (R.p - L.p + L.rho * V_L * (S_L - V_L) - R.rho * V_R * (S_R - V_R)) /
+                 (L.rho * (S_L - V_L) - R.rho * (S_R - V_R));
+  if (isnan(S_star) || isinf(S_star)) S_star = 0.5f * (V_L + V_R);
+  int side;
+  if (S_L >= 0) {
+    side = 0;
+  } else if (S_L < 0 && S_star >= 0) {
+    side = 1;
+  } else if (S_star < 0 && S_R >= 0) {
+    side = 2;
+  } else {
+    if (!(S_R < 0)) bits |= 4u;
+    side = 3;
+  }
+  if (side == 0 || side == 3) {
+    const float* src = (side == 0) ? FL : FR;
+#pragma unroll
+    for (int i = 0; i < kDim; ++i) F[i] = src[i];
+    return bits;
+  }
+  const float P_LR = 0.5f * (L.p + R.p + L.rho * (S_L - V_L) * (S_star - V_L) +
+                             R.rho * (S_R - V_R) * (S_star - V_R));
+  const float D[kDim] = {0.f, -g.nxr.x, -g.nxr.y, -g.nxr.z, S_star};
+  const float Sk = (side == 1) ? S_L : S_R;
+  const float* qk = (side == 1) ? qL : qR;
+  const float* Fk = (side == 1) ? FL : FR;
+  const float inv = 1.0f / (Sk - S_star);
+#pragma unroll
+  for (int i = 0; i < kDim; ++i) F[i] = (S_star * (Sk * qk[i] - Fk[i]) + Sk * P_LR * D[i]) * inv;
+  if (solver == 3) {
+    const float phi_L = L.rho * (S_L - V_L);
+    const float phi_R = R.rho * (S_R - V_R);
+    const float M = smin(1.f, smax(norm3(L.vel) / a_L, norm3(R.vel) / a_R));
+    int lambd = 0;
+    if ((V_L - a_L) > 0 && (V_R - a_R) < 0) lambd = 1;
+    if ((V_L + a_L) > 0 && (V_R + a_R) < 0) lambd = 1;
+    if ((V_R - a_R) > 0 && (V_L - a_L) < 0) lambd = 1;
+    if ((V_R + a_R) > 0 && (V_L + a_L) < 0) lambd = 1;
+    float f_star = 1.f;
+    if (lambd == 0) f_star = M * sqrtf(4.f + (1.f - M * M) * (1.f - M * M)) / (1.f + M * M);
+    const float h = smin(L.p / R.p, R.p / L.p);
+    const float gsw = 1.f - powf(h, M);
+    const float dV = V_R - V_L;
+    const F3 dv = sub(R.vel, L.vel);
+    const float cs = Sk * inv * gsw;
+    const float fs = (f_star - 1.f) * dV;
+    const F3 vff = f3(fs * g.en.x + cs * (dv.x - dV * g.en.x), fs * g.en.y + cs * (dv.y - dV * g.en.y),
+                      fs * g.en.z + cs * (dv.z - dV * g.en.z));
+    const F3 am = cross3(g.ec, vff);
+    const float w = phi_L * phi_R / (phi_R - phi_L);
+    F[1] += am.x * w;
+    F[2] += am.y * w;
+    F[3] += am.z * w;
+    F[4] += fs * S_star * w;
+  }
+  return bits;
+}
+
+// h(r) switch and the blended limiter (physics/adiabatic.hpp:685-828)
+__device__ __forceinline__ float limiter_switch(float r) {
+  float o = 0.f;
+  if (r < 1.f && r > 0.f) o = 1.f - tanhf(4.f * (r * r) * __expf(0.1f * __logf(1.f - r)));
+  if (r >= 1.f) {
+    const float x = r - 1.f;
+    const float t = tanhf(10.f * (x * x * x));
+    const float t2 = t * t;
+    o = t2 * t2 * t2;
+  }
+  return o;
+}
+
+__device__ __forceinline__ float limiter_field(float r, float nu_plus, float eta_p, float sb_scale) {
+  if (isnan(r)) return 0.f;
+  const float sb = smax(0.f, smax(smin(1.f, r * sb_scale), smin(r, eta_p)));
+  const float to = smax(0.f, smin(sb, 1.f + (1.f + nu_plus) * (1.f / 3.f) * (r - 1.f)));
+  const float hv = limiter_switch(r);
+  return (1.f - hv) * to + hv * sb;
+}
+
+// Neumaier-compensated FP32 accumulator: the sum of the FP32 terms is kept
+// as hi + lo (about twice FP32 precision) and folded into FP64 at the end.
+struct Acc {
+  float hi, lo;
+  __device__ __forceinline__ void add(float x) {
+    const float t = hi + x;
+    if (fabsf(hi) >= fabsf(x))
+      lo += (hi - t) + x;
+    else
+      lo += (x - t) + hi;
+    hi = t;
+  }
+};
+
+}  // namespace mx
+}  // namespace splash

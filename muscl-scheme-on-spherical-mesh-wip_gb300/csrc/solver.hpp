@@ -44,6 +44,7 @@ struct Solver {
   cudaStream_t stream = nullptr;
   PhysParams P{};
   DevGeom G{};
+  DevGeomMixed GM{};
   DevState S{};
   double* d_stage = nullptr;  // [n_faces][5] reference-order staging
   int* d_perm = nullptr;
@@ -66,6 +67,8 @@ struct Solver {
   int read_scalars(double* out);
   int capture_graph();
   int step(double dt0);
+  cudaError_t launch_step(cudaEvent_t* ev);  // one un-captured step
+  cudaError_t launch_prepare();
   static int check_cuda(cudaError_t e, const char* what);
 };
 

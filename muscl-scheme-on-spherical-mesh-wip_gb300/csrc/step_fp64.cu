@@ -21,6 +21,7 @@
 
 #include "kernels.hpp"
 #include "physics_fp64.cuh"
+#include "reduce.cuh"
 
 namespace splash {
 namespace f64 {
@@ -30,135 +31,6 @@ constexpr int kBlock = 128;
 
 __device__ __forceinline__ D3 plane3(const double* p, int stride, int i) {
   return D3{p[i], p[stride + i], p[2 * stride + i]};
-}
-
-// Warp + block reduction of one partial record; thread 0 of the block
-// writes it.  Fixed tree order, so the result is deterministic.
-__device__ void block_partials(double vmax, double dmin, const double sums[5], double* out) {
-  __shared__ double sm[kBlock / 32][7];
-  double v[7] = {vmax, dmin, sums[0], sums[1], sums[2], sums[3], sums[4]};
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const double a = __shfl_down_sync(0xffffffffu, v[0], o);
-    const double b = __shfl_down_sync(0xffffffffu, v[1], o);
-    v[0] = fmax(v[0], a);
-    v[1] = fmin(v[1], b);
-#pragma unroll
-    for (int k = 2; k < 7; ++k) v[k] = v[k] + __shfl_down_sync(0xffffffffu, v[k], o);
-  }
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (lane == 0) {
-#pragma unroll
-    for (int k = 0; k < 7; ++k) sm[warp][k] = v[k];
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double r[7];
-#pragma unroll
-    for (int k = 0; k < 7; ++k) r[k] = sm[0][k];
-    for (int w = 1; w < kBlock / 32; ++w) {
-      r[0] = fmax(r[0], sm[w][0]);
-      r[1] = fmin(r[1], sm[w][1]);
-#pragma unroll
-      for (int k = 2; k < 7; ++k) r[k] = r[k] + sm[w][k];
-    }
-#pragma unroll
-    for (int k = 0; k < 7; ++k) out[k] = r[k];
-  }
-}
-
-// Per-face contributions to the dt clip of the NEXT step and to the
-// diagnostics sums, for a conserved state u (u[4] = energy):
-// find_v_max (MUSCL_base.hpp:311-343) and extra_dt_constr
-// (physics/adiabatic.hpp:543-580).
-__device__ __forceinline__ void dt_candidates(const double* u, D3 r, double area,
-                                              const PhysParams& P, double& vmax,
-                                              double& dmin, double sums[5]) {
-  D3 vpos = cross3(r, d3(u[1], u[2], u[3]));
-  vpos = divs(vpos, u[0]);
-  const double vn = norm3(vpos);
-  const double p = pressure_fc(u, r, P.gam);
-  const double c_s = sqrt(P.gam * p / u[0]);
-  vmax = fmax(vn, c_s);
-  // extra_dt_constr
-  D3 vel = cross3(r, d3(u[1], u[2], u[3]));
-  vel = divs(vel, -u[0]);
-  const D3 omega0 = d3(0, 0, P.omega_ns);
-  const D3 vel0 = cross3(omega0, r);
-  const double nvel = norm3(vel);
-  const double press = pressure(u, nvel, P.gam);
-  const double gam3d = 1 / (2 - P.gam);
-  const double GM = 0.217909;
-  const double g_eff = GM - nvel * nvel;
-  const double rho = gam3d / (2 * gam3d - 1) * g_eff * u[0] * u[0] / press;
-  dmin = 0.01 * u[0] / (P.alpha * rho * norm3(sub(vel, vel0)));
-#pragma unroll
-  for (int k = 0; k < 5; ++k) sums[k] = u[k] * area;
-}
-
-// physics/adiabatic.hpp:396-541 ; w[4] is the pressure
-__device__ __forceinline__ void source_term(const double* w, D3 fcn, double acc0,
-                                            const PhysParams& P, double* res) {
-#pragma unroll
-  for (int i = 0; i < kDim; ++i) res[i] = 0;
-  if (!P.accretion_on) return;
-  D3 vel = cross3(fcn, d3(w[1], w[2], w[3]));
-  vel = divs(vel, -w[0]);
-  res[0] = acc0;
-  const D3 omega_acc = d3(P.omega_acc_x, P.omega_acc_y, P.omega_acc_z);
-  const D3 omxr = cross3(omega_acc, fcn);
-  D3 rxv = cross3(fcn, omxr);
-  res[1] = res[0] * rxv.x;
-  res[2] = res[0] * rxv.y;
-  res[3] = res[0] * rxv.z;
-  const double nd = norm3(sub(omxr, vel));
-  res[4] = res[0] * (P.e_acc + (nd * nd) / 2.);
-  rxv = cross3(fcn, vel);
-  const double nvel = norm3(vel);
-  if (!P.friction_on) {
-    const double fall_eff = 1;
-    const double dmdt = -(fall_eff * P.acc_rate * 4 * M_PI) / P.total_mass * w[0];
-    res[0] += dmdt;
-    res[1] += dmdt * rxv.x;
-    res[2] += dmdt * rxv.y;
-    res[3] += dmdt * rxv.z;
-    res[4] += dmdt * (P.gam / (P.gam - 1) * w[4] / w[0] + (nvel * nvel) / 2.);
-  }
-  const double GM = 0.217909;
-  const double g_eff = GM - nvel * nvel;
-  const double c_sigma = 4.85e36;
-  const double k_m = 1.6e-13;
-  const double kappa = 3.4e6;
-  const double C = 12. / 5 * k_m * w[0] / w[4] * pow(3. / 4 * c_sigma * g_eff * w[0], 1. / 4);
-  const double beta_switch = 0.736194670678821;
-  const double C_switch = -1 - 1 / (beta_switch - 1);
-  double beta;
-  if (C <= C_switch)
-    beta = 1 - 1 / (1 + C);
-  else
-    beta = 1 - pow(2 / C, 4.0);
-  const double beta_ceil = 1 - 1e-8, beta_floor = 1e-8;
-  if (beta < beta_floor || isnan(beta)) beta = beta_floor;
-  if (beta > beta_ceil) beta = beta_ceil;
-  res[4] -= g_eff / kappa * (1 - beta);
-  if (P.friction_on) {
-    const double gam3d = 1 / (2 - P.gam);
-    const double rho = gam3d / (2 * gam3d - 1) * g_eff * w[0] * w[0] / w[4];
-    const D3 omega0 = d3(0, 0, P.omega_ns);
-    const D3 vel0 = cross3(omega0, fcn);
-    const double dv = norm3(sub(vel, vel0));
-    const D3 wr = scal(sub(vel, vel0), -P.alpha * rho * dv);
-    const D3 l_fr = cross3(fcn, wr);
-    res[1] += l_fr.x;
-    res[2] += l_fr.y;
-    res[3] += l_fr.z;
-    res[4] += dot3(wr, vel0);
-    res[0] -= P.alpha * rho * dv;
-    res[1] -= P.alpha * rho * dv / w[0] * w[1];
-    res[2] -= P.alpha * rho * dv / w[0] * w[2];
-    res[3] -= P.alpha * rho * dv / w[0] * w[3];
-    res[4] -= P.alpha * rho * dv * (nvel * nvel / 2. + w[4] * P.gam / ((P.gam - 1) * w[0]));
-  }
 }
 
 // ---------------------------------------------------------------------
@@ -178,7 +50,7 @@ __global__ void __launch_bounds__(kBlock) prepare_kernel(DevGeom G, DevState S, 
     S.W0[4 * G.fpad + f] = pressure_fc(u, r, P.gam) - 0.0;
     dt_candidates(u, r, G.area[f], P, vmax, dmin, sums);
   }
-  block_partials(vmax, dmin, sums, S.partial + (size_t)blockIdx.x * kPartialStride);
+  red::block_partials<kBlock>(vmax, dmin, sums, S.partial + (size_t)blockIdx.x * kPartialStride);
 }
 
 // dt = min(dt0, 0.1 h0 / max_vel, extra_dt)  (MUSCL_base.hpp:100-115)
@@ -340,7 +212,7 @@ __global__ void __launch_bounds__(kBlock) flux_update_kernel(DevGeom G, DevState
       dt_candidates(u, fcn, area, P, vmax, dmin, sums);
     }
   }
-  if (STAGE == 2) block_partials(vmax, dmin, sums, S.partial + (size_t)blockIdx.x * kPartialStride);
+  if (STAGE == 2) red::block_partials<kBlock>(vmax, dmin, sums, S.partial + (size_t)blockIdx.x * kPartialStride);
 }
 
 __global__ void set_scalar_kernel(double* dst, double v) { *dst = v; }
@@ -374,6 +246,11 @@ int fp64_partial_blocks(int n_faces) { return f64::blocks_for(n_faces); }
 cudaError_t fp64_prepare(const DevGeom& G, const DevState& S, const PhysParams& P,
                          cudaStream_t st) {
   f64::prepare_kernel<<<f64::blocks_for(G.n_faces), f64::kBlock, 0, st>>>(G, S, P);
+  return cudaGetLastError();
+}
+
+cudaError_t dt_reduce(const DevState& S, const PhysParams& P, int nblocks, cudaStream_t st) {
+  f64::dt_kernel<<<1, 256, 0, st>>>(S, P, nblocks);
   return cudaGetLastError();
 }
 

@@ -1,0 +1,96 @@
+"""FP32/FP64 mixed path: accuracy against the FP64 path (itself at 1e-10
+of the reference), conservation, and behaviour parity (stop flags, API)."""
+import numpy as np
+import pytest
+
+from helpers import load, mesh_of, rel_linf
+
+pytestmark = pytest.mark.gpu
+
+
+def make(case, precision):
+    from test_gpu_parity import gpu_solver
+
+    return gpu_solver(case, precision=precision)
+
+
+def l1_rel(a, b, area):
+    """Area-weighted relative L1 per field: sum A|a-b| / sum A|b|."""
+    num = np.sum(area[:, None] * np.abs(a - b), axis=0)
+    den = np.sum(area[:, None] * np.abs(b), axis=0)
+    return num / np.where(den > 0, den, 1)
+
+
+def test_accreting_mid_size_2000_steps():
+    """icosphere_hex(7), HLLC+, accretion on, Sigma = Pi = 1 +- 1e-3, 2000
+    steps at dt0 = 2e-4: relative L1 density error of the mixed path below
+    1e-5 against FP64 (the stated accuracy bar)."""
+    import splash_gb300 as sg
+
+    g = sg.Geometry(mesh_of("hex", 7))
+    gam = sg.initial_conditions.gam2d(4 / 3)
+    U0 = sg.initial_conditions.quiet_noise(g.unit_face_centers(), gam, seed=1)
+    case = {"U0": U0, "gam": gam, "accretion_on": True, "solver": 3, "mesh": "hex", "level": 7,
+            "params": np.array([1e-2, 0.5, 0.5, 0.2, 0.1, 1e-6, 1.0])}
+    a = make(case, 0)
+    b = make(case, 1)
+    a.do_steps(2000, 2e-4)
+    b.do_steps(2000, 2e-4)
+    Ua, Ub = a.get_state(), b.get_state()
+    err = l1_rel(Ub, Ua, g["area"])
+    assert err[0] < 1e-5, err
+    assert np.all(np.isfinite(Ub))
+    assert abs(a.time() - b.time()) < 1e-9 * a.time()
+    # mass budget: both paths gain the same mass from accretion
+    ma, mb = np.sum(g["area"] * Ua[:, 0]), np.sum(g["area"] * Ub[:, 0])
+    assert abs(ma - mb) < 1e-9 * ma
+
+
+@pytest.mark.parametrize("case_name,tol", [("c0_hex4_hllep", 2e-5), ("hex3_hllc_acc", 2e-5),
+                                           ("hex3_hllcp_acc", 2e-5), ("hex3_hllcp_nofric", 2e-5),
+                                           ("quad3_hllc_acc", 2e-5), ("c1_hex4_hllcp", 1e-6)])
+def test_mixed_close_to_reference_states(case_name, tol):
+    """Against the reference's own states: relative L-infinity per field."""
+    c = load(f"state_{case_name}.npz")
+    s = make(c, 1)
+    done = 0
+    for k, nstep in enumerate(c["steps"]):
+        s.do_steps(int(nstep) - done, float(c["dt0"]))
+        done = int(nstep)
+    err = rel_linf(s.get_state(), c["U"][-1])
+    assert np.all(err < tol), (case_name, err)
+    assert s.get_stop_check() == bool(c["stop"][-1])
+
+
+def test_mixed_stop_flags_and_round_trip():
+    import splash_gb300 as sg
+
+    c = load("state_shear_quad4_hllc.npz")
+    s = make(c, 1)
+    assert np.array_equal(s.get_state(), c["U0"])
+    s.do_step(float(c["dt0"]))
+    assert s.error_word() & sg.STOP_NEG_EXTRA_DT
+    U = c["U0"].copy()
+    U[3, 0] = np.nan
+    s.set_state(U)
+    s.do_step(1e-3)
+    assert s.error_word() & sg.STOP_NAN_FLUX
+
+
+def test_mass_conservation_without_sources():
+    """Accretion off: the total mass changes only through the flux
+    asymmetry; FP64 keeps it to round-off and the mixed path to FP32 flux
+    precision."""
+    import splash_gb300 as sg
+
+    g = sg.Geometry(mesh_of("hex", 6))
+    gam = sg.initial_conditions.gam2d(4 / 3)
+    U0 = sg.initial_conditions.rotating_blob(g.unit_face_centers(), gam, seed=3)
+    case = {"U0": U0, "gam": gam, "accretion_on": False, "solver": 2, "mesh": "hex", "level": 6,
+            "params": np.array([1e-2, 0.5, 0.5, 0.2, 0.1, 1e-6, 1.0])}
+    m0 = np.sum(g["area"] * U0[:, 0])
+    for prec, tol in ((0, 1e-12), (1, 1e-7)):
+        s = make(case, prec)
+        s.do_steps(200, 1e-3)
+        m = np.sum(g["area"] * s.get_state()[:, 0])
+        assert abs(m / m0 - 1) < tol, (prec, m / m0 - 1)
