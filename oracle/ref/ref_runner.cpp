@@ -202,6 +202,34 @@ int run(SurfaceMesh& mesh, const std::vector<std::vector<double>>& U_in, int dim
     s.dump_functions(out + "_funcs.bin", seed, nsamp, dt);
     return 0;
   }
+  if (mode == "writers") {
+    // The reference driver's output sequence (test.cpp:84-149): geometry
+    // and state writers at t = 0, light curves after every step, state
+    // writers and the final state at the end.  Files land in results/.
+    s.write_face_centers();
+    s.write_faces();
+    s.write_vertices();
+    s.write_t_rho();
+    s.write_t_p();
+    s.write_t_omega_z();
+    s.write_t_L();
+    FILE* lc = open_out(out + "_lightcurves.txt");
+    std::vector<double> l = s.get_light_curves();
+    std::fprintf(lc, "%.17g %.17g %.17g %.17g %.17g\n", s.time(), l[0], l[1], l[2], l[3]);
+    for (int i = 0; i < nsteps; ++i) {
+      s.do_step(dt);
+      l = s.get_light_curves();
+      std::fprintf(lc, "%.17g %.17g %.17g %.17g %.17g\n", s.time(), l[0], l[1], l[2], l[3]);
+    }
+    std::fclose(lc);
+    s.write_t_rho();
+    s.write_t_p();
+    s.write_t_curl();
+    s.write_t_omega_z();
+    s.write_t_L();
+    s.write_final_state();
+    return 0;
+  }
   if (mode == "time") {
     // Times only the do_step loop (construction excluded), stdout discarded
     // by the caller.

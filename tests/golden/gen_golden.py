@@ -183,6 +183,29 @@ def funcs_case(name, solver, params, acc=True, mesh="hex", level=3, nsamp=300, s
     print(f"funcs_{name}: {nsamp} samples")
 
 
+def writers_case(name, mesh, level, solver, gam, acc, params, dt, nsteps, recipe, seed):
+    """The reference's own output files (results/*.dat, light curves) for the
+    driver sequence of test.cpp:84-149, stored as text."""
+    g, _, _ = geometry(mesh, level)
+    U0 = recipe(unit(g["face_centers"]), gam, seed=seed)
+    with tempfile.TemporaryDirectory() as td:
+        td = Path(td)
+        (td / "input").mkdir()
+        (td / "results").mkdir()
+        (td / "input" / "parameters.json").write_text(json.dumps(params_json(params)))
+        ic.write_input_dat(td / "input" / "input.dat", U0)
+        cmd = [str(RUNNER), "writers", mesh, str(level), solver, "5", repr(gam), "0.0",
+               "1" if acc else "0", "8", repr(dt), str(nsteps), "0", str(td / "out")]
+        subprocess.run(cmd, cwd=td, check=True, stdout=subprocess.DEVNULL)
+        files = {p.name: p.read_text() for p in sorted((td / "results").iterdir())}
+        files["lightcurves.txt"] = (td / "out_lightcurves.txt").read_text()
+    rec = {"U0": U0, "gam": np.float64(gam), "dt0": np.float64(dt), "steps": nsteps,
+           "solver": SOLVERS[solver], "accretion_on": int(acc), "mesh": mesh, "level": level,
+           "files": np.array(list(files.keys())), "texts": np.array(list(files.values()))}
+    np.savez_compressed(HERE / f"writers_{name}.npz", **rec)
+    print(f"writers_{name}: {sorted(files)}")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.parse_args()
@@ -227,6 +250,8 @@ def main():
     # u_phi = 0.5 makes g_eff < 0, so extra_dt_constr latches stop_check
     state_case("shear_quad4_hllc", "quad", 4, "HLLC", gam, False, ACC_PARAMS, 1e-2, 30, 10,
                lambda r, g_, seed: ic.shear_layer(r, g_, seed=seed), 2)
+    writers_case("hex3_hllcp", "hex", 3, "HLLCplus", gam, True, ACC_PARAMS, 1e-3, 5,
+                 lambda r, g_, seed: ic.rotating_blob(r, g_, seed=seed), 5)
 
 
 if __name__ == "__main__":
