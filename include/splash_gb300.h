@@ -190,6 +190,30 @@ int splash_geometry_info(const splash_geometry* g, int64_t sizes[4], double scal
 int splash_geometry_get(const splash_geometry* g, const char* name, void* dst, size_t bytes,
                         size_t* written);
 
+/* ---- allocation-free CFL clip --------------------------------------------
+ * No counterpart in the reference: an addition for callers that cannot
+ * allocate device memory when they need the time step (a coupling code that
+ * owns all device memory through its own pool, or code about to capture its
+ * stream into a CUDA graph).  Computes, on the CURRENT CUDA device and on
+ * `stream` (NULL = the default stream), the dt that do_step(dt0) would use
+ * for a conserved state already on the device:
+ *   U            [n_faces][5] conserved state (device)
+ *   unit_centres [n_faces][3] unit face centres, fc/|fc| (device)
+ *   area         [n_faces] face areas (device)
+ *   h0           minimum edge arc length (splash_geometry_info scalars[0])
+ *   out          9 doubles (device): dt, max_vel, extra_dt, stop (1.0 when
+ *                extra_dt_constr was negative), then the sums of
+ *                Sigma*A, l_x*A, l_y*A, l_z*A, E*A.
+ * It allocates nothing: the reduction's partial records live in a static
+ * 1 MiB __device__ array inside the library (held by every GPU that loads
+ * it until exit), so n_faces is limited to 4,194,304 (larger sizes return
+ * SPLASH_E_INVALID).  The first call on a device looks up that array's
+ * device address; make it before any stream capture.  All calls share the
+ * array: calls that overlap on the GPU race.  Asynchronous on `stream`. */
+int splash_cfl_dt_noalloc(const double* U, const double* unit_centres, const double* area,
+                          int n_faces, double gam, double omega_ns, double alpha, double h0,
+                          double dt0, double* out, void* stream);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif

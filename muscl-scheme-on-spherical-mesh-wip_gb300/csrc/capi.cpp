@@ -53,6 +53,18 @@ int fail(int code, const char* fmt, ...) {
 
 }  // namespace
 
+namespace splash {
+int set_error(int code, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+}  // namespace splash
+
 struct splash_geometry {
   splash::RefGeometry g;
 };

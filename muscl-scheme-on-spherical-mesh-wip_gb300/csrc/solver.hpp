@@ -16,6 +16,10 @@ namespace splash {
 // True when the FP32/FP64 mixed kernels are compiled into the library.
 bool mixed_available();
 
+// Records the calling thread's error message (read by splash_last_error)
+// and returns `code`.
+int set_error(int code, const char* fmt, ...);
+
 struct Solver {
   // configuration
   splash_params par{};
