@@ -30,6 +30,14 @@
 #include <stddef.h>
 #include <stdint.h>
 
+/* Exported entry points; everything else in the library has hidden
+ * visibility, so no internal C++ symbol can clash with a caller's. */
+#if defined(__GNUC__)
+#define SPLASH_API __attribute__((visibility("default")))
+#else
+#define SPLASH_API
+#endif
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -96,9 +104,9 @@ typedef struct splash_geometry splash_geometry;
 
 /* ---- library ---------------------------------------------------------- */
 /* Message of the calling thread's last failure ("" if none). */
-const char* splash_last_error(void);
+SPLASH_API const char* splash_last_error(void);
 /* Library version string. */
-const char* splash_version(void);
+SPLASH_API const char* splash_version(void);
 
 /* ---- solver lifetime ---------------------------------------------------- */
 /* Replaces the constructors MUSCL_HLLE_p / MUSCL_HLLC / MUSCL_HLLCplus
@@ -112,82 +120,82 @@ const char* splash_version(void);
  * SPLASH_E_UNSUPPORTED: the reference prints "check dim", latches
  * stop_check and then indexes past the state vector
  * (physics/adiabatic.hpp:26-30, Riemann_solvers/HLLC.hpp:208). */
-int splash_create(const splash_mesh_desc* mesh, const double* U_in, int dim, double gam,
+SPLASH_API int splash_create(const splash_mesh_desc* mesh, const double* U_in, int dim, double gam,
                   double omega_ns, int accretion_on, const splash_params* params,
                   int solver_kind, int precision, int device, int threads,
                   splash_solver** out);
-int splash_destroy(splash_solver* s);
+SPLASH_API int splash_destroy(splash_solver* s);
 
 /* ---- the hot path ------------------------------------------------------ */
 /* Replaces MUSCL_base::do_step(double dt0) (MUSCL_base.hpp:97-225): one RK2
  * midpoint step with dt = min(dt0, 0.1 h0 / max_vel, extra_dt_constr()).
  * Asynchronous: enqueues one CUDA-graph replay on the solver's stream. */
-int splash_do_step(splash_solver* s, double dt0);
+SPLASH_API int splash_do_step(splash_solver* s, double dt0);
 /* `n` consecutive do_step(dt0) calls without returning to the host. */
-int splash_do_steps(splash_solver* s, int n, double dt0);
+SPLASH_API int splash_do_steps(splash_solver* s, int n, double dt0);
 /* Blocks until all enqueued steps have finished. */
-int splash_synchronize(splash_solver* s);
+SPLASH_API int splash_synchronize(splash_solver* s);
 
 /* The cudaStream_t the solver launches on (as void*), so a caller can
  * order its own work or record CUDA events against the step. */
-int splash_stream(splash_solver* s, void** stream);
+SPLASH_API int splash_stream(splash_solver* s, void** stream);
 /* Runs `reps` un-captured steps with CUDA events around every launch and
  * returns the mean device time per launch in milliseconds:
  * ms[0] dt reduction, ms[1] reconstruct (stage 1), ms[2] flux+update
  * (stage 1), ms[3] reconstruct (stage 2), ms[4] flux+update (stage 2).
  * The steps advance the state like do_step(dt0). */
-int splash_kernel_times(splash_solver* s, int reps, double dt0, double ms[5]);
+SPLASH_API int splash_kernel_times(splash_solver* s, int reps, double dt0, double ms[5]);
 /* Device bytes held by the solver: out[0] geometry, out[1] state + scratch. */
-int splash_memory(splash_solver* s, int64_t out[2]);
+SPLASH_API int splash_memory(splash_solver* s, int64_t out[2]);
 
 /* ---- accessors ---------------------------------------------------------- */
-int splash_time(splash_solver* s, double* t);               /* MUSCL_base.hpp:227-230 */
-int splash_stop_check(splash_solver* s, int* stop);         /* MUSCL_base.hpp:232-235 */
-int splash_error_word(splash_solver* s, uint32_t* bits);    /* SPLASH_STOP_* bits */
-int splash_last_dt(splash_solver* s, double* dt);           /* the clipped dt of the last step */
-int splash_steps(splash_solver* s, int64_t* steps);         /* MUSCL_base::steps */
-int splash_n_faces(splash_solver* s, int* n_faces);
-int splash_dim(splash_solver* s, int* dim);
+SPLASH_API int splash_time(splash_solver* s, double* t);               /* MUSCL_base.hpp:227-230 */
+SPLASH_API int splash_stop_check(splash_solver* s, int* stop);         /* MUSCL_base.hpp:232-235 */
+SPLASH_API int splash_error_word(splash_solver* s, uint32_t* bits);    /* SPLASH_STOP_* bits */
+SPLASH_API int splash_last_dt(splash_solver* s, double* dt);           /* the clipped dt of the last step */
+SPLASH_API int splash_steps(splash_solver* s, int64_t* steps);         /* MUSCL_base::steps */
+SPLASH_API int splash_n_faces(splash_solver* s, int* n_faces);
+SPLASH_API int splash_dim(splash_solver* s, int* dim);
 /* [n_faces][dim] conserved state, reference order (MUSCL_base::U). */
-int splash_get_state(splash_solver* s, double* U);
-int splash_set_state(splash_solver* s, const double* U);
+SPLASH_API int splash_get_state(splash_solver* s, double* U);
+SPLASH_API int splash_set_state(splash_solver* s, const double* U);
 /* Per-step diagnostics of MUSCL_base.hpp:187-214 for the current state:
  * out[0] = sum Sigma*A, out[1..3] = sum l*A, out[4] = sum E*A. */
-int splash_diagnostics(splash_solver* s, double out[5]);
+SPLASH_API int splash_diagnostics(splash_solver* s, double out[5]);
 /* Internal (space-filling-curve) position -> reference face id, [n_faces]. */
-int splash_get_permutation(splash_solver* s, int* internal_to_ref);
+SPLASH_API int splash_get_permutation(splash_solver* s, int* internal_to_ref);
 
 /* ---- writers (physics/adiabatic.hpp:101-348) ---------------------------- */
 /* Each appends one line "t  v0 v1 ... " to `path` with the reference's
  * default stream formatting (6 significant digits). */
-int splash_write_t_rho(splash_solver* s, const char* path);     /* adiabatic.hpp:101-111 */
-int splash_write_t_p(splash_solver* s, const char* path);       /* adiabatic.hpp:113-133 */
-int splash_write_t_curl(splash_solver* s, const char* path);    /* adiabatic.hpp:135-177 */
-int splash_write_t_omega_z(splash_solver* s, const char* path); /* adiabatic.hpp:195-226 */
+SPLASH_API int splash_write_t_rho(splash_solver* s, const char* path);     /* adiabatic.hpp:101-111 */
+SPLASH_API int splash_write_t_p(splash_solver* s, const char* path);       /* adiabatic.hpp:113-133 */
+SPLASH_API int splash_write_t_curl(splash_solver* s, const char* path);    /* adiabatic.hpp:135-177 */
+SPLASH_API int splash_write_t_omega_z(splash_solver* s, const char* path); /* adiabatic.hpp:195-226 */
 /* three files, Lx/Ly/Lz (adiabatic.hpp:179-193) */
-int splash_write_t_L(splash_solver* s, const char* path_x, const char* path_y,
+SPLASH_API int splash_write_t_L(splash_solver* s, const char* path_x, const char* path_y,
                      const char* path_z);
 /* out[4] = flux towards observers at 0, 45, 90, 180 deg (adiabatic.hpp:228-333) */
-int splash_get_light_curves(splash_solver* s, double out[4]);
+SPLASH_API int splash_get_light_curves(splash_solver* s, double out[4]);
 /* [n_faces] lines of dim values (adiabatic.hpp:335-348) */
-int splash_write_final_state(splash_solver* s, const char* path);
+SPLASH_API int splash_write_final_state(splash_solver* s, const char* path);
 
 /* ---- geometry (host, reference numbering) ------------------------------ */
 /* Builds the reference geometry (geometry/MUSCL_geometry.hpp:43-575) for a
  * mesh description; used by the drop-in classes' geometry writers
  * (MUSCL_geometry.hpp:1069-1117) and by the test-suite. */
-int splash_geometry_build(const splash_mesh_desc* mesh, int threads, splash_geometry** out);
-int splash_geometry_free(splash_geometry* g);
+SPLASH_API int splash_geometry_build(const splash_mesh_desc* mesh, int threads, splash_geometry** out);
+SPLASH_API int splash_geometry_free(splash_geometry* g);
 /* sizes[0..3] = n_vertices, n_faces, n_slots, max_slots;
  * scalars[0..1] = h0, round_diff */
-int splash_geometry_info(const splash_geometry* g, int64_t sizes[4], double scalars[2]);
+SPLASH_API int splash_geometry_info(const splash_geometry* g, int64_t sizes[4], double scalars[2]);
 /* Copies the named array into dst (capacity `bytes`).  Names: vertices,
  * face_off, face_vtx, nbr_off, nbr, nbr_edge, face_centers, normals, area,
  * edge_normals, bm_dist, h_plus, h_minus, ff_plus, ff_minus, beta_plus,
  * beta_minus, and hilbert_order (internal position -> reference face id,
  * the numbering splash_create uses).  *written receives the byte count
  * (may be NULL). */
-int splash_geometry_get(const splash_geometry* g, const char* name, void* dst, size_t bytes,
+SPLASH_API int splash_geometry_get(const splash_geometry* g, const char* name, void* dst, size_t bytes,
                         size_t* written);
 
 /* ---- allocation-free CFL clip --------------------------------------------
@@ -210,7 +218,7 @@ int splash_geometry_get(const splash_geometry* g, const char* name, void* dst, s
  * SPLASH_E_INVALID).  The first call on a device looks up that array's
  * device address; make it before any stream capture.  All calls share the
  * array: calls that overlap on the GPU race.  Asynchronous on `stream`. */
-int splash_cfl_dt_noalloc(const double* U, const double* unit_centres, const double* area,
+SPLASH_API int splash_cfl_dt_noalloc(const double* U, const double* unit_centres, const double* area,
                           int n_faces, double gam, double omega_ns, double alpha, double h0,
                           double dt0, double* out, void* stream);
 

@@ -29,13 +29,13 @@ LIBNAME = "libsplash_gb300.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CXXFLAGS = ["-std=c++17", "-O3", "-fPIC", "-fopenmp", "-ffp-contract=off", "-Wall",
-            "-Wno-unknown-pragmas"]
+            "-Wno-unknown-pragmas", "-fvisibility=hidden", "-fvisibility-inlines-hidden"]
 # per-.cu extra flags: the FP64 path must not fuse multiply-adds (reference
 # operand order); the mixed path may.
 CU_FLAGS = {
     "step_fp64.cu": ["-fmad=false"],
     "cfl_noalloc.cu": ["-fmad=false"],
-    "step_mixed.cu": ["-fmad=true"],
+    "step_mixed.cu": ["-fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"],
 }
 
 
@@ -83,6 +83,7 @@ def build_library(verbose: bool = False, force: bool = False) -> Path:
         objs.append(obj)
         if force or _newer(src, obj, headers):
             jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+                         "-Xcompiler", "-fvisibility=hidden",
                          *CU_FLAGS.get(src.name, []), f"-I{INCLUDE}", f"-I{CSRC}",
                          "-c", str(src), "-o", str(obj)])
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:

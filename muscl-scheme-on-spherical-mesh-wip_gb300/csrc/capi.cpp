@@ -259,7 +259,7 @@ void Solver::build_device_geometry(const RefGeometry& g) {
     // FP32 slot planes; FP64 for the values feeding FP64 steps
     auto tof = [](const std::vector<double>& v) { return std::vector<float>(v.begin(), v.end()); };
     std::vector<float> h_invh(2 * PS, 1.0f);
-    std::vector<double> h_coef(PS, 0.0);
+    std::vector<float> h_coef(PS, 0.0f);
     for (size_t q = 0; q < PS; ++q) {
       h_invh[q] = (float)(1.0 / h_hpm[q]);
       h_invh[PS + q] = (float)(1.0 / h_hpm[PS + q]);
@@ -267,7 +267,7 @@ void Solver::build_device_geometry(const RefGeometry& g) {
     for (int i = 0; i < nf; ++i)
       for (int j = 0; j < (int)h_nslots[i]; ++j) {
         const size_t q = (size_t)j * fpad + i;
-        h_coef[q] = g.round_diff * h_chord[q] / h_area[i];
+        h_coef[q] = (float)(g.round_diff * h_chord[q] / h_area[i]);
       }
     GM.n_faces = nf;
     GM.fpad = fpad;
@@ -288,7 +288,7 @@ void Solver::build_device_geometry(const RefGeometry& g) {
     GM.nxr = upload(tof(h_nxr));
     GM.coef = upload(h_coef);
     GM.rev = upload(h_rev);
-    geometry_bytes = h_nslots.size() + 8 * (h_fcn.size() + h_area.size() + h_acc.size() + h_coef.size()) +
+    geometry_bytes = h_nslots.size() + 8 * (h_fcn.size() + h_area.size() + h_acc.size()) + 4 * h_coef.size() +
                      4 * (h_fcn.size() + h_sten.size() + h_rev.size() + h_beta.size() + h_invh.size() +
                           h_bm.size() + h_eta.size() + h_arc.size() + h_ec.size() + h_en.size() +
                           h_nxr.size());

@@ -18,7 +18,10 @@ cudaError_t fp64_set_dt0(const DevState& S, double dt0, cudaStream_t st);
 cudaError_t fp64_step(const DevGeom& G, const DevState& S, const PhysParams& P, cudaStream_t st,
                       cudaEvent_t* ev = nullptr);
 // The dt clip (one block) shared by both paths.
-cudaError_t dt_reduce(const DevState& S, const PhysParams& P, int nblocks, cudaStream_t st);
+// squared_speeds: the partials hold max |v|^2 (mixed path), so the finalize
+// takes the square root of the reduced maximum.
+cudaError_t dt_reduce(const DevState& S, const PhysParams& P, int nblocks, cudaStream_t st,
+                      bool squared_speeds = false);
 cudaError_t fp64_scatter_state(const double* aos, const int* perm, double* U, int n_faces, int fpad,
                                cudaStream_t st);
 cudaError_t fp64_gather_state(const double* U, const int* perm, double* aos, int n_faces, int fpad,

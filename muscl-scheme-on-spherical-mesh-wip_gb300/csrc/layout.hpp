@@ -85,7 +85,7 @@ struct DevGeomMixed {
   const float* ec;        // 3 planes, unit edge centre
   const float* en;        // 3 planes
   const float* nxr;       // 3 planes
-  const double* coef;     // round_diff * chord / area (FP64)
+  const float* coef;      // round_diff * chord / area
   const int* rev;
 };
 

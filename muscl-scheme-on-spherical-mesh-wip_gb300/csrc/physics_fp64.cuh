@@ -46,7 +46,7 @@ __device__ __forceinline__ double pressure(const double* u, double vn, double ga
 // MUSCL_base.hpp:517-539 (u[4] = energy, r = unit face centre)
 __device__ __forceinline__ double pressure_fc(const double* u, D3 r, double gam) {
   D3 vel = cross3(r, d3(u[1], u[2], u[3]));
-  vel = divs(vel, -u[0]);
+  vel = scal(vel, 1.0 / (-u[0]));
   const double n = norm3(vel);
   return smax(1e-16, (u[4] - u[0] * (n * n) / 2) * (gam - 1));
 }
@@ -54,7 +54,7 @@ __device__ __forceinline__ double pressure_fc(const double* u, D3 r, double gam)
 // MUSCL_base.hpp:541-562 (u[4] = pressure, r = unit edge centre)
 __device__ __forceinline__ double energy_at_edge(const double* u, D3 r, double gam) {
   D3 vel = cross3(r, d3(u[1], u[2], u[3]));
-  vel = divs(vel, -u[0]);
+  vel = scal(vel, 1.0 / (-u[0]));
   const double n = norm3(vel);
   return 1 / (gam - 1) * u[4] + u[0] * (n * n) / 2;
 }
@@ -70,7 +70,7 @@ struct SlotGeom {
 // velocity at the edge: cross(ec, l) / ((-u0) |ec|)   (adiabatic.hpp:375-376)
 __device__ __forceinline__ D3 edge_vel(const double* u, const SlotGeom& g) {
   const D3 v = cross3(g.ec, d3(u[1], u[2], u[3]));
-  return divs(v, (-u[0]) * g.ecn);
+  return scal(v, 1.0 / ((-u[0]) * g.ecn));
 }
 
 // physics/adiabatic.hpp:352-392
@@ -131,9 +131,10 @@ __device__ __forceinline__ unsigned flux_star(const double* uL, const double* uR
 #pragma unroll
       for (int i = 0; i < kDim; ++i) F[i] = FL[i];
     } else if (S_L < 0 && S_R > 0) {
+      const double inv = 1.0 / (S_R - S_L);
 #pragma unroll
       for (int i = 0; i < kDim; ++i)
-        F[i] = (S_R * FL[i] - S_L * FR[i] + S_R * S_L * (uR[i] - uL[i])) / (S_R - S_L);
+        F[i] = (S_R * FL[i] - S_L * FR[i] + S_R * S_L * (uR[i] - uL[i])) * inv;
     } else {
       // S_R <= 0, or NaN wave speeds (reference prints and stops)
       if (!(S_R <= 0)) bits |= 4u;
@@ -182,8 +183,9 @@ __device__ __forceinline__ unsigned flux_star(const double* uL, const double* uR
   const double Sk = (side == 1) ? S_L : S_R;
   const double* uk = (side == 1) ? uL : uR;
   const double* Fk = (side == 1) ? FL : FR;
+  const double inv_k = 1.0 / (Sk - S_star);
 #pragma unroll
-  for (int i = 0; i < kDim; ++i) F[i] = (S_star * (Sk * uk[i] - Fk[i]) + Sk * P_LR * D[i]) / (Sk - S_star);
+  for (int i = 0; i < kDim; ++i) F[i] = (S_star * (Sk * uk[i] - Fk[i]) + Sk * P_LR * D[i]) * inv_k;
   if (solver == 3) {
     F[0] = F[0] + 0.0;  // flux_fix[0] = 0 is added like the other fields
     const double phi_L = uL[0] * (S_L - V_L);
@@ -199,37 +201,47 @@ __device__ __forceinline__ unsigned flux_star(const double* uL, const double* uR
     double f_star = 1;
     if (lambd_L == 0 && lambd_R == 0) f_star = M * sqrt(4 + (1 - M * M) * (1 - M * M)) / ((1 + M * M));
     const double h = smin(p_L / p_R, p_R / p_L);
-    const double gsw = 1 - pow(h, M);
+    const double gsw = 1 - exp(M * log(h));
     const double dV = V_R - V_L;
     const D3 dv = sub(vel_R, vel_L);
-    const double cs = Sk / (Sk - S_star) * gsw;
+    const double cs = Sk * inv_k * gsw;
     const D3 vff = d3((f_star - 1) * dV * g.en.x + cs * (dv.x - dV * g.en.x),
                       (f_star - 1) * dV * g.en.y + cs * (dv.y - dV * g.en.y),
                       (f_star - 1) * dV * g.en.z + cs * (dv.z - dV * g.en.z));
     const D3 am = cross3(g.ec, vff);
-    F[1] = F[1] + am.x * phi_L * phi_R / (phi_R - phi_L);
-    F[2] = F[2] + am.y * phi_L * phi_R / (phi_R - phi_L);
-    F[3] = F[3] + am.z * phi_L * phi_R / (phi_R - phi_L);
-    F[4] = F[4] + (f_star - 1) * (V_R - V_L) * S_star * phi_L * phi_R / (phi_R - phi_L);
+    const double w = phi_L * phi_R / (phi_R - phi_L);
+    F[1] = F[1] + am.x * w;
+    F[2] = F[2] + am.y * w;
+    F[3] = F[3] + am.z * w;
+    F[4] = F[4] + (f_star - 1) * (V_R - V_L) * S_star * w;
   }
   return bits;
 }
 
-// h(r) switch of physics/adiabatic.hpp:692-702
+// h(r) switch of physics/adiabatic.hpp:692-702.  pow(1 - r, 0.1) is
+// evaluated as exp(0.1 log(1 - r)) and the integer powers as products: the
+// same function, at a fraction of the FP64 instruction count of the
+// correctly rounded pow (GB300's FP64 pipe is the bottleneck of this path).
 __device__ __forceinline__ double limiter_switch(double r) {
   double o = 0;
-  if (r < 1 && r > 0) o = (1 - tanh(4 * (r * r) * pow(1 - r, 0.1)));
-  if (r >= 1) o = pow(tanh(10 * pow(r - 1, 3.0)), 6.0);
+  if (r < 1 && r > 0) o = (1 - tanh(4 * (r * r) * exp(0.1 * log(1 - r))));
+  if (r >= 1) {
+    const double x = r - 1;
+    const double t = tanh(10 * ((x * x) * x));
+    const double t2 = t * t;
+    o = (t2 * t2) * t2;
+  }
   return o;
 }
 
 // physics/adiabatic.hpp:685-828 for one field: blend of the third-order
-// limiter and the irregular-grid superbee, NaN ratio -> 0.
-__device__ __forceinline__ double limiter_field(double r, double nu_plus, double eta_p,
-                                                double eta_m, double twoN) {
+// limiter and the irregular-grid superbee, NaN ratio -> 0.  sb_scale is
+// eta_minus / (2 N nu_plus) and to_scale is (1 + nu_plus) / 3, both per slot.
+__device__ __forceinline__ double limiter_field(double r, double eta_p, double sb_scale,
+                                                double to_scale) {
   if (isnan(r)) return 0.0;
-  const double sb = smax(0., smax(smin(1., eta_m * r / (twoN * nu_plus)), smin(r, eta_p)));
-  const double to = smax(0., smin(sb, 1 + (1 + nu_plus) / 3 * (r - 1)));
+  const double sb = smax(0., smax(smin(1., r * sb_scale), smin(r, eta_p)));
+  const double to = smax(0., smin(sb, 1 + to_scale * (r - 1)));
   const double hv = limiter_switch(r);
   return ((1 - hv) * to + hv * sb);
 }
@@ -296,14 +308,17 @@ __device__ __forceinline__ void source_term(const double* w, D3 fcn, double acc0
   const double c_sigma = 4.85e36;
   const double k_m = 1.6e-13;
   const double kappa = 3.4e6;
-  const double C = 12. / 5 * k_m * w[0] / w[4] * pow(3. / 4 * c_sigma * g_eff * w[0], 1. / 4);
+  const double C = 12. / 5 * k_m * w[0] / w[4] * sqrt(sqrt(3. / 4 * c_sigma * g_eff * w[0]));
   const double beta_switch = 0.736194670678821;
   const double C_switch = -1 - 1 / (beta_switch - 1);
   double beta;
   if (C <= C_switch)
     beta = 1 - 1 / (1 + C);
   else
-    beta = 1 - pow(2 / C, 4.0);
+  {
+    const double x2 = (2 / C) * (2 / C);
+    beta = 1 - x2 * x2;
+  }
   const double beta_ceil = 1 - 1e-8, beta_floor = 1e-8;
   if (beta < beta_floor || isnan(beta)) beta = beta_floor;
   if (beta > beta_ceil) beta = beta_ceil;

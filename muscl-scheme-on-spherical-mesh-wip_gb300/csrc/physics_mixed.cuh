@@ -165,7 +165,7 @@ __device__ __forceinline__ unsigned flux_star(const float* uL, const float* uR, 
     float f_star = 1.f;
     if (lambd == 0) f_star = M * sqrtf(4.f + (1.f - M * M) * (1.f - M * M)) / (1.f + M * M);
     const float h = smin(L.p / R.p, R.p / L.p);
-    const float gsw = 1.f - powf(h, M);
+    const float gsw = 1.f - __expf(M * __logf(h));
     const float dV = V_R - V_L;
     const F3 dv = sub(R.vel, L.vel);
     const float cs = Sk * inv * gsw;
@@ -182,13 +182,19 @@ __device__ __forceinline__ unsigned flux_star(const float* uL, const float* uR, 
   return bits;
 }
 
-// h(r) switch and the blended limiter (physics/adiabatic.hpp:685-828)
+// h(r) switch and the blended limiter (physics/adiabatic.hpp:685-828).
+// On (0, 1) the switch is 1 - tanh(y) = 2 / (1 + e^{2y}) (no cancellation);
+// for r >= 1 it is tanh(y)^6 = ((e^{2y} - 1) / (e^{2y} + 1))^6.
 __device__ __forceinline__ float limiter_switch(float r) {
   float o = 0.f;
-  if (r < 1.f && r > 0.f) o = 1.f - tanhf(4.f * (r * r) * __expf(0.1f * __logf(1.f - r)));
+  if (r < 1.f && r > 0.f) {
+    const float y = 4.f * (r * r) * __expf(0.1f * __logf(1.f - r));
+    o = __fdividef(2.f, 1.f + __expf(2.f * y));
+  }
   if (r >= 1.f) {
     const float x = r - 1.f;
-    const float t = tanhf(10.f * (x * x * x));
+    const float e = __expf(fminf(20.f * (x * x * x), 80.f));
+    const float t = __fdividef(e - 1.f, e + 1.f);
     const float t2 = t * t;
     o = t2 * t2 * t2;
   }

@@ -54,9 +54,10 @@ __global__ void __launch_bounds__(kBlock) prepare_kernel(DevGeom G, DevState S, 
 }
 
 // dt = min(dt0, 0.1 h0 / max_vel, extra_dt)  (MUSCL_base.hpp:100-115)
-__global__ void __launch_bounds__(256) dt_kernel(DevState S, PhysParams P, int nblocks) {
+__global__ void __launch_bounds__(256) dt_kernel(DevState S, PhysParams P, int nblocks,
+                                                 int squared_speeds) {
   __shared__ double sm[256][7];
-  double v[7] = {1e-8, 1e20, 0, 0, 0, 0, 0};
+  double v[7] = {squared_speeds ? 1e-16 : 1e-8, 1e20, 0, 0, 0, 0, 0};
   for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
     const double* p = S.partial + (size_t)b * kPartialStride;
     v[0] = fmax(v[0], p[0]);
@@ -77,7 +78,7 @@ __global__ void __launch_bounds__(256) dt_kernel(DevState S, PhysParams P, int n
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    const double max_vel = sm[0][0];
+    const double max_vel = squared_speeds ? sqrt(sm[0][0]) : sm[0][0];
     double extra = sm[0][1];
     if (extra < 0) {
       atomicOr(S.err, 8u);  // SPLASH_STOP_NEG_EXTRA_DT
@@ -98,32 +99,34 @@ __global__ void __launch_bounds__(256) dt_kernel(DevState S, PhysParams P, int n
 // find_U_edges (MUSCL_base.hpp:361-434) for every slot of one face.
 __global__ void __launch_bounds__(kBlock) reconstruct_kernel(DevGeom G, const double* __restrict__ W,
                                                              double* __restrict__ uplus,
-                                                             const double* __restrict__ scal,
+                                                             const double* __restrict__ sc,
                                                              PhysParams P) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= G.n_faces) return;
   const int fp = G.fpad;
   const int PS = G.max_slots * fp;  // one slot-plane set
-  const double dt = scal[kScDt];
+  const double dt = sc[kScDt];
   double w[kDim];
 #pragma unroll
   for (int k = 0; k < kDim; ++k) w[k] = W[k * fp + f];
   const int n = G.nslots[f];
   const double twoN = (double)(2 * n);
   const double gam = P.gam;
+  const double c = sqrt(gam * (w[4] + 0.0) / (w[0] + 0.0));  // sound speed (per face)
   for (int j = 0; j < n; ++j) {
     const int s = j * fp + f;
     const int ia = G.sten[s], ib = G.sten[PS + s], ic = G.sten[2 * PS + s], id = G.sten[3 * PS + s];
     const double bp0 = G.beta[s], bp1 = G.beta[PS + s], bm0 = G.beta[2 * PS + s], bm1 = G.beta[3 * PS + s];
     const double hp = G.hpm[s], hm = G.hpm[PS + s], bmd = G.bm[s];
+    const double ihp = 1.0 / hp, ihm = 1.0 / hm;
     double pp[kDim], r[kDim];
 #pragma unroll
     for (int k = 0; k < kDim; ++k) {
       const double* Wk = W + k * fp;
       const double Up = bp0 * Wk[ia] + bp1 * Wk[ib];
-      pp[k] = (Up - w[k]) / hp;
+      pp[k] = (Up - w[k]) * ihp;
       const double Um = bm0 * Wk[ic] + bm1 * Wk[id];
-      const double pm = (-Um + w[k]) / hm;
+      const double pm = (-Um + w[k]) * ihm;
       r[k] = pm / pp[k];
     }
     // Courant factor of the limiter (adiabatic.hpp:741-758, 792-810)
@@ -131,15 +134,15 @@ __global__ void __launch_bounds__(kBlock) reconstruct_kernel(DevGeom G, const do
     const double ecn = G.ecn[s];
     const D3 en = plane3(G.en, PS, s);
     D3 vel = cross3(ec, d3(w[1], w[2], w[3]));
-    vel = divs(vel, (-w[0] - 0.0) * ecn);
-    const double p = w[4] + 0.0;
-    const double c = sqrt(gam * p / (w[0] + 0.0));
+    vel = scal(vel, 1.0 / ((-w[0] - 0.0) * ecn));
     const double nu_plus = (c + dot3(vel, en)) * dt * G.arc_a[s];
-    const double eta_p = G.eta[s], eta_m = G.eta[PS + s];
+    const double eta_p = G.eta[s];
+    const double sb_scale = G.eta[PS + s] / (twoN * nu_plus);
+    const double to_scale = (1 + nu_plus) / 3;
     double up[kDim];
 #pragma unroll
     for (int k = 0; k < kDim; ++k) {
-      const double lim = limiter_field(r[k], nu_plus, eta_p, eta_m, twoN);
+      const double lim = limiter_field(r[k], eta_p, sb_scale, to_scale);
       if (k == 0 || k == 4)
         up[k] = w[k] + 0.0 + pp[k] * lim * bmd;
       else
@@ -249,8 +252,9 @@ cudaError_t fp64_prepare(const DevGeom& G, const DevState& S, const PhysParams& 
   return cudaGetLastError();
 }
 
-cudaError_t dt_reduce(const DevState& S, const PhysParams& P, int nblocks, cudaStream_t st) {
-  f64::dt_kernel<<<1, 256, 0, st>>>(S, P, nblocks);
+cudaError_t dt_reduce(const DevState& S, const PhysParams& P, int nblocks, cudaStream_t st,
+                      bool squared_speeds) {
+  f64::dt_kernel<<<1, 256, 0, st>>>(S, P, nblocks, squared_speeds ? 1 : 0);
   return cudaGetLastError();
 }
 
@@ -263,7 +267,7 @@ cudaError_t fp64_step(const DevGeom& G, const DevState& S, const PhysParams& P, 
                       cudaEvent_t* ev) {
   const int nb = f64::blocks_for(G.n_faces);
   if (ev) cudaEventRecord(ev[0], st);
-  f64::dt_kernel<<<1, 256, 0, st>>>(S, P, nb);
+  f64::dt_kernel<<<1, 256, 0, st>>>(S, P, nb, 0);
   if (ev) cudaEventRecord(ev[1], st);
   f64::reconstruct_kernel<<<nb, f64::kBlock, 0, st>>>(G, S.W0, S.uplus, S.scal, P);
   if (ev) cudaEventRecord(ev[2], st);

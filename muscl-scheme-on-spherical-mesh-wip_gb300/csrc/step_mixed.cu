@@ -38,19 +38,45 @@ __device__ __forceinline__ f64::D3 plane3d(const double* p, int stride, int i) {
 }
 
 // FP64 pressure recovery with one division: Pi = (E - |r x l|^2/(2 Sigma))(gam-1),
-// floored at 1e-16 like MUSCL_base.hpp:538.
-__device__ __forceinline__ double pressure_recover(const double* u, f64::D3 r, double gam) {
+// floored at 1e-16 like MUSCL_base.hpp:538.  Also returns |v|^2 and 1/Sigma
+// for the dt candidates.
+__device__ __forceinline__ double pressure_recover(const double* u, f64::D3 r, double gam,
+                                                   double& v2, double& inv_rho) {
   const f64::D3 c = f64::cross3(r, f64::d3(u[1], u[2], u[3]));
-  const double ke = (c.x * c.x + c.y * c.y + c.z * c.z) / (2.0 * u[0]);
-  const double p = (u[4] - ke) * (gam - 1.0);
+  inv_rho = 1.0 / u[0];
+  const double c2 = c.x * c.x + c.y * c.y + c.z * c.z;
+  v2 = c2 * inv_rho * inv_rho;
+  const double p = (u[4] - 0.5 * c2 * inv_rho) * (gam - 1.0);
   return (1e-16 < p) ? p : 1e-16;
 }
 
-__device__ __forceinline__ void store_w32(float* W32, int fp, int f, const double* u, f64::D3 r,
-                                          double gam) {
+__device__ __forceinline__ void store_w32(float* W32, int fp, int f, const double* u, double p) {
 #pragma unroll
   for (int k = 0; k < 4; ++k) W32[k * fp + f] = (float)u[k];
-  W32[4 * fp + f] = (float)pressure_recover(u, r, gam);
+  W32[4 * fp + f] = (float)p;
+}
+
+// dt candidates in FP64 with one sqrt and one division: the CFL maximum is
+// reduced over squared speeds max(|v|^2, gam p / Sigma) (the square root is
+// monotone, so the dt finalize takes one sqrt of the maximum), and
+// extra_dt_constr (physics/adiabatic.hpp:543-580) simplifies to
+// 0.01 p / (alpha k g_eff Sigma |v - v0|) with k = gam3d / (2 gam3d - 1).
+__device__ __forceinline__ void dt_candidates_sq(const double* u, f64::D3 r, double area, double p,
+                                                 double v2, double inv_rho, const PhysParams& P,
+                                                 double& vmax2, double& dmin, double sums[5]) {
+  vmax2 = fmax(v2, P.gam * p * inv_rho);
+  const f64::D3 c = f64::cross3(r, f64::d3(u[1], u[2], u[3]));
+  // v = (r x l) / (-Sigma) ; v0 = omega_ns z x r
+  const double vx = -c.x * inv_rho + P.omega_ns * r.y;
+  const double vy = -c.y * inv_rho - P.omega_ns * r.x;
+  const double vz = -c.z * inv_rho;
+  const double dv = sqrt(vx * vx + vy * vy + vz * vz);
+  const double gam3d = 1 / (2 - P.gam);
+  const double k = gam3d / (2 * gam3d - 1);
+  const double g_eff = 0.217909 - v2;
+  dmin = 0.01 * p / (P.alpha * k * g_eff * u[0] * dv);
+#pragma unroll
+  for (int q = 0; q < 5; ++q) sums[q] = u[q] * area;
 }
 
 // physics/adiabatic.hpp:396-541 in FP32, except the accretion mass source
@@ -130,8 +156,10 @@ __global__ void __launch_bounds__(kBlock) prepare_kernel(DevGeomMixed G, DevStat
 #pragma unroll
     for (int k = 0; k < kDim; ++k) u[k] = S.U[k * G.fpad + f];
     const f64::D3 r = plane3d(G.fcn, G.fpad, f);
-    store_w32(S.W32, G.fpad, f, u, r, P.gam);
-    f64::dt_candidates(u, r, G.area[f], P, vmax, dmin, sums);
+    double v2, inv_rho;
+    const double p = pressure_recover(u, r, P.gam, v2, inv_rho);
+    store_w32(S.W32, G.fpad, f, u, p);
+    dt_candidates_sq(u, r, G.area[f], p, v2, inv_rho, P, vmax, dmin, sums);
   }
   red::block_partials<kBlock>(vmax, dmin, sums, S.partial + (size_t)blockIdx.x * kPartialStride);
 }
@@ -214,7 +242,7 @@ __global__ void __launch_bounds__(kBlock) flux_update_kernel(DevGeomMixed G, Dev
       g.en = plane3f(G.en, PS, s);
       g.nxr = plane3f(G.nxr, PS, s);
       bits |= flux_star(uL, uR, g, gam, P.solver, F);
-      const float cf = (float)(dt_here * G.coef[s]);
+      const float cf = dtf * G.coef[s];
 #pragma unroll
       for (int k = 0; k < kDim; ++k) {
         if (isnan(F[k])) bits |= 1u;
@@ -222,20 +250,22 @@ __global__ void __launch_bounds__(kBlock) flux_update_kernel(DevGeomMixed G, Dev
       }
     }
     if (bits) atomicOr(S.err, bits);
+    // the compensated FP32 sum is rounded once to FP32 (an increment of
+    // dt * Phi, small against U) and added to the FP64 state; U0 stays in
+    // S.U until stage 2 overwrites it
     double u[kDim];
 #pragma unroll
-    for (int k = 0; k < kDim; ++k)
-      u[k] = S.U[k * fp + f] + ((double)acc[k].hi + (double)acc[k].lo);
+    for (int k = 0; k < kDim; ++k) u[k] = S.U[k * fp + f] + (double)(acc[k].hi + acc[k].lo);
     if (P.accretion_on) u[0] += dt_here * acc0;  // accretion mass source in FP64
     if (u[0] < 1e-8) u[0] = 1e-8;
     const f64::D3 r = plane3d(G.fcn, fp, f);
-    store_w32(S.W32, fp, f, u, r, P.gam);
+    double v2, inv_rho;
+    const double p = pressure_recover(u, r, P.gam, v2, inv_rho);
+    store_w32(S.W32, fp, f, u, p);
     if (STAGE == 2) {
 #pragma unroll
       for (int k = 0; k < kDim; ++k) S.U[k * fp + f] = u[k];
-      f64::dt_candidates(u, r, G.area[f], P, vmax, dmin, sums);
-    } else {
-      // the stage-2 combine needs U0, which stays in S.U untouched
+      dt_candidates_sq(u, r, G.area[f], p, v2, inv_rho, P, vmax, dmin, sums);
     }
   }
   if (STAGE == 2)
@@ -259,7 +289,7 @@ cudaError_t mixed_step(const DevGeomMixed& G, const DevState& S, const PhysParam
                        cudaStream_t st, cudaEvent_t* ev) {
   const int nb = mx::blocks_for(G.n_faces);
   if (ev) cudaEventRecord(ev[0], st);
-  cudaError_t e = dt_reduce(S, P, nb, st);
+  cudaError_t e = dt_reduce(S, P, nb, st, /*squared_speeds=*/true);
   if (e != cudaSuccess) return e;
   if (ev) cudaEventRecord(ev[1], st);
   mx::reconstruct_kernel<<<nb, mx::kBlock, 0, st>>>(G, S, P);
