@@ -192,11 +192,50 @@ SPLASH_API int splash_geometry_info(const splash_geometry* g, int64_t sizes[4], 
 /* Copies the named array into dst (capacity `bytes`).  Names: vertices,
  * face_off, face_vtx, nbr_off, nbr, nbr_edge, face_centers, normals, area,
  * edge_normals, bm_dist, h_plus, h_minus, ff_plus, ff_minus, beta_plus,
- * beta_minus, and hilbert_order (internal position -> reference face id,
- * the numbering splash_create uses).  *written receives the byte count
+ * beta_minus, unit_face_centers (fc/|fc|), and hilbert_order (internal
+ * position -> reference face id, the numbering splash_create uses).  *written receives the byte count
  * (may be NULL). */
 SPLASH_API int splash_geometry_get(const splash_geometry* g, const char* name, void* dst, size_t bytes,
                         size_t* written);
+
+/* ---- ensembles -------------------------------------------------------------
+ * Many independent solvers (different meshes, parameters and states, each
+ * with its own CFL dt) advanced together: one do_step of the ensemble is one
+ * CUDA-graph replay whose launches cover every member.  No counterpart in the
+ * reference, which runs one solver per process; each member computes exactly
+ * what splash_create/splash_do_step with SPLASH_PREC_MIXED would.  Members on
+ * the same mesh share its geometry on the device. */
+typedef struct splash_member {
+  int mesh_kind;        /* splash_mesh_kind */
+  int level;            /* subdivision level */
+  const double* U_in;   /* [n_faces][5] conserved state, reference face order */
+  double gam;
+  double omega_ns;
+  int accretion_on;
+  splash_params params;
+  int solver_kind;      /* splash_solver_kind */
+} splash_member;
+
+typedef struct splash_ensemble splash_ensemble;
+
+/* Builds the ensemble (FP32/FP64 mixed precision).  With `autotune` != 0 the
+ * block schedule (member order of the face tiles, reconstruction tile width)
+ * is picked by timing every candidate for a few steps on the ensemble itself;
+ * the state is restored afterwards. */
+SPLASH_API int splash_ensemble_create(const splash_member* members, int n, int device, int autotune,
+                           splash_ensemble** out);
+SPLASH_API int splash_ensemble_destroy(splash_ensemble* e);
+/* n steps of every member: member i advances by min(dt0, its CFL clip). */
+SPLASH_API int splash_ensemble_do_steps(splash_ensemble* e, int n, double dt0);
+SPLASH_API int splash_ensemble_synchronize(splash_ensemble* e);
+SPLASH_API int splash_ensemble_stream(splash_ensemble* e, void** stream);
+SPLASH_API int splash_ensemble_get_state(splash_ensemble* e, int member, double* U);
+/* out = {t, dt of the last step, max_vel, extra_dt}; err = stop bits */
+SPLASH_API int splash_ensemble_member_info(splash_ensemble* e, int member, double out[4], uint32_t* err);
+/* The chosen schedule and the autotuner's per-candidate ms per step
+ * (index order*3 + {64,128,256}-wide tiles). */
+SPLASH_API int splash_ensemble_schedule(splash_ensemble* e, int* order, int* recon_width, double trial_ms[9]);
+SPLASH_API int splash_ensemble_size(splash_ensemble* e, int* n_members, int64_t* total_faces);
 
 /* ---- allocation-free CFL clip --------------------------------------------
  * No counterpart in the reference: an addition for callers that cannot

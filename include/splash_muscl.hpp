@@ -261,15 +261,9 @@ class Solver {
   void write_face_centers() {
     Geometry g(mesh_);
     std::ofstream os("results/face_centers.dat");
-    const std::vector<double>& fc = g.d("face_centers");
-    for (size_t i = 0; i + 2 < fc.size(); i += 3) {
-      double s = 0.0;
-      s += fc[i] * fc[i];
-      s += fc[i + 1] * fc[i + 1];
-      s += fc[i + 2] * fc[i + 2];
-      const double n = std::sqrt(s);
-      os << std::setprecision(15) << fc[i] / n << " " << fc[i + 1] / n << " " << fc[i + 2] / n << "\n";
-    }
+    const std::vector<double>& u = g.d("unit_face_centers");
+    for (size_t i = 0; i + 2 < u.size(); i += 3)
+      os << std::setprecision(15) << u[i] << " " << u[i + 1] << " " << u[i + 2] << "\n";
   }
   void write_faces() {
     Geometry g(mesh_);

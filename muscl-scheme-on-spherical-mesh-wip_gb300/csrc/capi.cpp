@@ -27,6 +27,7 @@
 #include "kernels.hpp"
 #include "layout.hpp"
 #include "mesh.hpp"
+#include "slot_planes.hpp"
 #include "solver.hpp"
 
 namespace {
@@ -147,184 +148,66 @@ inline double smax(double a, double b) { return (a < b) ? b : a; }
 
 namespace splash {
 
-// Host precompute of every slot-plane array; see layout.hpp.
+// Uploads the slot planes of one mesh for the solver's precision.
 void Solver::build_device_geometry(const RefGeometry& g) {
-  const int nf = g.n_faces;
-  n_faces = nf;
-  max_slots = g.max_slots;
-  fpad = (nf + 31) / 32 * 32;
-  const size_t PS = (size_t)max_slots * fpad;
-
-  perm = hilbert_order(g.face_centers.data(), nf);
-  iperm.assign(nf, 0);
-  for (int i = 0; i < nf; ++i) iperm[perm[i]] = i;
-
-  // reference-order reverse slot (std::find of MUSCL_base.hpp:383-384)
-  std::vector<int> j0_of(g.n_slots, -1);
-  for (int f = 0; f < nf; ++f) {
-    for (int s = g.face_off[f]; s < g.face_off[f + 1]; ++s) {
-      const int nb = g.nbr_edge[s];
-      int j0 = -1;
-      for (int q = g.face_off[nb]; q < g.face_off[nb + 1]; ++q)
-        if (g.nbr_edge[q] == f) {
-          j0 = q - g.face_off[nb];
-          break;
-        }
-      if (j0 < 0) throw std::runtime_error("edge neighbour relation is not symmetric");
-      j0_of[s] = j0;
-    }
-  }
-
-  std::vector<int8_t> h_nslots(fpad, 0);
-  std::vector<double> h_fcn(3 * (size_t)fpad, 0.0), h_area(fpad, 1.0), h_acc(fpad, 0.0);
-  std::vector<int> h_sten(4 * PS, 0), h_rev(PS, 0);
-  std::vector<double> h_beta(4 * PS, 0.0), h_hpm(2 * PS, 1.0), h_bm(PS, 1.0), h_eta(2 * PS, 1.0),
-      h_arc(PS, 0.0), h_ec(3 * PS, 0.0), h_ecn(PS, 1.0), h_en(3 * PS, 0.0), h_nxr(3 * PS, 0.0),
-      h_chord(PS, 0.0);
-
-  const double sigma = par.acc_width / 2.355;
-  const double mu = M_PI / 2;
-  for (int i = 0; i < nf; ++i) {
-    const int r = perm[i];
-    const int n = g.face_off[r + 1] - g.face_off[r];
-    h_nslots[i] = (int8_t)n;
-    V3 fc = at3(g.face_centers, r);
-    const V3 fcn = vdiv(fc, vnorm(fc));
-    h_fcn[i] = fcn.x;
-    h_fcn[fpad + i] = fcn.y;
-    h_fcn[2 * (size_t)fpad + i] = fcn.z;
-    h_area[i] = g.area[r];
-    if (accretion_on) {
-      // res[0] of physics/adiabatic.hpp:428-436 (depends on geometry only)
-      const double theta_acc = std::acos(fcn.y * std::sin(par.tilt_angle) + fcn.z * std::cos(par.tilt_angle));
-      h_acc[i] = 1 / area_coeff * par.accretion_rate / std::sqrt(2 * M_PI * sigma * sigma) *
-                 std::exp(-(theta_acc - mu) * (theta_acc - mu) / (2 * sigma * sigma));
-    }
-    for (int j = 0; j < n; ++j) {
-      const int sr = g.face_off[r] + j;
-      const size_t s = (size_t)j * fpad + i;
-      h_sten[s] = iperm[g.ff_plus[2 * (size_t)sr]];
-      h_sten[PS + s] = iperm[g.ff_plus[2 * (size_t)sr + 1]];
-      h_sten[2 * PS + s] = iperm[g.ff_minus[2 * (size_t)sr]];
-      h_sten[3 * PS + s] = iperm[g.ff_minus[2 * (size_t)sr + 1]];
-      h_beta[s] = g.beta_plus[2 * (size_t)sr];
-      h_beta[PS + s] = g.beta_plus[2 * (size_t)sr + 1];
-      h_beta[2 * PS + s] = g.beta_minus[2 * (size_t)sr];
-      h_beta[3 * PS + s] = g.beta_minus[2 * (size_t)sr + 1];
-      h_hpm[s] = g.h_plus[sr];
-      h_hpm[PS + s] = g.h_minus[sr];
-      h_bm[s] = g.bm_dist[sr];
-      h_eta[s] = g.h_plus[sr] / g.bm_dist[sr];
-      h_eta[PS + s] = g.h_minus[sr] / g.bm_dist[sr];
-      const int va = g.face_vtx[sr];
-      const int vb = g.face_vtx[g.face_off[r] + ((j + 1 == n) ? 0 : j + 1)];
-      const V3 A = at3(g.vertices, va), B = at3(g.vertices, vb);
-      h_arc[s] = great_circle(&g.vertices[3 * (size_t)va], &g.vertices[3 * (size_t)vb]) / g.area[r];
-      V3 ec = vdiv(vadd(A, B), 2.);
-      ec = vdiv(ec, vnorm(ec));
-      const double ecn = vnorm(ec);
-      h_ec[s] = ec.x;
-      h_ec[PS + s] = ec.y;
-      h_ec[2 * PS + s] = ec.z;
-      h_ecn[s] = ecn;
-      const V3 en = at3(g.edge_normals, sr);
-      h_en[s] = en.x;
-      h_en[PS + s] = en.y;
-      h_en[2 * PS + s] = en.z;
-      const V3 nxr = vcross(en, vdiv(ec, ecn));
-      h_nxr[s] = nxr.x;
-      h_nxr[PS + s] = nxr.y;
-      h_nxr[2 * PS + s] = nxr.z;
-      h_chord[s] = vnorm(vsub(A, B));
-      const int nb = g.nbr_edge[sr];
-      h_rev[s] = j0_of[sr] * fpad + iperm[nb];
-    }
-    // unused slots of low-valence faces point at themselves (never read)
-    for (int j = n; j < max_slots; ++j) {
-      const size_t s = (size_t)j * fpad + i;
-      for (int q = 0; q < 4; ++q) h_sten[q * PS + s] = i;
-      h_rev[s] = (int)s;
-    }
-  }
-  // padding faces
-  for (int i = nf; i < fpad; ++i) {
-    for (int j = 0; j < max_slots; ++j) {
-      const size_t s = (size_t)j * fpad + i;
-      for (int q = 0; q < 4; ++q) h_sten[q * PS + s] = 0;
-      h_rev[s] = 0;
-    }
-  }
-
+  const SlotPlanes sp = make_slot_planes(g);
+  n_faces = sp.n_faces;
+  max_slots = sp.max_slots;
+  fpad = sp.fpad;
+  perm = sp.perm;
+  iperm = sp.iperm;
+  const std::vector<double> acc = accretion_source(sp, par, area_coeff, accretion_on);
   if (precision == SPLASH_PREC_MIXED) {
-    // FP32 slot planes; FP64 for the values feeding FP64 steps
-    auto tof = [](const std::vector<double>& v) { return std::vector<float>(v.begin(), v.end()); };
-    std::vector<float> h_invh(2 * PS, 1.0f);
-    std::vector<float> h_coef(PS, 0.0f);
-    for (size_t q = 0; q < PS; ++q) {
-      h_invh[q] = (float)(1.0 / h_hpm[q]);
-      h_invh[PS + q] = (float)(1.0 / h_hpm[PS + q]);
-    }
-    for (int i = 0; i < nf; ++i)
-      for (int j = 0; j < (int)h_nslots[i]; ++j) {
-        const size_t q = (size_t)j * fpad + i;
-        h_coef[q] = (float)(g.round_diff * h_chord[q] / h_area[i]);
-      }
-    GM.n_faces = nf;
+    const MixedPlanes mp = make_mixed_planes(sp);
+    GM.n_faces = n_faces;
     GM.fpad = fpad;
     GM.max_slots = max_slots;
-    GM.nslots = upload(h_nslots);
-    GM.fcn = upload(h_fcn);
-    GM.fcn32 = upload(tof(h_fcn));
-    GM.area = upload(h_area);
-    GM.acc_src = upload(h_acc);
-    GM.sten = upload(h_sten);
-    GM.beta = upload(tof(h_beta));
-    GM.inv_h = upload(h_invh);
-    GM.bm = upload(tof(h_bm));
-    GM.eta = upload(tof(h_eta));
-    GM.arc_a = upload(tof(h_arc));
-    GM.ec = upload(tof(h_ec));
-    GM.en = upload(tof(h_en));
-    GM.nxr = upload(tof(h_nxr));
-    GM.coef = upload(h_coef);
-    GM.rev = upload(h_rev);
-    geometry_bytes = h_nslots.size() + 8 * (h_fcn.size() + h_area.size() + h_acc.size()) + 4 * h_coef.size() +
-                     4 * (h_fcn.size() + h_sten.size() + h_rev.size() + h_beta.size() + h_invh.size() +
-                          h_bm.size() + h_eta.size() + h_arc.size() + h_ec.size() + h_en.size() +
-                          h_nxr.size());
-    wr_vertices = g.vertices;
-    wr_face_off = g.face_off;
-    wr_face_vtx = g.face_vtx;
-    wr_face_centers = g.face_centers;
-    wr_area = g.area;
-    return;
+    GM.nslots = upload(sp.nslots);
+    GM.fcn = upload(sp.fcn);
+    GM.fcn32 = upload(mp.fcn32);
+    GM.area = upload(sp.area);
+    GM.acc_src = upload(acc);
+    GM.sten = upload(sp.sten);
+    GM.beta = upload(mp.beta);
+    GM.inv_h = upload(mp.inv_h);
+    GM.bm = upload(mp.bm);
+    GM.eta = upload(mp.eta);
+    GM.arc_a = upload(mp.arc);
+    GM.ec = upload(mp.ec);
+    GM.en = upload(mp.en);
+    GM.nxr = upload(mp.nxr);
+    GM.coef = upload(mp.coef);
+    GM.rev = upload(sp.rev);
+    geometry_bytes = sp.nslots.size() + 8 * (sp.fcn.size() + sp.area.size() + acc.size()) +
+                     4 * (sp.sten.size() + sp.rev.size() + mp.fcn32.size() + mp.beta.size() +
+                          mp.inv_h.size() + mp.bm.size() + mp.eta.size() + mp.arc.size() +
+                          mp.ec.size() + mp.en.size() + mp.nxr.size() + mp.coef.size());
+  } else {
+    G.n_faces = n_faces;
+    G.fpad = fpad;
+    G.max_slots = max_slots;
+    G.nslots = upload(sp.nslots);
+    G.fcn = upload(sp.fcn);
+    G.area = upload(sp.area);
+    G.acc_src = upload(acc);
+    G.sten = upload(sp.sten);
+    G.beta = upload(sp.beta);
+    G.hpm = upload(sp.hpm);
+    G.bm = upload(sp.bm);
+    G.eta = upload(sp.eta);
+    G.arc_a = upload(sp.arc);
+    G.ec = upload(sp.ec);
+    G.ecn = upload(sp.ecn);
+    G.en = upload(sp.en);
+    G.nxr = upload(sp.nxr);
+    G.chord = upload(sp.chord);
+    G.rev = upload(sp.rev);
+    geometry_bytes = sp.nslots.size() + 8 * (sp.fcn.size() + sp.area.size() + acc.size()) +
+                     4 * (sp.sten.size() + sp.rev.size()) +
+                     8 * (sp.beta.size() + sp.hpm.size() + sp.bm.size() + sp.eta.size() +
+                          sp.arc.size() + sp.ec.size() + sp.ecn.size() + sp.en.size() +
+                          sp.nxr.size() + sp.chord.size());
   }
-
-  G.n_faces = nf;
-  G.fpad = fpad;
-  G.max_slots = max_slots;
-  G.nslots = upload(h_nslots);
-  G.fcn = upload(h_fcn);
-  G.area = upload(h_area);
-  G.acc_src = upload(h_acc);
-  G.sten = upload(h_sten);
-  G.beta = upload(h_beta);
-  G.hpm = upload(h_hpm);
-  G.bm = upload(h_bm);
-  G.eta = upload(h_eta);
-  G.arc_a = upload(h_arc);
-  G.ec = upload(h_ec);
-  G.ecn = upload(h_ecn);
-  G.en = upload(h_en);
-  G.nxr = upload(h_nxr);
-  G.chord = upload(h_chord);
-  G.rev = upload(h_rev);
-  geometry_bytes = 0;
-  geometry_bytes += h_nslots.size() + 8 * (h_fcn.size() + h_area.size() + h_acc.size());
-  geometry_bytes += 4 * (h_sten.size() + h_rev.size());
-  geometry_bytes += 8 * (h_beta.size() + h_hpm.size() + h_bm.size() + h_eta.size() + h_arc.size() +
-                         h_ec.size() + h_ecn.size() + h_en.size() + h_nxr.size() + h_chord.size());
-
   // keep what the writers need, in reference order
   wr_vertices = g.vertices;
   wr_face_off = g.face_off;
@@ -337,9 +220,11 @@ cudaError_t Solver::launch_prepare() {
   return precision == SPLASH_PREC_MIXED ? mixed_prepare(GM, S, P, stream) : fp64_prepare(G, S, P, stream);
 }
 
-cudaError_t Solver::launch_step(cudaEvent_t* ev) {
-  return precision == SPLASH_PREC_MIXED ? mixed_step(GM, S, P, stream, ev)
-                                        : fp64_step(G, S, P, stream, ev);
+cudaError_t Solver::launch_step(cudaEvent_t* ev, double dt0) {
+  if (precision == SPLASH_PREC_MIXED) return mixed_step(GM, S, P, dt0, stream, ev);
+  cudaError_t e = fp64_set_dt0(S, dt0, stream);
+  if (e != cudaSuccess) return e;
+  return fp64_step(G, S, P, stream, ev);
 }
 
 int Solver::upload_state(const double* U_ref) {
@@ -368,7 +253,11 @@ int Solver::read_scalars(double* out) {
 
 int Solver::capture_graph() {
   SPLASH_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-  cudaError_t le = launch_step(nullptr);
+  // FP64: the graph holds the five step launches, dt0 is set by a launch
+  // before each replay; mixed: the graph holds the whole step, dt0 being an
+  // argument of its first node
+  cudaError_t le = (precision == SPLASH_PREC_MIXED) ? mixed_step(GM, S, P, graph_dt0, stream, nullptr)
+                                                     : fp64_step(G, S, P, stream, nullptr);
   cudaGraph_t g = nullptr;
   cudaError_t ce = cudaStreamEndCapture(stream, &g);
   if (le != cudaSuccess) {
@@ -378,11 +267,40 @@ int Solver::capture_graph() {
   SPLASH_CUDA(ce);
   graph = g;
   SPLASH_CUDA(cudaGraphInstantiate(&graph_exec, graph, 0));
+  if (precision == SPLASH_PREC_MIXED) {
+    size_t n = 0;
+    SPLASH_CUDA(cudaGraphGetNodes(graph, nullptr, &n));
+    std::vector<cudaGraphNode_t> nodes(n);
+    SPLASH_CUDA(cudaGraphGetNodes(graph, nodes.data(), &n));
+    for (cudaGraphNode_t nd : nodes) {
+      cudaGraphNodeType t;
+      SPLASH_CUDA(cudaGraphNodeGetType(nd, &t));
+      if (t != cudaGraphNodeTypeKernel) continue;
+      cudaKernelNodeParams kp{};
+      SPLASH_CUDA(cudaGraphKernelNodeGetParams(nd, &kp));
+      if (kp.func == mixed_finalize_kernel_ptr()) dt0_node = nd;
+    }
+    if (!dt0_node) return fail(SPLASH_E_CUDA, "dt node not found in the captured step");
+  }
   return SPLASH_OK;
 }
 
 int Solver::step(double dt0) {
-  SPLASH_CUDA(fp64_set_dt0(S, dt0, stream));
+  if (precision == SPLASH_PREC_MIXED) {
+    if (dt0 != graph_dt0) {
+      // new dt0: rewrite the finalize node's arguments in the instantiated
+      // graph (takes effect from the next launch; launches in flight keep theirs)
+      cudaKernelNodeParams kp{};
+      SPLASH_CUDA(cudaGraphKernelNodeGetParams(dt0_node, &kp));
+      void* args[] = {&S, &P, &dt0};
+      kp.kernelParams = args;
+      kp.extra = nullptr;
+      SPLASH_CUDA(cudaGraphExecKernelNodeSetParams(graph_exec, dt0_node, &kp));
+      graph_dt0 = dt0;
+    }
+  } else {
+    SPLASH_CUDA(fp64_set_dt0(S, dt0, stream));
+  }
   SPLASH_CUDA(cudaGraphLaunch(graph_exec, stream));
   ++steps;
   return SPLASH_OK;
@@ -425,20 +343,9 @@ int splash_create(const splash_mesh_desc* mesh, const double* U_in, int dim, dou
     s->precision = precision;
     s->solver_kind = solver_kind;
     s->device = device;
-    // adiabatic ctor: area_coeff (loop counter taken to start at 0) and
-    // total_mass (physics/adiabatic.hpp:70-90)
+    // adiabatic ctor: area_coeff and total_mass (physics/adiabatic.hpp:70-90)
+    s->area_coeff = splash::area_coefficient(g, params->acc_width);
     {
-      double ac = 0;
-      const double mu = M_PI / 2;
-      const double sigma = params->acc_width / 2.355;
-      for (int n = 0; n < g.n_faces; ++n) {
-        const V3 c = at3(g.face_centers, n);
-        const double theta = std::acos(c.z / vnorm(c));
-        ac += g.area[n] / std::sqrt(2 * M_PI * sigma * sigma) *
-              std::exp(-(theta - mu) * (theta - mu) / (2 * sigma * sigma));
-      }
-      ac /= 4 * M_PI;
-      s->area_coeff = ac;
       double tm = 0;
       for (int n = 0; n < g.n_faces; ++n) tm += U_in[(size_t)n * dim] * g.area[n];
       s->total_mass = tm;
@@ -450,6 +357,9 @@ int splash_create(const splash_mesh_desc* mesh, const double* U_in, int dim, dou
     SPLASH_CUDA(cudaSetDevice(device));
     SPLASH_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
 
+    if (precision == SPLASH_PREC_MIXED && g.max_slots > 8)
+      return fail(SPLASH_E_UNSUPPORTED, "the mixed path handles faces of up to 8 edges (mesh has %d)",
+                  g.max_slots);
     s->build_device_geometry(g);
     splash::PhysParams& P = s->P;
     P.gam = gam;
@@ -488,6 +398,7 @@ int splash_create(const splash_mesh_desc* mesh, const double* U_in, int dim, dou
     S.partial = s->dalloc<double>((size_t)s->n_partials * splash::kPartialStride);
     S.scal = s->dalloc<double>(splash::kScCount);
     S.err = s->dalloc<unsigned int>(4);
+    S.keys = s->dalloc<unsigned long long>(2);
     s->d_stage = s->dalloc<double>((size_t)s->n_faces * splash::kDim);
     s->d_perm = s->upload(s->perm);
     SPLASH_CUDA(cudaMemset(S.U, 0, splash::kDim * fp * sizeof(double)));
@@ -551,8 +462,7 @@ int splash_kernel_times(splash_solver* h, int reps, double dt0, double ms[5]) {
   double acc[5] = {0, 0, 0, 0, 0};
   int rc = SPLASH_OK;
   for (int r = 0; r < reps && rc == SPLASH_OK; ++r) {
-    cudaError_t e = splash::fp64_set_dt0(s->S, dt0, s->stream);
-    if (e == cudaSuccess) e = s->launch_step(ev);
+    cudaError_t e = s->launch_step(ev, dt0);
     if (e == cudaSuccess) e = cudaEventSynchronize(ev[5]);
     if (e != cudaSuccess) {
       rc = fail(SPLASH_E_CUDA, "kernel timing: %s", cudaGetErrorString(e));
@@ -937,6 +847,20 @@ int splash_geometry_get(const splash_geometry* gh, const char* name, void* dst, 
   else if (k == "ff_minus") pick_i(g.ff_minus);
   else if (k == "beta_plus") pick_d(g.beta_plus);
   else if (k == "beta_minus") pick_d(g.beta_minus);
+  else if (k == "unit_face_centers") {
+    // fc / |fc| as write_face_centers prints it (MUSCL_geometry.hpp:1076-1077),
+    // evaluated here so the caller's compiler flags cannot change the digits
+    static thread_local std::vector<double> unit;
+    unit.resize(g.face_centers.size());
+    for (size_t i = 0; i + 2 < g.face_centers.size(); i += 3) {
+      const V3 c = at3(g.face_centers, i / 3);
+      const double n = vnorm(c);
+      unit[i] = c.x / n;
+      unit[i + 1] = c.y / n;
+      unit[i + 2] = c.z / n;
+    }
+    pick_d(unit);
+  }
   else if (k == "hilbert_order") {
     // the internal face numbering a solver built on this mesh uses
     static thread_local std::vector<int> order;

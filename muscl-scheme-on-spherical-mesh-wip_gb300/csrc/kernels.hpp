@@ -17,11 +17,6 @@ cudaError_t fp64_set_dt0(const DevState& S, double dt0, cudaStream_t st);
 // an event is recorded before the first and after every launch.
 cudaError_t fp64_step(const DevGeom& G, const DevState& S, const PhysParams& P, cudaStream_t st,
                       cudaEvent_t* ev = nullptr);
-// The dt clip (one block) shared by both paths.
-// squared_speeds: the partials hold max |v|^2 (mixed path), so the finalize
-// takes the square root of the reduced maximum.
-cudaError_t dt_reduce(const DevState& S, const PhysParams& P, int nblocks, cudaStream_t st,
-                      bool squared_speeds = false);
 cudaError_t fp64_scatter_state(const double* aos, const int* perm, double* U, int n_faces, int fpad,
                                cudaStream_t st);
 cudaError_t fp64_gather_state(const double* U, const int* perm, double* aos, int n_faces, int fpad,
@@ -30,8 +25,22 @@ cudaError_t fp64_gather_state(const double* U, const int* perm, double* aos, int
 // ---- FP32/FP64 mixed path (step_mixed.cu) ----
 cudaError_t mixed_prepare(const DevGeomMixed& G, const DevState& S, const PhysParams& P,
                           cudaStream_t st);
-cudaError_t mixed_step(const DevGeomMixed& G, const DevState& S, const PhysParams& P,
+// One do_step: the dt finalize (1 thread, argument dt0) then the four
+// stage launches.  Capturable; the finalize node's dt0 can be updated in an
+// instantiated graph (mixed_finalize_kernel_ptr identifies the node).
+cudaError_t mixed_step(const DevGeomMixed& G, const DevState& S, const PhysParams& P, double dt0,
                        cudaStream_t st, cudaEvent_t* ev = nullptr);
+const void* mixed_finalize_kernel_ptr();
 int mixed_partial_blocks(int n_faces);
+
+// ---- ensemble (step_mixed.cu): batched launches over instances ----
+// ftiles: (instance, first face) of 32-face tiles; rtiles: tiles of
+// `recon_width` faces for the reconstruction (blockDim.x = recon_width).
+cudaError_t ensemble_prepare(const EnsInstance* inst, int n_inst, const int2* ftiles, int n_ftiles,
+                             cudaStream_t st);
+cudaError_t ensemble_step(const EnsInstance* inst, int n_inst, const int2* rtiles, int n_rtiles,
+                          int recon_width, const int2* ftiles, int n_ftiles, int max_slots, double dt0,
+                          cudaStream_t st);
+const void* ensemble_finalize_kernel_ptr();
 
 }  // namespace splash

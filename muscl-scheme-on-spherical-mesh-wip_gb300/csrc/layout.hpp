@@ -100,6 +100,16 @@ struct DevState {
   double* partial;  // per-block partial records (kPartialStride doubles)
   double* scal;   // device scalars, see ScalarSlot
   unsigned int* err;  // stop bits
+  unsigned long long* keys;  // mixed path: [0] max |v|^2 key, [1] min extra-dt key
+};
+
+// One member of an ensemble: its mesh level's geometry (shared between
+// members on the same mesh, except the per-member accretion source), its own
+// state buffers and its own physics parameters.
+struct EnsInstance {
+  DevGeomMixed G;
+  DevState S;
+  PhysParams P;
 };
 
 enum ScalarSlot : int {

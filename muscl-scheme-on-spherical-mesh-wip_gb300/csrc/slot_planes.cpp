@@ -1,0 +1,190 @@
+// Host preparation of the device layout; see slot_planes.hpp.
+#include "slot_planes.hpp"
+
+#include <cmath>
+#include <stdexcept>
+
+#include "hilbert.hpp"
+
+namespace splash {
+
+namespace {
+struct V3 {
+  double x, y, z;
+};
+inline V3 vadd(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline V3 vsub(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline V3 vdiv(V3 a, double s) { return {a.x / s, a.y / s, a.z / s}; }
+inline double vnorm(V3 a) {
+  double s = 0.0;
+  s += a.x * a.x;
+  s += a.y * a.y;
+  s += a.z * a.z;
+  return std::sqrt(s);
+}
+inline V3 vcross(V3 a, V3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline V3 at3(const std::vector<double>& v, size_t i) { return {v[3 * i], v[3 * i + 1], v[3 * i + 2]}; }
+}  // namespace
+
+SlotPlanes make_slot_planes(const RefGeometry& g) {
+  SlotPlanes sp;
+  const int nf = g.n_faces;
+  const int max_slots = g.max_slots;
+  const int fpad = (nf + 31) / 32 * 32;
+  sp.n_faces = nf;
+  sp.max_slots = max_slots;
+  sp.fpad = fpad;
+  sp.round_diff = g.round_diff;
+  const size_t PS = sp.PS();
+
+  sp.perm = hilbert_order(g.face_centers.data(), nf);
+  sp.iperm.assign(nf, 0);
+  for (int i = 0; i < nf; ++i) sp.iperm[sp.perm[i]] = i;
+  const std::vector<int>& perm = sp.perm;
+  const std::vector<int>& iperm = sp.iperm;
+
+  // reference-order reverse slot (std::find of MUSCL_base.hpp:383-384)
+  std::vector<int> j0_of(g.n_slots, -1);
+  for (int f = 0; f < nf; ++f) {
+    for (int s = g.face_off[f]; s < g.face_off[f + 1]; ++s) {
+      const int nb = g.nbr_edge[s];
+      int j0 = -1;
+      for (int q = g.face_off[nb]; q < g.face_off[nb + 1]; ++q)
+        if (g.nbr_edge[q] == f) {
+          j0 = q - g.face_off[nb];
+          break;
+        }
+      if (j0 < 0) throw std::runtime_error("edge neighbour relation is not symmetric");
+      j0_of[s] = j0;
+    }
+  }
+
+  sp.nslots.assign(fpad, 0);
+  sp.fcn.assign(3 * (size_t)fpad, 0.0);
+  sp.area.assign(fpad, 1.0);
+  sp.sten.assign(4 * PS, 0);
+  sp.rev.assign(PS, 0);
+  sp.beta.assign(4 * PS, 0.0);
+  sp.hpm.assign(2 * PS, 1.0);
+  sp.bm.assign(PS, 1.0);
+  sp.eta.assign(2 * PS, 1.0);
+  sp.arc.assign(PS, 0.0);
+  sp.ec.assign(3 * PS, 0.0);
+  sp.ecn.assign(PS, 1.0);
+  sp.en.assign(3 * PS, 0.0);
+  sp.nxr.assign(3 * PS, 0.0);
+  sp.chord.assign(PS, 0.0);
+
+  for (int i = 0; i < nf; ++i) {
+    const int r = perm[i];
+    const int n = g.face_off[r + 1] - g.face_off[r];
+    sp.nslots[i] = (int8_t)n;
+    const V3 fc = at3(g.face_centers, r);
+    const V3 fcn = vdiv(fc, vnorm(fc));
+    sp.fcn[i] = fcn.x;
+    sp.fcn[fpad + i] = fcn.y;
+    sp.fcn[2 * (size_t)fpad + i] = fcn.z;
+    sp.area[i] = g.area[r];
+    for (int j = 0; j < n; ++j) {
+      const int sr = g.face_off[r] + j;
+      const size_t s = (size_t)j * fpad + i;
+      sp.sten[s] = iperm[g.ff_plus[2 * (size_t)sr]];
+      sp.sten[PS + s] = iperm[g.ff_plus[2 * (size_t)sr + 1]];
+      sp.sten[2 * PS + s] = iperm[g.ff_minus[2 * (size_t)sr]];
+      sp.sten[3 * PS + s] = iperm[g.ff_minus[2 * (size_t)sr + 1]];
+      sp.beta[s] = g.beta_plus[2 * (size_t)sr];
+      sp.beta[PS + s] = g.beta_plus[2 * (size_t)sr + 1];
+      sp.beta[2 * PS + s] = g.beta_minus[2 * (size_t)sr];
+      sp.beta[3 * PS + s] = g.beta_minus[2 * (size_t)sr + 1];
+      sp.hpm[s] = g.h_plus[sr];
+      sp.hpm[PS + s] = g.h_minus[sr];
+      sp.bm[s] = g.bm_dist[sr];
+      sp.eta[s] = g.h_plus[sr] / g.bm_dist[sr];
+      sp.eta[PS + s] = g.h_minus[sr] / g.bm_dist[sr];
+      const int va = g.face_vtx[sr];
+      const int vb = g.face_vtx[g.face_off[r] + ((j + 1 == n) ? 0 : j + 1)];
+      const V3 A = at3(g.vertices, va), B = at3(g.vertices, vb);
+      // great-circle edge length / area: the limiter's Courant factor
+      // (physics/adiabatic.hpp:757-758)
+      sp.arc[s] = great_circle(&g.vertices[3 * (size_t)va], &g.vertices[3 * (size_t)vb]) / g.area[r];
+      V3 ec = vdiv(vadd(A, B), 2.);
+      ec = vdiv(ec, vnorm(ec));
+      const double ecn = vnorm(ec);
+      sp.ec[s] = ec.x;
+      sp.ec[PS + s] = ec.y;
+      sp.ec[2 * PS + s] = ec.z;
+      sp.ecn[s] = ecn;
+      const V3 en = at3(g.edge_normals, sr);
+      sp.en[s] = en.x;
+      sp.en[PS + s] = en.y;
+      sp.en[2 * PS + s] = en.z;
+      const V3 nxr = vcross(en, vdiv(ec, ecn));
+      sp.nxr[s] = nxr.x;
+      sp.nxr[PS + s] = nxr.y;
+      sp.nxr[2 * PS + s] = nxr.z;
+      sp.chord[s] = vnorm(vsub(A, B));
+      sp.rev[s] = j0_of[sr] * fpad + iperm[g.nbr_edge[sr]];
+    }
+    // unused slots of low-valence faces point at themselves (never read)
+    for (int j = n; j < max_slots; ++j) {
+      const size_t s = (size_t)j * fpad + i;
+      for (int q = 0; q < 4; ++q) sp.sten[q * PS + s] = i;
+      sp.rev[s] = (int)s;
+    }
+  }
+  return sp;
+}
+
+double area_coefficient(const RefGeometry& g, double acc_width) {
+  double ac = 0;
+  const double mu = M_PI / 2;
+  const double sigma = acc_width / 2.355;
+  for (int n = 0; n < g.n_faces; ++n) {
+    const V3 c = at3(g.face_centers, n);
+    const double theta = std::acos(c.z / vnorm(c));
+    ac += g.area[n] / std::sqrt(2 * M_PI * sigma * sigma) *
+          std::exp(-(theta - mu) * (theta - mu) / (2 * sigma * sigma));
+  }
+  ac /= 4 * M_PI;
+  return ac;
+}
+
+std::vector<double> accretion_source(const SlotPlanes& sp, const splash_params& par,
+                                     double area_coeff, bool accretion_on) {
+  std::vector<double> acc(sp.fpad, 0.0);
+  if (!accretion_on) return acc;
+  const double sigma = par.acc_width / 2.355;
+  const double mu = M_PI / 2;
+  for (int i = 0; i < sp.n_faces; ++i) {
+    const V3 fcn{sp.fcn[i], sp.fcn[sp.fpad + i], sp.fcn[2 * (size_t)sp.fpad + i]};
+    const double theta_acc = std::acos(fcn.y * std::sin(par.tilt_angle) + fcn.z * std::cos(par.tilt_angle));
+    acc[i] = 1 / area_coeff * par.accretion_rate / std::sqrt(2 * M_PI * sigma * sigma) *
+             std::exp(-(theta_acc - mu) * (theta_acc - mu) / (2 * sigma * sigma));
+  }
+  return acc;
+}
+
+MixedPlanes make_mixed_planes(const SlotPlanes& sp) {
+  auto tof = [](const std::vector<double>& v) { return std::vector<float>(v.begin(), v.end()); };
+  MixedPlanes mp;
+  const size_t PS = sp.PS();
+  mp.fcn32 = tof(sp.fcn);
+  mp.beta = tof(sp.beta);
+  mp.bm = tof(sp.bm);
+  mp.eta = tof(sp.eta);
+  mp.arc = tof(sp.arc);
+  mp.ec = tof(sp.ec);
+  mp.en = tof(sp.en);
+  mp.nxr = tof(sp.nxr);
+  mp.inv_h.assign(2 * PS, 1.0f);
+  for (size_t q = 0; q < 2 * PS; ++q) mp.inv_h[q] = (float)(1.0 / sp.hpm[q]);
+  mp.coef.assign(PS, 0.0f);
+  for (int i = 0; i < sp.n_faces; ++i)
+    for (int j = 0; j < (int)sp.nslots[i]; ++j) {
+      const size_t q = (size_t)j * sp.fpad + i;
+      mp.coef[q] = (float)(sp.round_diff * sp.chord[q] / sp.area[i]);
+    }
+  return mp;
+}
+
+}  // namespace splash

@@ -1,0 +1,48 @@
+// Host-side preparation of the device layout (see layout.hpp): the Hilbert
+// renumbering and every per-face / per-slot constant of the time step,
+// evaluated once with the reference's own expressions.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include "geometry.hpp"
+#include "splash_gb300.h"
+
+namespace splash {
+
+struct SlotPlanes {
+  int n_faces = 0, fpad = 0, max_slots = 0;
+  std::vector<int> perm, iperm;  // perm[internal] = reference face
+  // per face [fpad]
+  std::vector<int8_t> nslots;
+  std::vector<double> fcn;   // 3 planes
+  std::vector<double> area;
+  // per slot [max_slots * fpad] (x planes)
+  std::vector<int> sten;     // 4 planes, internal ids
+  std::vector<int> rev;      // slot-plane index of the reverse slot
+  std::vector<double> beta;  // 4 planes
+  std::vector<double> hpm;   // 2 planes
+  std::vector<double> bm, eta /*2 planes*/, arc, ec /*3*/, ecn, en /*3*/, nxr /*3*/, chord;
+  double round_diff = 0.0;
+  size_t PS() const { return (size_t)max_slots * fpad; }
+};
+
+SlotPlanes make_slot_planes(const RefGeometry& g);
+
+// area_coeff of physics/adiabatic.hpp:70-84 (loop counter starting at 0)
+double area_coefficient(const RefGeometry& g, double acc_width);
+
+// Accretion mass source res[0] of physics/adiabatic.hpp:428-436 per internal
+// face (zeros when accretion is off): a function of geometry and parameters
+// only, so it is evaluated once on the host.
+std::vector<double> accretion_source(const SlotPlanes& sp, const splash_params& par,
+                                     double area_coeff, bool accretion_on);
+
+// FP32 planes of the mixed path.
+struct MixedPlanes {
+  std::vector<float> fcn32, beta, inv_h, bm, eta, arc, ec, en, nxr, coef;
+};
+MixedPlanes make_mixed_planes(const SlotPlanes& sp);
+
+}  // namespace splash

@@ -56,6 +56,8 @@ struct Solver {
   std::vector<void*> dev_allocs;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
+  cudaGraphNode_t dt0_node = nullptr;  // mixed path: the finalize node taking dt0
+  double graph_dt0 = 0.0;              // dt0 the instantiated graph currently uses
   int64_t steps = 0;
 
   ~Solver();
@@ -71,7 +73,7 @@ struct Solver {
   int read_scalars(double* out);
   int capture_graph();
   int step(double dt0);
-  cudaError_t launch_step(cudaEvent_t* ev);  // one un-captured step
+  cudaError_t launch_step(cudaEvent_t* ev, double dt0);  // one un-captured step
   cudaError_t launch_prepare();
   static int check_cuda(cudaError_t e, const char* what);
 };

@@ -54,10 +54,9 @@ __global__ void __launch_bounds__(kBlock) prepare_kernel(DevGeom G, DevState S, 
 }
 
 // dt = min(dt0, 0.1 h0 / max_vel, extra_dt)  (MUSCL_base.hpp:100-115)
-__global__ void __launch_bounds__(256) dt_kernel(DevState S, PhysParams P, int nblocks,
-                                                 int squared_speeds) {
+__global__ void __launch_bounds__(256) dt_kernel(DevState S, PhysParams P, int nblocks) {
   __shared__ double sm[256][7];
-  double v[7] = {squared_speeds ? 1e-16 : 1e-8, 1e20, 0, 0, 0, 0, 0};
+  double v[7] = {1e-8, 1e20, 0, 0, 0, 0, 0};
   for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
     const double* p = S.partial + (size_t)b * kPartialStride;
     v[0] = fmax(v[0], p[0]);
@@ -78,7 +77,7 @@ __global__ void __launch_bounds__(256) dt_kernel(DevState S, PhysParams P, int n
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    const double max_vel = squared_speeds ? sqrt(sm[0][0]) : sm[0][0];
+    const double max_vel = sm[0][0];
     double extra = sm[0][1];
     if (extra < 0) {
       atomicOr(S.err, 8u);  // SPLASH_STOP_NEG_EXTRA_DT
@@ -252,12 +251,6 @@ cudaError_t fp64_prepare(const DevGeom& G, const DevState& S, const PhysParams& 
   return cudaGetLastError();
 }
 
-cudaError_t dt_reduce(const DevState& S, const PhysParams& P, int nblocks, cudaStream_t st,
-                      bool squared_speeds) {
-  f64::dt_kernel<<<1, 256, 0, st>>>(S, P, nblocks, squared_speeds ? 1 : 0);
-  return cudaGetLastError();
-}
-
 cudaError_t fp64_set_dt0(const DevState& S, double dt0, cudaStream_t st) {
   f64::set_scalar_kernel<<<1, 1, 0, st>>>(S.scal + kScDt0, dt0);
   return cudaGetLastError();
@@ -267,7 +260,7 @@ cudaError_t fp64_step(const DevGeom& G, const DevState& S, const PhysParams& P, 
                       cudaEvent_t* ev) {
   const int nb = f64::blocks_for(G.n_faces);
   if (ev) cudaEventRecord(ev[0], st);
-  f64::dt_kernel<<<1, 256, 0, st>>>(S, P, nb, 0);
+  f64::dt_kernel<<<1, 256, 0, st>>>(S, P, nb);
   if (ev) cudaEventRecord(ev[1], st);
   f64::reconstruct_kernel<<<nb, f64::kBlock, 0, st>>>(G, S.W0, S.uplus, S.scal, P);
   if (ev) cudaEventRecord(ev[2], st);

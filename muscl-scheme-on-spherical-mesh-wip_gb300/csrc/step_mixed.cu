@@ -37,6 +37,36 @@ __device__ __forceinline__ f64::D3 plane3d(const double* p, int stride, int i) {
   return f64::D3{p[i], p[stride + i], p[2 * stride + i]};
 }
 
+// Order-preserving 64-bit keys of doubles: unsigned comparison of the keys
+// orders the values, so the dt clip's max and min are exact integer
+// atomics (no FP64 work, independent of the reduction order).
+__device__ __forceinline__ unsigned long long order_key(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double key_value(unsigned long long k) {
+  const unsigned long long b = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
+  return __longlong_as_double((long long)b);
+}
+
+// Warp-reduces the dt candidates (NaN ignored, like the reference's
+// comparisons) and folds them into the global keys with one atomic each.
+__device__ __forceinline__ void fold_candidates(double vmax2, double dmin, unsigned long long* keys) {
+  unsigned long long kmax = isnan(vmax2) ? 0ull : order_key(vmax2);
+  unsigned long long kmin = isnan(dmin) ? ~0ull : order_key(dmin);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long a = __shfl_down_sync(0xffffffffu, kmax, o);
+    const unsigned long long b = __shfl_down_sync(0xffffffffu, kmin, o);
+    kmax = a > kmax ? a : kmax;
+    kmin = b < kmin ? b : kmin;
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(&keys[0], kmax);
+    atomicMin(&keys[1], kmin);
+  }
+}
+
 // FP64 pressure recovery with one division: Pi = (E - |r x l|^2/(2 Sigma))(gam-1),
 // floored at 1e-16 like MUSCL_base.hpp:538.  Also returns |v|^2 and 1/Sigma
 // for the dt candidates.
@@ -61,9 +91,9 @@ __device__ __forceinline__ void store_w32(float* W32, int fp, int f, const doubl
 // monotone, so the dt finalize takes one sqrt of the maximum), and
 // extra_dt_constr (physics/adiabatic.hpp:543-580) simplifies to
 // 0.01 p / (alpha k g_eff Sigma |v - v0|) with k = gam3d / (2 gam3d - 1).
-__device__ __forceinline__ void dt_candidates_sq(const double* u, f64::D3 r, double area, double p,
-                                                 double v2, double inv_rho, const PhysParams& P,
-                                                 double& vmax2, double& dmin, double sums[5]) {
+__device__ __forceinline__ void dt_candidates_sq(const double* u, f64::D3 r, double p, double v2,
+                                                 double inv_rho, const PhysParams& P, double& vmax2,
+                                                 double& dmin) {
   vmax2 = fmax(v2, P.gam * p * inv_rho);
   const f64::D3 c = f64::cross3(r, f64::d3(u[1], u[2], u[3]));
   // v = (r x l) / (-Sigma) ; v0 = omega_ns z x r
@@ -75,8 +105,6 @@ __device__ __forceinline__ void dt_candidates_sq(const double* u, f64::D3 r, dou
   const double k = gam3d / (2 * gam3d - 1);
   const double g_eff = 0.217909 - v2;
   dmin = 0.01 * p / (P.alpha * k * g_eff * u[0] * dv);
-#pragma unroll
-  for (int q = 0; q < 5; ++q) sums[q] = u[q] * area;
 }
 
 // physics/adiabatic.hpp:396-541 in FP32, except the accretion mass source
@@ -148,9 +176,11 @@ __device__ __forceinline__ void source_f32(const float* w, F3 fcn, float acc0, c
   }
 }
 
-__global__ void __launch_bounds__(kBlock) prepare_kernel(DevGeomMixed G, DevState S, PhysParams P) {
-  const int f = blockIdx.x * blockDim.x + threadIdx.x;
-  double vmax = 0.0, dmin = 1e20, sums[5] = {0, 0, 0, 0, 0};
+// W32 and the dt candidates of the current U for face f (all 32 lanes of a
+// warp call it; lanes past the last face contribute neutral values).
+__device__ __forceinline__ void prepare_body(const DevGeomMixed& G, const DevState& S,
+                                             const PhysParams& P, int f) {
+  double vmax = 0.0, dmin = 1e20;
   if (f < G.n_faces) {
     double u[kDim];
 #pragma unroll
@@ -159,15 +189,54 @@ __global__ void __launch_bounds__(kBlock) prepare_kernel(DevGeomMixed G, DevStat
     double v2, inv_rho;
     const double p = pressure_recover(u, r, P.gam, v2, inv_rho);
     store_w32(S.W32, G.fpad, f, u, p);
-    dt_candidates_sq(u, r, G.area[f], p, v2, inv_rho, P, vmax, dmin, sums);
+    dt_candidates_sq(u, r, p, v2, inv_rho, P, vmax, dmin);
   }
-  red::block_partials<kBlock>(vmax, dmin, sums, S.partial + (size_t)blockIdx.x * kPartialStride);
+  fold_candidates(vmax, dmin, S.keys);
 }
 
+__global__ void __launch_bounds__(32) prepare_kernel(DevGeomMixed G, DevState S, PhysParams P) {
+  prepare_body(G, S, P, blockIdx.x * 32 + threadIdx.x);
+}
+
+// initial keys: max |v|^2 starts at (1e-8)^2 and min extra dt at 1e20, the
+// reference's initial values (MUSCL_base.hpp:314, adiabatic.hpp:545)
+__global__ void reset_keys_kernel(unsigned long long* keys) {
+  keys[0] = order_key(1e-16);
+  keys[1] = order_key(1e20);
+}
+
+// dt = min(dt0, 0.1 h0 / max_vel, extra_dt) (MUSCL_base.hpp:100-115), time,
+// and a fresh start for the keys the step's stage-2 launch will fold into.
+__device__ __forceinline__ void finalize_body(const DevState& S, const PhysParams& P, double dt0) {
+  const double max_vel = sqrt(key_value(S.keys[0]));
+  double extra = key_value(S.keys[1]);
+  if (extra < 0) {
+    atomicOr(S.err, 8u);  // SPLASH_STOP_NEG_EXTRA_DT
+    extra = 1e20;
+  }
+  double dt = dt0;
+  if (dt > P.h0 * 0.1 / max_vel) dt = P.h0 * 0.1 / max_vel;
+  if (dt > extra) dt = extra;
+  S.scal[kScDt] = dt;
+  S.scal[kScDt0] = dt0;
+  S.scal[kScMaxVel] = max_vel;
+  S.scal[kScExtraDt] = extra;
+  S.scal[kScTime] = S.scal[kScTime] + dt;
+  S.keys[0] = order_key(1e-16);
+  S.keys[1] = order_key(1e20);
+}
+
+__global__ void finalize_kernel(DevState S, PhysParams P, double dt0) { finalize_body(S, P, dt0); }
+
 // find_U_edges (MUSCL_base.hpp:361-434) in FP32; edge field 4 stays Pi.
-__global__ void __launch_bounds__(kBlock) reconstruct_kernel(DevGeomMixed G, DevState S, PhysParams P) {
-  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+// One thread per (face, slot): blockIdx.y is the slot plane, so a warp reads
+// consecutive faces of one plane and the 4-face gathers of six slots are in
+// flight at once instead of one after the other.
+__device__ __forceinline__ void recon_body(const DevGeomMixed& G, const DevState& S, const PhysParams& P,
+                                           int f, int j) {
   if (f >= G.n_faces) return;
+  const int n = G.nslots[f];
+  if (j >= n) return;
   const int fp = G.fpad;
   const int PS = G.max_slots * fp;
   const float* __restrict__ W = S.W32;
@@ -176,44 +245,92 @@ __global__ void __launch_bounds__(kBlock) reconstruct_kernel(DevGeomMixed G, Dev
   float w[kDim];
 #pragma unroll
   for (int k = 0; k < kDim; ++k) w[k] = W[k * fp + f];
-  const int n = G.nslots[f];
-  const float twoN = (float)(2 * n);
   const float inv_rho = -1.0f / w[0];
   const float c = sqrtf(gam * w[4] / w[0]);
-  for (int j = 0; j < n; ++j) {
-    const int s = j * fp + f;
-    const int ia = G.sten[s], ib = G.sten[PS + s], ic = G.sten[2 * PS + s], id = G.sten[3 * PS + s];
-    const float bp0 = G.beta[s], bp1 = G.beta[PS + s], bm0 = G.beta[2 * PS + s], bm1 = G.beta[3 * PS + s];
-    const float ihp = G.inv_h[s], ihm = G.inv_h[PS + s], bmd = G.bm[s];
-    const F3 ec = plane3f(G.ec, PS, s);
-    const F3 en = plane3f(G.en, PS, s);
-    const F3 vel = scal(cross3(ec, f3(w[1], w[2], w[3])), inv_rho);
-    const float nu_plus = (c + dot3(vel, en)) * dt * G.arc_a[s];
-    const float eta_p = G.eta[s];
-    const float sb_scale = G.eta[PS + s] / (twoN * nu_plus);
+  const int s = j * fp + f;
+  const int ia = G.sten[s], ib = G.sten[PS + s], ic = G.sten[2 * PS + s], id = G.sten[3 * PS + s];
+  const float bp0 = G.beta[s], bp1 = G.beta[PS + s], bm0 = G.beta[2 * PS + s], bm1 = G.beta[3 * PS + s];
+  const float ihp = G.inv_h[s], ihm = G.inv_h[PS + s], bmd = G.bm[s];
+  const F3 ec = plane3f(G.ec, PS, s);
+  const F3 en = plane3f(G.en, PS, s);
+  const F3 vel = scal(cross3(ec, f3(w[1], w[2], w[3])), inv_rho);
+  const float nu_plus = (c + dot3(vel, en)) * dt * G.arc_a[s];
+  const float eta_p = G.eta[s];
+  const float sb_scale = G.eta[PS + s] / ((float)(2 * n) * nu_plus);
 #pragma unroll
-    for (int k = 0; k < kDim; ++k) {
-      const float* Wk = W + k * fp;
-      const float pp = (bp0 * Wk[ia] + bp1 * Wk[ib] - w[k]) * ihp;
-      const float pm = (w[k] - (bm0 * Wk[ic] + bm1 * Wk[id])) * ihm;
-      const float r = pm / pp;
-      const float lim = limiter_field(r, nu_plus, eta_p, sb_scale);
-      S.uplus32[k * PS + s] = w[k] + pp * lim * bmd;
-    }
+  for (int k = 0; k < kDim; ++k) {
+    const float* Wk = W + k * fp;
+    const float pp = (bp0 * Wk[ia] + bp1 * Wk[ib] - w[k]) * ihp;
+    const float pm = (w[k] - (bm0 * Wk[ic] + bm1 * Wk[id])) * ihm;
+    const float r = pm / pp;
+    const float lim = limiter_field(r, nu_plus, eta_p, sb_scale);
+    S.uplus32[k * PS + s] = w[k] + pp * lim * bmd;
   }
 }
 
+__global__ void __launch_bounds__(kBlock) reconstruct_kernel(DevGeomMixed G, DevState S, PhysParams P) {
+  recon_body(G, S, P, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
+}
+
+constexpr int kFaceTile = 32;   // faces per flux block (x)
+constexpr int kMaxSlotLanes = 8;  // slot lanes per face (y), >= max_slots
+
+// find_flux_var + res2d + RK combine (MUSCL_base.hpp:345-359, 238-276,
+// 124-161).  Block = 32 faces x max_slots slot lanes: every (face, slot)
+// thread evaluates one Riemann flux and parks its contribution in shared
+// memory; then one warp sums each face's contributions in slot order
+// (compensated), adds the source and does the FP64 update.
+struct FluxShared {
+  float contrib[kMaxSlotLanes][kDim][kFaceTile];
+  unsigned bits;
+};
+
 template <int STAGE>
-__global__ void __launch_bounds__(kBlock) flux_update_kernel(DevGeomMixed G, DevState S, PhysParams P) {
-  const int f = blockIdx.x * blockDim.x + threadIdx.x;
-  double vmax = 0.0, dmin = 1e20, sums[5] = {0, 0, 0, 0, 0};
+__device__ __forceinline__ void flux_body(const DevGeomMixed& G, const DevState& S, const PhysParams& P,
+                                          int face_begin, FluxShared& sh) {
+  float (&contrib)[kMaxSlotLanes][kDim][kFaceTile] = sh.contrib;
+  unsigned& sbits = sh.bits;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int f = face_begin + tx;
+  const int fp = G.fpad;
+  const int PS = G.max_slots * fp;
+  const double dt = S.scal[kScDt];
+  const double dt_here = (STAGE == 1) ? dt / 2 : dt;
+  const float dtf = (float)dt_here;
+  const float gam = (float)P.gam;
+  if (tx == 0 && ty == 0) sbits = 0;
+  __syncthreads();
+  {
+    float F[kDim] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    float cf = 0.f;
+    if (f < G.n_faces && ty < G.nslots[f]) {
+      const int s = ty * fp + f;
+      const int rv = G.rev[s];
+      float uL[kDim], uR[kDim];
+#pragma unroll
+      for (int k = 0; k < kDim; ++k) {
+        uL[k] = S.uplus32[k * PS + s];
+        uR[k] = S.uplus32[k * PS + rv];
+      }
+      SlotGeomF g;
+      g.ec = plane3f(G.ec, PS, s);
+      g.en = plane3f(G.en, PS, s);
+      g.nxr = plane3f(G.nxr, PS, s);
+      unsigned bits = flux_star(uL, uR, g, gam, P.solver, F);
+#pragma unroll
+      for (int k = 0; k < kDim; ++k)
+        if (isnan(F[k])) bits |= 1u;
+      if (bits) atomicOr(&sbits, bits);
+      cf = dtf * G.coef[s];
+    }
+#pragma unroll
+    for (int k = 0; k < kDim; ++k) contrib[ty][k][tx] = -cf * F[k];
+  }
+  __syncthreads();
+  if (ty != 0) return;
+  if (tx == 0 && sbits) atomicOr(S.err, sbits);
+  double vmax = 0.0, dmin = 1e20;
   if (f < G.n_faces) {
-    const int fp = G.fpad;
-    const int PS = G.max_slots * fp;
-    const double dt = S.scal[kScDt];
-    const double dt_here = (STAGE == 1) ? dt / 2 : dt;
-    const float dtf = (float)dt_here;
-    const float gam = (float)P.gam;
     float w[kDim], src[kDim];
 #pragma unroll
     for (int k = 0; k < kDim; ++k) w[k] = S.W32[k * fp + f];
@@ -227,29 +344,10 @@ __global__ void __launch_bounds__(kBlock) flux_update_kernel(DevGeomMixed G, Dev
       acc[k].lo = 0.f;
     }
     const int n = G.nslots[f];
-    unsigned bits = 0;
     for (int j = 0; j < n; ++j) {
-      const int s = j * fp + f;
-      const int rv = G.rev[s];
-      float uL[kDim], uR[kDim], F[kDim];
 #pragma unroll
-      for (int k = 0; k < kDim; ++k) {
-        uL[k] = S.uplus32[k * PS + s];
-        uR[k] = S.uplus32[k * PS + rv];
-      }
-      SlotGeomF g;
-      g.ec = plane3f(G.ec, PS, s);
-      g.en = plane3f(G.en, PS, s);
-      g.nxr = plane3f(G.nxr, PS, s);
-      bits |= flux_star(uL, uR, g, gam, P.solver, F);
-      const float cf = dtf * G.coef[s];
-#pragma unroll
-      for (int k = 0; k < kDim; ++k) {
-        if (isnan(F[k])) bits |= 1u;
-        acc[k].add(-cf * F[k]);
-      }
+      for (int k = 0; k < kDim; ++k) acc[k].add(contrib[j][k][tx]);
     }
-    if (bits) atomicOr(S.err, bits);
     // the compensated FP32 sum is rounded once to FP32 (an increment of
     // dt * Phi, small against U) and added to the FP64 state; U0 stays in
     // S.U until stage 2 overwrites it
@@ -265,11 +363,57 @@ __global__ void __launch_bounds__(kBlock) flux_update_kernel(DevGeomMixed G, Dev
     if (STAGE == 2) {
 #pragma unroll
       for (int k = 0; k < kDim; ++k) S.U[k * fp + f] = u[k];
-      dt_candidates_sq(u, r, G.area[f], p, v2, inv_rho, P, vmax, dmin, sums);
+      dt_candidates_sq(u, r, p, v2, inv_rho, P, vmax, dmin);
     }
   }
-  if (STAGE == 2)
-    red::block_partials<kBlock>(vmax, dmin, sums, S.partial + (size_t)blockIdx.x * kPartialStride);
+  if (STAGE == 2) fold_candidates(vmax, dmin, S.keys);
+}
+
+template <int STAGE>
+__global__ void __launch_bounds__(kFaceTile * kMaxSlotLanes) flux_update_kernel(DevGeomMixed G, DevState S,
+                                                                                PhysParams P) {
+  __shared__ FluxShared sh;
+  flux_body<STAGE>(G, S, P, blockIdx.x * kFaceTile, sh);
+}
+
+// ---------------------------------------------------------------- ensemble
+// Batched launches over many independent instances: every block looks up
+// its (instance, first face) tile and runs the same bodies as a single
+// solver, so each instance's arithmetic is exactly that of a standalone run.
+__global__ void __launch_bounds__(32) ens_prepare_kernel(const EnsInstance* __restrict__ inst,
+                                                         const int2* __restrict__ tiles) {
+  const int2 t = tiles[blockIdx.x];
+  const EnsInstance& I = inst[t.x];
+  prepare_body(I.G, I.S, I.P, t.y + threadIdx.x);
+}
+
+__global__ void ens_reset_keys_kernel(const EnsInstance* __restrict__ inst, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    inst[i].S.keys[0] = order_key(1e-16);
+    inst[i].S.keys[1] = order_key(1e20);
+  }
+}
+
+__global__ void ens_finalize_kernel(const EnsInstance* __restrict__ inst, int n, double dt0) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) finalize_body(inst[i].S, inst[i].P, dt0);
+}
+
+__global__ void __launch_bounds__(256) ens_reconstruct_kernel(const EnsInstance* __restrict__ inst,
+                                                              const int2* __restrict__ tiles) {
+  const int2 t = tiles[blockIdx.x];
+  const EnsInstance& I = inst[t.x];
+  recon_body(I.G, I.S, I.P, t.y + threadIdx.x, blockIdx.y);
+}
+
+template <int STAGE>
+__global__ void __launch_bounds__(kFaceTile * kMaxSlotLanes) ens_flux_kernel(
+    const EnsInstance* __restrict__ inst, const int2* __restrict__ tiles) {
+  __shared__ FluxShared sh;
+  const int2 t = tiles[blockIdx.x];
+  const EnsInstance& I = inst[t.x];
+  flux_body<STAGE>(I.G, I.S, I.P, t.y, sh);
 }
 
 inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
@@ -277,30 +421,58 @@ inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
 }  // namespace
 }  // namespace mx
 
-int mixed_partial_blocks(int n_faces) { return mx::blocks_for(n_faces); }
+// the stage-2 flux launch writes one partial record per 32-face tile; the
+// prepare launch (128 faces per block) writes fewer, all within that count
+int mixed_partial_blocks(int n_faces) { return (n_faces + mx::kFaceTile - 1) / mx::kFaceTile; }
+
+const void* mixed_finalize_kernel_ptr() { return (const void*)mx::finalize_kernel; }
 
 cudaError_t mixed_prepare(const DevGeomMixed& G, const DevState& S, const PhysParams& P,
                           cudaStream_t st) {
-  mx::prepare_kernel<<<mx::blocks_for(G.n_faces), mx::kBlock, 0, st>>>(G, S, P);
+  mx::reset_keys_kernel<<<1, 1, 0, st>>>(S.keys);
+  mx::prepare_kernel<<<(G.n_faces + 31) / 32, 32, 0, st>>>(G, S, P);
   return cudaGetLastError();
 }
 
-cudaError_t mixed_step(const DevGeomMixed& G, const DevState& S, const PhysParams& P,
+cudaError_t mixed_step(const DevGeomMixed& G, const DevState& S, const PhysParams& P, double dt0,
                        cudaStream_t st, cudaEvent_t* ev) {
-  const int nb = mx::blocks_for(G.n_faces);
+  const int ntile = (G.n_faces + mx::kFaceTile - 1) / mx::kFaceTile;
+  const dim3 rgrid(mx::blocks_for(G.n_faces), G.max_slots);
+  const dim3 fblock(mx::kFaceTile, G.max_slots);
   if (ev) cudaEventRecord(ev[0], st);
-  cudaError_t e = dt_reduce(S, P, nb, st, /*squared_speeds=*/true);
-  if (e != cudaSuccess) return e;
+  mx::finalize_kernel<<<1, 1, 0, st>>>(S, P, dt0);
   if (ev) cudaEventRecord(ev[1], st);
-  mx::reconstruct_kernel<<<nb, mx::kBlock, 0, st>>>(G, S, P);
+  mx::reconstruct_kernel<<<rgrid, mx::kBlock, 0, st>>>(G, S, P);
   if (ev) cudaEventRecord(ev[2], st);
-  mx::flux_update_kernel<1><<<nb, mx::kBlock, 0, st>>>(G, S, P);
+  mx::flux_update_kernel<1><<<ntile, fblock, 0, st>>>(G, S, P);
   if (ev) cudaEventRecord(ev[3], st);
-  mx::reconstruct_kernel<<<nb, mx::kBlock, 0, st>>>(G, S, P);
+  mx::reconstruct_kernel<<<rgrid, mx::kBlock, 0, st>>>(G, S, P);
   if (ev) cudaEventRecord(ev[4], st);
-  mx::flux_update_kernel<2><<<nb, mx::kBlock, 0, st>>>(G, S, P);
+  mx::flux_update_kernel<2><<<ntile, fblock, 0, st>>>(G, S, P);
   if (ev) cudaEventRecord(ev[5], st);
   return cudaGetLastError();
 }
+
+cudaError_t ensemble_prepare(const EnsInstance* inst, int n_inst, const int2* ftiles, int n_ftiles,
+                             cudaStream_t st) {
+  mx::ens_reset_keys_kernel<<<(n_inst + 127) / 128, 128, 0, st>>>(inst, n_inst);
+  mx::ens_prepare_kernel<<<n_ftiles, 32, 0, st>>>(inst, ftiles);
+  return cudaGetLastError();
+}
+
+cudaError_t ensemble_step(const EnsInstance* inst, int n_inst, const int2* rtiles, int n_rtiles,
+                          int recon_width, const int2* ftiles, int n_ftiles, int max_slots, double dt0,
+                          cudaStream_t st) {
+  const dim3 rgrid(n_rtiles, max_slots);
+  const dim3 fblock(mx::kFaceTile, max_slots);
+  mx::ens_finalize_kernel<<<(n_inst + 127) / 128, 128, 0, st>>>(inst, n_inst, dt0);
+  mx::ens_reconstruct_kernel<<<rgrid, recon_width, 0, st>>>(inst, rtiles);
+  mx::ens_flux_kernel<1><<<n_ftiles, fblock, 0, st>>>(inst, ftiles);
+  mx::ens_reconstruct_kernel<<<rgrid, recon_width, 0, st>>>(inst, rtiles);
+  mx::ens_flux_kernel<2><<<n_ftiles, fblock, 0, st>>>(inst, ftiles);
+  return cudaGetLastError();
+}
+
+const void* ensemble_finalize_kernel_ptr() { return (const void*)mx::ens_finalize_kernel; }
 
 }  // namespace splash

@@ -51,6 +51,10 @@ EXPORTED = (
     "splash_write_t_L", "splash_get_light_curves", "splash_write_final_state",
     "splash_geometry_build", "splash_geometry_free", "splash_geometry_info",
     "splash_geometry_get", "splash_stream", "splash_kernel_times", "splash_memory",
+    "splash_ensemble_create", "splash_ensemble_destroy", "splash_ensemble_do_steps",
+    "splash_ensemble_synchronize", "splash_ensemble_stream", "splash_ensemble_get_state",
+    "splash_ensemble_member_info", "splash_ensemble_schedule", "splash_ensemble_size",
+    "splash_cfl_dt_noalloc",
 )
 
 
@@ -72,6 +76,14 @@ class Params(C.Structure):
         ("accretion_rate", C.c_double), ("e_acc", C.c_double), ("omega_acc_abs", C.c_double),
         ("tilt_angle", C.c_double), ("acc_width", C.c_double), ("alpha", C.c_double),
         ("friction_on", C.c_int),
+    ]
+
+
+class Member(C.Structure):
+    _fields_ = [
+        ("mesh_kind", C.c_int), ("level", C.c_int), ("U_in", C.POINTER(C.c_double)),
+        ("gam", C.c_double), ("omega_ns", C.c_double), ("accretion_on", C.c_int),
+        ("params", Params), ("solver_kind", C.c_int),
     ]
 
 
@@ -115,6 +127,13 @@ def library(path: str | os.PathLike | None = None) -> C.CDLL:
         "splash_stream": [vp, C.POINTER(vp)],
         "splash_kernel_times": [vp, C.c_int, C.c_double, dp],
         "splash_memory": [vp, C.POINTER(C.c_int64)],
+        "splash_ensemble_create": [C.POINTER(Member), C.c_int, C.c_int, C.c_int, C.POINTER(vp)],
+        "splash_ensemble_destroy": [vp], "splash_ensemble_do_steps": [vp, C.c_int, C.c_double],
+        "splash_ensemble_synchronize": [vp], "splash_ensemble_stream": [vp, C.POINTER(vp)],
+        "splash_ensemble_get_state": [vp, C.c_int, dp],
+        "splash_ensemble_member_info": [vp, C.c_int, dp, C.POINTER(C.c_uint32)],
+        "splash_ensemble_schedule": [vp, ip, ip, dp],
+        "splash_ensemble_size": [vp, ip, C.POINTER(C.c_int64)],
     }.items():
         fn = getattr(lib, name)
         fn.argtypes = args
@@ -427,6 +446,84 @@ class MUSCL_HLLC(_Named):
 class MUSCL_HLLCplus(_Named):
     """Riemann_solvers/HLLCplus.hpp:11-13 (mesh, U_in, dim, gam, omega_ns, accretion_on, threads)."""
     _KIND = SOLVER_HLLCPLUS
+
+
+class Ensemble:
+    """Many independent solvers advanced together (FP32/FP64 mixed).
+
+    members: list of dicts with keys mesh (Mesh), U_in, gam, omega_ns,
+    accretion_on, params (SolverParams), solver."""
+
+    def __init__(self, members, device: int = 0, autotune: bool = True):
+        lib = library()
+        self._lib = lib
+        self.handle = C.c_void_p()
+        self._keep = []
+        arr = (Member * len(members))()
+        self.n_faces = []
+        for i, m in enumerate(members):
+            U = np.ascontiguousarray(m["U_in"], dtype=np.float64)
+            self._keep.append(U)
+            mesh = m["mesh"]
+            arr[i].mesh_kind = mesh.kind
+            arr[i].level = mesh.level
+            arr[i].U_in = _dptr(U)
+            arr[i].gam = m["gam"]
+            arr[i].omega_ns = m.get("omega_ns", 0.0)
+            arr[i].accretion_on = 1 if m.get("accretion_on", False) else 0
+            arr[i].params = (m.get("params") or SolverParams()).to_c()
+            arr[i].solver_kind = m.get("solver", SOLVER_HLLCPLUS)
+            self.n_faces.append(U.shape[0])
+        _check(lib.splash_ensemble_create(arr, len(members), device, 1 if autotune else 0,
+                                          C.byref(self.handle)))
+        self._keep = []
+
+    def close(self):
+        if self.handle:
+            self._lib.splash_ensemble_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def do_steps(self, n: int, dt0: float) -> None:
+        _check(self._lib.splash_ensemble_do_steps(self.handle, n, dt0))
+
+    def synchronize(self) -> None:
+        _check(self._lib.splash_ensemble_synchronize(self.handle))
+
+    def stream(self) -> int:
+        p = C.c_void_p()
+        _check(self._lib.splash_ensemble_stream(self.handle, C.byref(p)))
+        return int(p.value or 0)
+
+    def get_state(self, member: int) -> np.ndarray:
+        U = np.empty((self.n_faces[member], 5))
+        _check(self._lib.splash_ensemble_get_state(self.handle, member, _dptr(U)))
+        return U
+
+    def member_info(self, member: int) -> dict:
+        out = np.zeros(4)
+        err = C.c_uint32()
+        _check(self._lib.splash_ensemble_member_info(self.handle, member, _dptr(out), C.byref(err)))
+        return {"t": out[0], "dt": out[1], "max_vel": out[2], "extra_dt": out[3], "err": int(err.value)}
+
+    def schedule(self) -> dict:
+        o = C.c_int()
+        w = C.c_int()
+        ms = np.zeros(9)
+        _check(self._lib.splash_ensemble_schedule(self.handle, C.byref(o), C.byref(w), _dptr(ms)))
+        return {"order": ["member", "largest-first", "round-robin"][o.value], "recon_width": w.value,
+                "trial_ms": ms.reshape(3, 3).tolist()}
+
+    def size(self) -> tuple[int, int]:
+        n = C.c_int()
+        t = C.c_int64()
+        _check(self._lib.splash_ensemble_size(self.handle, C.byref(n), C.byref(t)))
+        return n.value, t.value
 
 
 def read_input_dat(path, n_faces: int, dim: int) -> np.ndarray:

@@ -101,3 +101,22 @@ def test_mass_conservation_without_sources():
         s.do_steps(200, 1e-3)
         m = np.sum(g["area"] * s.get_state()[:, 0])
         assert abs(m / m0 - 1) < tol, (prec, m / m0 - 1)
+
+
+def test_mixed_dt0_changes_between_steps():
+    """do_step(dt0) with a different dt0 on every call: the captured step's
+    dt0 argument is rewritten in the instantiated graph and each step uses
+    its own dt0 (unclipped here), like MUSCL_base.hpp:100."""
+    c = load("state_hex3_hllcp_acc.npz")
+    s = make(c, 1)
+    t = 0.0
+    for dt0 in (1e-3, 5e-4, 5e-4, 2e-4, 1e-3):
+        s.do_step(dt0)
+        assert s.last_dt() == dt0
+        t += dt0
+    assert abs(s.time() - t) < 1e-15
+    # the same sequence on the FP64 path gives the same times
+    f = make(c, 0)
+    for dt0 in (1e-3, 5e-4, 5e-4, 2e-4, 1e-3):
+        f.do_step(dt0)
+    assert abs(f.time() - s.time()) < 1e-15
