@@ -41,6 +41,18 @@ PARAMS = dict(accretion_rate=1e-2, e_acc=0.5, omega_acc_abs=0.5, tilt_angle=0.2,
               alpha=1e-6, friction_on=True)
 
 
+def measured_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, or None."""
+    p = REPO / "profiles" / "traffic_hex7_mixed.txt"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        parts = line.split()
+        if len(parts) == 2 and parts[0] == kernel and not line.startswith("#"):
+            return float(parts[1])
+    return None
+
+
 def peaks():
     p = REPO / "MEASURED_PEAKS.json"
     if p.exists():
@@ -332,7 +344,8 @@ def run_ours(args):
         "mixed_over_fp64": value / value64,
         "accuracy": acc,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm,
-                     "unit": "GB/s", "frac": ach / hbm, "traffic": None,
+                     "unit": "GB/s", "frac": ach / hbm, "traffic": measured_traffic(dom),
+                     "algorithmic_bytes": algorithmic_bytes_mixed(geom, dom),
                      "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)",
                      "kernel_ms": kern},
         "clocks": clk,
