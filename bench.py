@@ -269,6 +269,60 @@ def ensemble_workload(sg, torch, steps=500, n_members=512, seed=3):
     return out
 
 
+def adjoint_workload(sg, torch, steps=1000, checkpoint_every=50, level=6, seed=4):
+    """The discrete-adjoint workload: icosphere_hex(6), HLLC, dim 5, FP64,
+    1000 steps at dt0 = 5e-4, checkpoints every 50 steps; rotating-blob
+    initial state (seed 4); accretion on (rate 1e-2, tilt 0.1, omega_acc 0.5,
+    width 0.1, e_acc 0.5, friction on); loss 1/2 sum area (Sigma - Sigma*)^2
+    against a run with rate 2e-2, tilt 0.3.  Cost = gradient time (forward
+    with checkpoints + recomputing backward, CUDA events) over the plain FP64
+    forward of the same steps (graph replays, CUDA events); one seeded
+    direction is checked against the tangent-linear model."""
+    dt0 = 5e-4
+    gam = sg.initial_conditions.gam2d(4 / 3)
+    mesh = sg.icosphere_hex(level)
+    geo = sg.Geometry(mesh)
+    U0 = sg.initial_conditions.rotating_blob(geo.unit_face_centers(), gam, seed=seed)
+    theta = np.array([1e-2, 0.1, 0.5])
+    params = sg.SolverParams(accretion_rate=theta[0], e_acc=0.5, omega_acc_abs=theta[2], tilt_angle=theta[1],
+                             acc_width=0.1, alpha=1e-6, friction_on=True)
+    base = sg.MUSCL_HLLC(mesh, U0, 5, gam, 0.0, True, params=params, precision=sg.PREC_FP64)
+    adj = sg.Adjoint(base, checkpoint_every=checkpoint_every)
+    stream = torch.cuda.ExternalStream(base.stream())
+    base.do_steps(3, dt0)
+    base.synchronize()
+    base.set_state(U0)
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    base.do_steps(steps, dt0)
+    b.record(stream)
+    b.synchronize()
+    fwd_ms = a.elapsed_time(b)
+    target = adj.forward(U0, np.array([2e-2, 0.3, 0.5]), steps, dt0)[:, 0].copy()
+    loss, gU, gth = adj.run(U0, theta, steps, dt0, target)
+    info = adj.info()
+    Uf = adj.forward(U0, theta, steps, dt0)
+    rng = np.random.default_rng(seed)
+    dU = rng.normal(size=U0.shape) * np.maximum(np.abs(U0).max(axis=0), 1e-3)
+    dth = rng.normal(size=3) * np.array([1e-2, 0.1, 0.5])
+    _, dUt = adj.tlm(U0, theta, dU, dth, steps, dt0)
+    tlm_ms = adj.info()["ms_tlm"]
+    g_adj = float(np.sum(gU * dU) + np.dot(gth, dth))
+    g_tlm = float(np.sum(geo["area"] * (Uf[:, 0] - target) * dUt[:, 0]))
+    out = {"workload": f"icosphere_hex({level}) {base.n_faces} faces, HLLC, FP64, {steps} steps dt0={dt0}, "
+                       f"checkpoints every {checkpoint_every}",
+           "forward_ms": fwd_ms, "gradient_forward_ms": info["ms_forward"],
+           "gradient_backward_ms": info["ms_backward"],
+           "adjoint_over_forward": (info["ms_forward"] + info["ms_backward"]) / fwd_ms,
+           "tlm_over_forward": tlm_ms / fwd_ms, "clipped_steps": info["clipped_steps"],
+           "loss": loss, "grad_theta": gth.tolist(), "rel_adjoint_vs_tlm": abs(g_adj - g_tlm) / abs(g_tlm),
+           "device_bytes": info["device_bytes"]}
+    adj.close()
+    base.close()
+    return out
+
+
 def l1_rel(a, b, area):
     num = np.sum(area[:, None] * np.abs(a - b), axis=0)
     den = np.sum(area[:, None] * np.abs(b), axis=0)
@@ -354,6 +408,8 @@ def run_ours(args):
     fp64.close()
     if not args.no_ensemble:
         line["ensemble"] = ensemble_workload(sg, torch)
+    if not args.no_adjoint:
+        line["adjoint"] = adjoint_workload(sg, torch)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(geom, U0, gam)
     if rank == 0:
@@ -405,6 +461,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

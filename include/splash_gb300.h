@@ -261,6 +261,57 @@ SPLASH_API int splash_cfl_dt_noalloc(const double* U, const double* unit_centres
                           int n_faces, double gam, double omega_ns, double alpha, double h0,
                           double dt0, double* out, void* stream);
 
+/* ---- tangent-linear model and discrete adjoint of N FP64 do_step calls --
+ * No counterpart in the reference (it has no derivative code).  The
+ * differentiated map is U0 (and theta) -> the state after n_steps FP64
+ * do_step(dt0) calls, with theta = {accretion_rate, tilt_angle,
+ * omega_acc_abs} (the splash_params fields of the same names; the other
+ * parameters, mesh, solver kind, gam and omega_ns come from `base`).  The
+ * dt schedule of the forward run is frozen: the CFL clip is a min() and its
+ * derivative is taken on the branch the forward took, so dt does not depend
+ * on the state (splash_adjoint_info reports the steps the clip shortened).
+ * Limiter kinks, Riemann wave-speed sides, HLLC+ switches and the density
+ * and pressure floors likewise reuse the forward's branch choices.
+ *
+ * An adjoint object borrows the geometry of `base` (an FP64 solver, which
+ * must outlive it) and owns its own state.  The forward run keeps the state
+ * every `checkpoint_every` steps; the backward run recomputes each interval
+ * from its checkpoint (the tape of one interval: about
+ * checkpoint_every * (20 + 10 * max_slots) * 8 bytes per face) and sweeps it
+ * in reverse.  States and adjoints are [n_faces][5] in reference face
+ * order; every call is synchronous. */
+typedef struct splash_adjoint splash_adjoint;
+
+SPLASH_API int splash_adjoint_create(splash_solver* base, int checkpoint_every, splash_adjoint** out);
+SPLASH_API int splash_adjoint_destroy(splash_adjoint* a);
+/* Runs n_steps from U0 with theta (NULL: base's parameters); keeps the
+ * checkpoints and the dt schedule; U_final may be NULL. */
+SPLASH_API int splash_adjoint_forward(splash_adjoint* a, const double* U0, const double* theta, int n_steps,
+                                      double dt0, double* U_final);
+/* Given lambda_final = dLoss/dU_final of the last forward run, writes
+ * grad_U0 = dLoss/dU0 ([n_faces][5]) and grad_theta[3] = dLoss/dtheta
+ * (either may be NULL). */
+SPLASH_API int splash_adjoint_backward(splash_adjoint* a, const double* lambda_final, double* grad_U0,
+                                       double* grad_theta);
+/* forward + loss = 1/2 sum_n area_n (Sigma_final_n - sigma_target_n)^2 +
+ * backward (area from the base solver's geometry, reference order). */
+SPLASH_API int splash_adjoint_run(splash_adjoint* a, const double* U0, const double* theta, int n_steps,
+                                  double dt0, const double* sigma_target, double* loss, double* grad_U0,
+                                  double* grad_theta);
+/* Tangent-linear run: U_final and its directional derivative dU_final
+ * along (dU0, dtheta) (NULL directions are zero).  The values are
+ * bit-identical to the FP64 forward run. */
+SPLASH_API int splash_tlm_run(splash_adjoint* a, const double* U0, const double* theta, const double* dU0,
+                              const double* dtheta, int n_steps, double dt0, double* U_final,
+                              double* dU_final);
+/* out[8]: steps of the last forward, steps whose dt the CFL clip shortened,
+ * min dt, max dt, forward ms, backward ms, last TLM ms (CUDA events), device
+ * bytes held. */
+SPLASH_API int splash_adjoint_info(splash_adjoint* a, double out[8]);
+SPLASH_API int splash_adjoint_error_word(splash_adjoint* a, unsigned* err);
+/* The dt of every step of the last forward run (n >= n_steps). */
+SPLASH_API int splash_adjoint_dt_schedule(splash_adjoint* a, double* dts, int n);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif

@@ -13,6 +13,9 @@ int fp64_partial_blocks(int n_faces);
 // W0 and the dt partials of the current U (after the state is set).
 cudaError_t fp64_prepare(const DevGeom& G, const DevState& S, const PhysParams& P, cudaStream_t st);
 cudaError_t fp64_set_dt0(const DevState& S, double dt0, cudaStream_t st);
+// The dt clip of one step alone (first launch of fp64_step): reduces the
+// per-block partials of the current state into S.scal.
+cudaError_t fp64_dt(const DevState& S, const PhysParams& P, int n_faces, cudaStream_t st);
 // One do_step (five launches; capturable).  With `ev` non-null (6 events)
 // an event is recorded before the first and after every launch.
 cudaError_t fp64_step(const DevGeom& G, const DevState& S, const PhysParams& P, cudaStream_t st,

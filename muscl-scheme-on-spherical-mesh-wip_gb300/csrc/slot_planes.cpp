@@ -151,15 +151,33 @@ double area_coefficient(const RefGeometry& g, double acc_width) {
 
 std::vector<double> accretion_source(const SlotPlanes& sp, const splash_params& par,
                                      double area_coeff, bool accretion_on) {
-  std::vector<double> acc(sp.fpad, 0.0);
+  return accretion_source_fcn(sp.fcn, sp.n_faces, sp.fpad, par, area_coeff, accretion_on);
+}
+
+std::vector<double> accretion_source_fcn(const std::vector<double>& fcn, int n_faces, int fpad,
+                                         const splash_params& par, double area_coeff, bool accretion_on,
+                                         std::vector<double>* d_rate, std::vector<double>* d_tilt) {
+  std::vector<double> acc(fpad, 0.0);
+  if (d_rate) d_rate->assign(fpad, 0.0);
+  if (d_tilt) d_tilt->assign(fpad, 0.0);
   if (!accretion_on) return acc;
   const double sigma = par.acc_width / 2.355;
   const double mu = M_PI / 2;
-  for (int i = 0; i < sp.n_faces; ++i) {
-    const V3 fcn{sp.fcn[i], sp.fcn[sp.fpad + i], sp.fcn[2 * (size_t)sp.fpad + i]};
-    const double theta_acc = std::acos(fcn.y * std::sin(par.tilt_angle) + fcn.z * std::cos(par.tilt_angle));
-    acc[i] = 1 / area_coeff * par.accretion_rate / std::sqrt(2 * M_PI * sigma * sigma) *
-             std::exp(-(theta_acc - mu) * (theta_acc - mu) / (2 * sigma * sigma));
+  const double st = std::sin(par.tilt_angle), ct = std::cos(par.tilt_angle);
+  for (int i = 0; i < n_faces; ++i) {
+    const V3 c{fcn[i], fcn[fpad + i], fcn[2 * (size_t)fpad + i]};
+    const double x = c.y * std::sin(par.tilt_angle) + c.z * std::cos(par.tilt_angle);
+    const double theta_acc = std::acos(x);
+    const double g = std::exp(-(theta_acc - mu) * (theta_acc - mu) / (2 * sigma * sigma));
+    acc[i] = 1 / area_coeff * par.accretion_rate / std::sqrt(2 * M_PI * sigma * sigma) * g;
+    // d acc / d rate, and d acc / d tilt through theta_acc = acos(x)
+    if (d_rate) (*d_rate)[i] = 1 / area_coeff / std::sqrt(2 * M_PI * sigma * sigma) * g;
+    if (d_tilt) {
+      const double dx = c.y * ct - c.z * st;
+      const double s2 = 1 - x * x;
+      const double dtheta = (s2 > 0) ? -dx / std::sqrt(s2) : 0.0;
+      (*d_tilt)[i] = acc[i] * (-(theta_acc - mu) / (sigma * sigma)) * dtheta;
+    }
   }
   return acc;
 }

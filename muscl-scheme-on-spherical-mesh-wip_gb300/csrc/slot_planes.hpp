@@ -39,6 +39,14 @@ double area_coefficient(const RefGeometry& g, double acc_width);
 std::vector<double> accretion_source(const SlotPlanes& sp, const splash_params& par,
                                      double area_coeff, bool accretion_on);
 
+// The same profile from the unit face centres alone (3 planes of fpad),
+// and its partial derivatives with respect to accretion_rate and
+// tilt_angle (d_rate, d_tilt; the adjoint's parameter gradients).
+std::vector<double> accretion_source_fcn(const std::vector<double>& fcn, int n_faces, int fpad,
+                                         const splash_params& par, double area_coeff, bool accretion_on,
+                                         std::vector<double>* d_rate = nullptr,
+                                         std::vector<double>* d_tilt = nullptr);
+
 // FP32 planes of the mixed path.
 struct MixedPlanes {
   std::vector<float> fcn32, beta, inv_h, bm, eta, arc, ec, en, nxr, coef;

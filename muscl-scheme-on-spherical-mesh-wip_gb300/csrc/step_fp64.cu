@@ -21,6 +21,7 @@
 
 #include "kernels.hpp"
 #include "physics_fp64.cuh"
+#include "step_body_fp64.cuh"
 #include "reduce.cuh"
 
 namespace splash {
@@ -28,10 +29,6 @@ namespace f64 {
 namespace {
 
 constexpr int kBlock = 128;
-
-__device__ __forceinline__ D3 plane3(const double* p, int stride, int i) {
-  return D3{p[i], p[stride + i], p[2 * stride + i]};
-}
 
 // ---------------------------------------------------------------------
 // W = (Sigma, l, Pi) of the conserved state and the partials of it
@@ -45,9 +42,10 @@ __global__ void __launch_bounds__(kBlock) prepare_kernel(DevGeom G, DevState S, 
 #pragma unroll
     for (int k = 0; k < kDim; ++k) u[k] = S.U[k * G.fpad + f];
     const D3 r = plane3(G.fcn, G.fpad, f);
+    double w[kDim];
+    prim_of(u, r, P.gam, w);
 #pragma unroll
-    for (int k = 0; k < 4; ++k) S.W0[k * G.fpad + f] = u[k] - 0.0;
-    S.W0[4 * G.fpad + f] = pressure_fc(u, r, P.gam) - 0.0;
+    for (int k = 0; k < kDim; ++k) S.W0[k * G.fpad + f] = w[k];
     dt_candidates(u, r, G.area[f], P, vmax, dmin, sums);
   }
   red::block_partials<kBlock>(vmax, dmin, sums, S.partial + (size_t)blockIdx.x * kPartialStride);
@@ -102,55 +100,7 @@ __global__ void __launch_bounds__(kBlock) reconstruct_kernel(DevGeom G, const do
                                                              PhysParams P) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= G.n_faces) return;
-  const int fp = G.fpad;
-  const int PS = G.max_slots * fp;  // one slot-plane set
-  const double dt = sc[kScDt];
-  double w[kDim];
-#pragma unroll
-  for (int k = 0; k < kDim; ++k) w[k] = W[k * fp + f];
-  const int n = G.nslots[f];
-  const double twoN = (double)(2 * n);
-  const double gam = P.gam;
-  const double c = sqrt(gam * (w[4] + 0.0) / (w[0] + 0.0));  // sound speed (per face)
-  for (int j = 0; j < n; ++j) {
-    const int s = j * fp + f;
-    const int ia = G.sten[s], ib = G.sten[PS + s], ic = G.sten[2 * PS + s], id = G.sten[3 * PS + s];
-    const double bp0 = G.beta[s], bp1 = G.beta[PS + s], bm0 = G.beta[2 * PS + s], bm1 = G.beta[3 * PS + s];
-    const double hp = G.hpm[s], hm = G.hpm[PS + s], bmd = G.bm[s];
-    const double ihp = 1.0 / hp, ihm = 1.0 / hm;
-    double pp[kDim], r[kDim];
-#pragma unroll
-    for (int k = 0; k < kDim; ++k) {
-      const double* Wk = W + k * fp;
-      const double Up = bp0 * Wk[ia] + bp1 * Wk[ib];
-      pp[k] = (Up - w[k]) * ihp;
-      const double Um = bm0 * Wk[ic] + bm1 * Wk[id];
-      const double pm = (-Um + w[k]) * ihm;
-      r[k] = pm / pp[k];
-    }
-    // Courant factor of the limiter (adiabatic.hpp:741-758, 792-810)
-    const D3 ec = plane3(G.ec, PS, s);
-    const double ecn = G.ecn[s];
-    const D3 en = plane3(G.en, PS, s);
-    D3 vel = cross3(ec, d3(w[1], w[2], w[3]));
-    vel = scal(vel, 1.0 / ((-w[0] - 0.0) * ecn));
-    const double nu_plus = (c + dot3(vel, en)) * dt * G.arc_a[s];
-    const double eta_p = G.eta[s];
-    const double sb_scale = G.eta[PS + s] / (twoN * nu_plus);
-    const double to_scale = (1 + nu_plus) / 3;
-    double up[kDim];
-#pragma unroll
-    for (int k = 0; k < kDim; ++k) {
-      const double lim = limiter_field(r[k], eta_p, sb_scale, to_scale);
-      if (k == 0 || k == 4)
-        up[k] = w[k] + 0.0 + pp[k] * lim * bmd;
-      else
-        up[k] = w[k] + pp[k] * lim * bmd;
-    }
-    up[4] = energy_at_edge(up, ec, gam);  // Pi -> E at the edge centre
-#pragma unroll
-    for (int k = 0; k < kDim; ++k) uplus[k * PS + s] = up[k];
-  }
+  recon_face<double>(G, P, sc[kScDt], Planes<double>{const_cast<double*>(W)}, Planes<double>{uplus}, f);
 }
 
 // find_flux_var + res2d + the RK combine with the density floor
@@ -162,56 +112,25 @@ __global__ void __launch_bounds__(kBlock) flux_update_kernel(DevGeom G, DevState
   double vmax = 0.0, dmin = 1e20, sums[5] = {0, 0, 0, 0, 0};
   if (f < G.n_faces) {
     const int fp = G.fpad;
-    const int PS = G.max_slots * fp;
     const double dt = S.scal[kScDt];
     const double dt_here = (STAGE == 1) ? dt / 2 : dt;
-    const double* Win = (STAGE == 1) ? S.W0 : S.W1;
-    const D3 fcn = plane3(G.fcn, fp, f);
-    const double area = G.area[f];
-    double w[kDim], acc[kDim];
-#pragma unroll
-    for (int k = 0; k < kDim; ++k) w[k] = Win[k * fp + f];
-    source_term(w, fcn, G.acc_src[f], P, acc);
-#pragma unroll
-    for (int k = 0; k < kDim; ++k) acc[k] = dt_here * acc[k];
-    const double rd_dt = P.round_diff * dt_here;
-    const int n = G.nslots[f];
-    unsigned bits = 0;
-    for (int j = 0; j < n; ++j) {
-      const int s = j * fp + f;
-      const int rv = G.rev[s];
-      double uL[kDim], uR[kDim], F[kDim];
-#pragma unroll
-      for (int k = 0; k < kDim; ++k) {
-        uL[k] = S.uplus[k * PS + s];
-        uR[k] = S.uplus[k * PS + rv];
-      }
-      SlotGeom g;
-      g.ec = plane3(G.ec, PS, s);
-      g.ecn = G.ecn[s];
-      g.en = plane3(G.en, PS, s);
-      g.nxr = plane3(G.nxr, PS, s);
-      bits |= flux_star(uL, uR, g, P.gam, P.solver, F);
-      const double coef = rd_dt * G.chord[s] / area;
-#pragma unroll
-      for (int k = 0; k < kDim; ++k) {
-        if (isnan(F[k])) bits |= 1u;
-        acc[k] -= coef * F[k];
-      }
-    }
-    if (bits) atomicOr(S.err, bits);
     double u[kDim];
-#pragma unroll
-    for (int k = 0; k < kDim; ++k) u[k] = acc[k] + S.U[k * fp + f];
-    if (u[0] < 1e-8) u[0] = 1e-8;
+    bool floored;
+    const unsigned bits =
+        flux_face<double, double>(G, P, face_src_params<double>(G, P, f), dt_here,
+                                  Planes<double>{(STAGE == 1) ? S.W0 : S.W1}, Planes<double>{S.U},
+                                  Planes<double>{S.uplus}, f, u, floored);
+    if (bits) atomicOr(S.err, bits);
+    const D3 fcn = plane3(G.fcn, fp, f);
+    double w[kDim];
+    prim_of(u, fcn, P.gam, w);
     double* Wout = (STAGE == 1) ? S.W1 : S.W0;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) Wout[k * fp + f] = u[k] - 0.0;
-    Wout[4 * fp + f] = pressure_fc(u, fcn, P.gam) - 0.0;
+    for (int k = 0; k < kDim; ++k) Wout[k * fp + f] = w[k];
     if (STAGE == 2) {
 #pragma unroll
       for (int k = 0; k < kDim; ++k) S.U[k * fp + f] = u[k];
-      dt_candidates(u, fcn, area, P, vmax, dmin, sums);
+      dt_candidates(u, fcn, G.area[f], P, vmax, dmin, sums);
     }
   }
   if (STAGE == 2) red::block_partials<kBlock>(vmax, dmin, sums, S.partial + (size_t)blockIdx.x * kPartialStride);
@@ -248,6 +167,11 @@ int fp64_partial_blocks(int n_faces) { return f64::blocks_for(n_faces); }
 cudaError_t fp64_prepare(const DevGeom& G, const DevState& S, const PhysParams& P,
                          cudaStream_t st) {
   f64::prepare_kernel<<<f64::blocks_for(G.n_faces), f64::kBlock, 0, st>>>(G, S, P);
+  return cudaGetLastError();
+}
+
+cudaError_t fp64_dt(const DevState& S, const PhysParams& P, int n_faces, cudaStream_t st) {
+  f64::dt_kernel<<<1, 256, 0, st>>>(S, P, f64::blocks_for(n_faces));
   return cudaGetLastError();
 }
 

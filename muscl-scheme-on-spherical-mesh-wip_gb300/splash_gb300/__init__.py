@@ -55,6 +55,9 @@ EXPORTED = (
     "splash_ensemble_synchronize", "splash_ensemble_stream", "splash_ensemble_get_state",
     "splash_ensemble_member_info", "splash_ensemble_schedule", "splash_ensemble_size",
     "splash_cfl_dt_noalloc",
+    "splash_adjoint_create", "splash_adjoint_destroy", "splash_adjoint_forward",
+    "splash_adjoint_backward", "splash_adjoint_run", "splash_tlm_run", "splash_adjoint_info",
+    "splash_adjoint_error_word", "splash_adjoint_dt_schedule",
 )
 
 
@@ -134,6 +137,15 @@ def library(path: str | os.PathLike | None = None) -> C.CDLL:
         "splash_ensemble_member_info": [vp, C.c_int, dp, C.POINTER(C.c_uint32)],
         "splash_ensemble_schedule": [vp, ip, ip, dp],
         "splash_ensemble_size": [vp, ip, C.POINTER(C.c_int64)],
+        "splash_adjoint_create": [vp, C.c_int, C.POINTER(vp)],
+        "splash_adjoint_destroy": [vp],
+        "splash_adjoint_forward": [vp, dp, dp, C.c_int, C.c_double, dp],
+        "splash_adjoint_backward": [vp, dp, dp, dp],
+        "splash_adjoint_run": [vp, dp, dp, C.c_int, C.c_double, dp, dp, dp, dp],
+        "splash_tlm_run": [vp, dp, dp, dp, dp, C.c_int, C.c_double, dp, dp],
+        "splash_adjoint_info": [vp, dp],
+        "splash_adjoint_error_word": [vp, C.POINTER(C.c_uint32)],
+        "splash_adjoint_dt_schedule": [vp, dp, C.c_int],
     }.items():
         fn = getattr(lib, name)
         fn.argtypes = args
@@ -524,6 +536,101 @@ class Ensemble:
         t = C.c_int64()
         _check(self._lib.splash_ensemble_size(self.handle, C.byref(n), C.byref(t)))
         return n.value, t.value
+
+
+class Adjoint:
+    """Tangent-linear model and discrete adjoint of n FP64 do_step calls.
+
+    ``base`` is an FP64 :class:`Solver` whose mesh, solver kind, gam,
+    omega_ns and parameters define the map; theta = (accretion_rate,
+    tilt_angle, omega_acc_abs).  The dt schedule of the forward run is
+    frozen (the derivative of the CFL min() on the branch taken).  States
+    are [n_faces, 5] arrays in reference face order."""
+
+    def __init__(self, base: Solver, checkpoint_every: int = 50):
+        lib = library()
+        self._lib = lib
+        self.base = base  # the adjoint borrows its geometry
+        self.n_faces = base.n_faces
+        self.handle = C.c_void_p()
+        _check(lib.splash_adjoint_create(base.handle, checkpoint_every, C.byref(self.handle)))
+
+    def close(self):
+        if self.handle:
+            self._lib.splash_adjoint_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def _arr(a, shape=None):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        if shape is not None and a.size != int(np.prod(shape)):
+            raise ValueError(f"expected {shape} values, got {a.shape}")
+        return a
+
+    def _p(self, a):
+        return _dptr(a) if a is not None else None
+
+    def forward(self, U0, theta, n_steps: int, dt0: float) -> np.ndarray:
+        U0 = self._arr(U0, (self.n_faces, 5))
+        th = self._arr(theta, (3,))
+        out = np.empty((self.n_faces, 5))
+        _check(self._lib.splash_adjoint_forward(self.handle, _dptr(U0), self._p(th), n_steps, dt0, _dptr(out)))
+        return out
+
+    def backward(self, lambda_final) -> tuple[np.ndarray, np.ndarray]:
+        lam = self._arr(lambda_final, (self.n_faces, 5))
+        gU = np.empty((self.n_faces, 5))
+        gth = np.empty(3)
+        _check(self._lib.splash_adjoint_backward(self.handle, _dptr(lam), _dptr(gU), _dptr(gth)))
+        return gU, gth
+
+    def run(self, U0, theta, n_steps: int, dt0: float, sigma_target) -> tuple[float, np.ndarray, np.ndarray]:
+        """loss = 1/2 sum area (Sigma_final - sigma_target)^2 and its gradients."""
+        U0 = self._arr(U0, (self.n_faces, 5))
+        th = self._arr(theta, (3,))
+        tgt = self._arr(sigma_target, (self.n_faces,))
+        loss = C.c_double()
+        gU = np.empty((self.n_faces, 5))
+        gth = np.empty(3)
+        _check(self._lib.splash_adjoint_run(self.handle, _dptr(U0), self._p(th), n_steps, dt0, _dptr(tgt),
+                                            C.byref(loss), _dptr(gU), _dptr(gth)))
+        return loss.value, gU, gth
+
+    def tlm(self, U0, theta, dU0, dtheta, n_steps: int, dt0: float) -> tuple[np.ndarray, np.ndarray]:
+        U0 = self._arr(U0, (self.n_faces, 5))
+        th = self._arr(theta, (3,))
+        dU = self._arr(dU0, (self.n_faces, 5))
+        dth = self._arr(dtheta, (3,))
+        U = np.empty((self.n_faces, 5))
+        dUf = np.empty((self.n_faces, 5))
+        _check(self._lib.splash_tlm_run(self.handle, _dptr(U0), self._p(th), self._p(dU), self._p(dth), n_steps,
+                                        dt0, _dptr(U), _dptr(dUf)))
+        return U, dUf
+
+    def info(self) -> dict:
+        o = np.zeros(8)
+        _check(self._lib.splash_adjoint_info(self.handle, _dptr(o)))
+        return {"steps": int(o[0]), "clipped_steps": int(o[1]), "dt_min": o[2], "dt_max": o[3],
+                "ms_forward": o[4], "ms_backward": o[5], "ms_tlm": o[6], "device_bytes": int(o[7])}
+
+    def error_word(self) -> int:
+        e = C.c_uint32()
+        _check(self._lib.splash_adjoint_error_word(self.handle, C.byref(e)))
+        return int(e.value)
+
+    def dt_schedule(self) -> np.ndarray:
+        n = self.info()["steps"]
+        d = np.empty(max(n, 1))
+        _check(self._lib.splash_adjoint_dt_schedule(self.handle, _dptr(d), len(d)))
+        return d[:n]
 
 
 def read_input_dat(path, n_faces: int, dim: int) -> np.ndarray:
