@@ -276,9 +276,9 @@ SPLASH_API int splash_cfl_dt_noalloc(const double* U, const double* unit_centres
  * An adjoint object borrows the geometry of `base` (an FP64 solver, which
  * must outlive it) and owns its own state.  The forward run keeps the state
  * every `checkpoint_every` steps; the backward run recomputes each interval
- * from its checkpoint (the tape of one interval: about
- * checkpoint_every * (20 + 10 * max_slots) * 8 bytes per face) and sweeps it
- * in reverse.  States and adjoints are [n_faces][5] in reference face
+ * from its checkpoint (the tape of one interval: checkpoint_every *
+ * (20 + 42 * max_slots) * 8 bytes per face, 4.5 GB for icosphere_hex(6) at
+ * 50 steps) and sweeps it in reverse.  States and adjoints are [n_faces][5] in reference face
  * order; every call is synchronous. */
 typedef struct splash_adjoint splash_adjoint;
 

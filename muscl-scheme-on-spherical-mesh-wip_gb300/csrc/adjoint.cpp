@@ -76,6 +76,7 @@ struct Adjoint {
   int ck_cap = 0;
   // tape of K steps + reverse scratch
   double *tU = nullptr, *tW0 = nullptr, *tU1 = nullptr, *tW1 = nullptr, *tP0 = nullptr, *tP1 = nullptr;
+  double *tJ0 = nullptr, *tJ1 = nullptr;
   uint8_t* tmask = nullptr;
   double *d_lam = nullptr, *d_scrU = nullptr, *d_scrW = nullptr;
   AdjScratch X{};
@@ -116,6 +117,8 @@ struct Adjoint {
     t.W1 = tW1 + (size_t)m * FS;
     t.P0 = tP0 + (size_t)m * kDim * PS;
     t.P1 = tP1 + (size_t)m * kDim * PS;
+    t.J0 = tJ0 + (size_t)m * kTapeJ * PS;
+    t.J1 = tJ1 + (size_t)m * kTapeJ * PS;
     t.mask = tmask + (size_t)m * fpad;
     return t;
   }
@@ -428,6 +431,8 @@ int splash_adjoint_create(splash_solver* base_h, int checkpoint_every, splash_ad
     a->tW1 = a->dalloc<double>(K * FS);
     a->tP0 = a->dalloc<double>(K * splash::kDim * PS);
     a->tP1 = a->dalloc<double>(K * splash::kDim * PS);
+    a->tJ0 = a->dalloc<double>(K * splash::kTapeJ * PS);
+    a->tJ1 = a->dalloc<double>(K * splash::kTapeJ * PS);
     a->tmask = a->dalloc<uint8_t>(K * fp);
     a->d_lam = a->dalloc<double>(FS);
     a->d_scrU = a->dalloc<double>(FS);

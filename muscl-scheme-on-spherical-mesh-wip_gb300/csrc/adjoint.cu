@@ -13,7 +13,8 @@
 //               A = (dF/duL)^T Fb, B = (dF/duR)^T Fb
 //   adj_recon   per face: the adjoint of slot s's edge state is
 //               A[s] + B[rev s] (the edge seen from both faces);
-//               reverse reconstruction -> interpolant adjoints PU, own Lw
+//               reverse reconstruction from the recomputation's limiter
+//               tape -> interpolant adjoints PU, own Lw
 //   adj_face    per face: lamW = Lw + sum over the inverse stencil of
 //               beta * PU, + source reverse (dt_here la), -> prim reverse
 // Every sum has a fixed order (no atomics): the adjoint is deterministic.
@@ -35,9 +36,13 @@ namespace {
 
 using namespace splash::f64;
 using D1 = Dual<1>;
-constexpr int kBlock = 128;  // must match the FP64 step (partials per block)
+static_assert(kTapeJ == rev::kTapePlanes, "tape plane count");
+constexpr int kBlock = 128;    // TLM kernels: must match the FP64 step (partials per block)
+constexpr int kRevBlock = 64;  // recomputation and reverse kernels (FP64-bound, register-heavy:
+                               // small blocks spread the faces evenly over the SMs)
 
 inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
+inline int rev_blocks_for(int n) { return (n + kRevBlock - 1) / kRevBlock; }
 
 __device__ __forceinline__ D1 dual1(double v, double d) {
   D1 r(v);
@@ -115,7 +120,7 @@ __global__ void __launch_bounds__(kBlock) tlm_flux_kernel(DevGeom G, DevState S,
 
 // ---------------------------------------------------------------------
 // recomputation (double, extra outputs)
-__global__ void __launch_bounds__(kBlock) rc_prim_kernel(DevGeom G, PhysParams P, const double* __restrict__ U,
+__global__ void __launch_bounds__(kRevBlock) rc_prim_kernel(DevGeom G, PhysParams P, const double* __restrict__ U,
                                                          double* __restrict__ W) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= G.n_faces) return;
@@ -128,15 +133,16 @@ __global__ void __launch_bounds__(kBlock) rc_prim_kernel(DevGeom G, PhysParams P
   for (int k = 0; k < kDim; ++k) W[(size_t)k * fp + f] = w[k];
 }
 
-__global__ void __launch_bounds__(kBlock) rc_recon_kernel(DevGeom G, PhysParams P, const double* __restrict__ dtp,
-                                                          const double* __restrict__ W, double* __restrict__ uplus) {
+__global__ void __launch_bounds__(kRevBlock) rc_recon_kernel(DevGeom G, PhysParams P, const double* __restrict__ dtp,
+                                                             const double* __restrict__ W, double* __restrict__ uplus,
+                                                             double* __restrict__ LJ) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= G.n_faces) return;
-  recon_face<double>(G, P, *dtp, Planes<double>{const_cast<double*>(W)}, Planes<double>{uplus}, f);
+  rev::recon_face_tape(G, P, *dtp, W, uplus, LJ, f);
 }
 
 template <int STAGE>
-__global__ void __launch_bounds__(kBlock) rc_flux_kernel(DevGeom G, PhysParams P, const double* __restrict__ dtp,
+__global__ void __launch_bounds__(kRevBlock) rc_flux_kernel(DevGeom G, PhysParams P, const double* __restrict__ dtp,
                                                          const double* __restrict__ Win, const double* __restrict__ U0,
                                                          const double* __restrict__ uplus, double* __restrict__ Uout,
                                                          double* __restrict__ Wout, uint8_t* __restrict__ mask) {
@@ -163,7 +169,7 @@ __global__ void __launch_bounds__(kBlock) rc_flux_kernel(DevGeom G, PhysParams P
 
 // ---------------------------------------------------------------------
 // reverse sweep
-__global__ void __launch_bounds__(kBlock) adj_flux_kernel(DevGeom G, PhysParams P, double dt_here,
+__global__ void __launch_bounds__(kRevBlock) adj_flux_kernel(DevGeom G, PhysParams P, double dt_here,
                                                           const double* __restrict__ uplus,
                                                           const double* __restrict__ lam,
                                                           const uint8_t* __restrict__ mask, int bit,
@@ -209,23 +215,27 @@ __global__ void __launch_bounds__(kBlock) adj_flux_kernel(DevGeom G, PhysParams 
   }
 }
 
-__global__ void __launch_bounds__(kBlock) adj_recon_kernel(DevGeom G, PhysParams P, double dt,
-                                                           const double* __restrict__ W, const double* __restrict__ A,
-                                                           const double* __restrict__ B, double* __restrict__ PU,
-                                                           double* __restrict__ Lw) {
+__global__ void __launch_bounds__(kRevBlock) adj_recon_kernel(DevGeom G, PhysParams P, double dt,
+                                                              const double* __restrict__ W,
+                                                              const double* __restrict__ uplus,
+                                                              const double* __restrict__ LJ,
+                                                              const double* __restrict__ A,
+                                                              const double* __restrict__ B, double* __restrict__ PU,
+                                                              double* __restrict__ Lw) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= G.n_faces) return;
   const int fp = G.fpad;
   const size_t PS = (size_t)G.max_slots * fp;
   double wb[kDim] = {0, 0, 0, 0, 0};
   rev::recon_face_rev(
-      G, P, dt, W, [&](int k, int s) { return A[(size_t)k * PS + s] + B[(size_t)k * PS + G.rev[s]]; }, PU, wb, f);
+      G, P, dt, W, uplus, LJ, [&](int k, int s) { return A[(size_t)k * PS + s] + B[(size_t)k * PS + G.rev[s]]; },
+      PU, wb, f);
 #pragma unroll
   for (int k = 0; k < kDim; ++k) Lw[(size_t)k * fp + f] = wb[k];
 }
 
 template <int STAGE>
-__global__ void __launch_bounds__(kBlock) adj_face_kernel(DevGeom G, PhysParams P, double dt_here, AdjScratch X,
+__global__ void __launch_bounds__(kRevBlock) adj_face_kernel(DevGeom G, PhysParams P, double dt_here, AdjScratch X,
                                                           const double* __restrict__ Win,
                                                           const double* __restrict__ Uin,
                                                           const double* __restrict__ la,
@@ -297,32 +307,34 @@ cudaError_t tlm_step(const DevGeom& G, const DevState& S, const TlmTangents& T, 
 }
 
 cudaError_t rc_prim(const DevGeom& G, const PhysParams& P, const double* U, double* W, cudaStream_t st) {
-  adj::rc_prim_kernel<<<adj::blocks_for(G.n_faces), adj::kBlock, 0, st>>>(G, P, U, W);
+  adj::rc_prim_kernel<<<adj::rev_blocks_for(G.n_faces), adj::kRevBlock, 0, st>>>(G, P, U, W);
   return cudaGetLastError();
 }
 
 cudaError_t rc_step(const DevGeom& G, const PhysParams& P, const double* dtp, const StepTape& t, double* U_next,
                     double* W_next, cudaStream_t st) {
-  const int nb = adj::blocks_for(G.n_faces);
-  adj::rc_recon_kernel<<<nb, adj::kBlock, 0, st>>>(G, P, dtp, t.W0, t.P0);
-  adj::rc_flux_kernel<1><<<nb, adj::kBlock, 0, st>>>(G, P, dtp, t.W0, t.U, t.P0, t.U1, t.W1, t.mask);
-  adj::rc_recon_kernel<<<nb, adj::kBlock, 0, st>>>(G, P, dtp, t.W1, t.P1);
-  adj::rc_flux_kernel<2><<<nb, adj::kBlock, 0, st>>>(G, P, dtp, t.W1, t.U, t.P1, U_next, W_next, t.mask);
+  const int nb = adj::rev_blocks_for(G.n_faces);
+  constexpr int B = adj::kRevBlock;
+  adj::rc_recon_kernel<<<nb, B, 0, st>>>(G, P, dtp, t.W0, t.P0, t.J0);
+  adj::rc_flux_kernel<1><<<nb, B, 0, st>>>(G, P, dtp, t.W0, t.U, t.P0, t.U1, t.W1, t.mask);
+  adj::rc_recon_kernel<<<nb, B, 0, st>>>(G, P, dtp, t.W1, t.P1, t.J1);
+  adj::rc_flux_kernel<2><<<nb, B, 0, st>>>(G, P, dtp, t.W1, t.U, t.P1, U_next, W_next, t.mask);
   return cudaGetLastError();
 }
 
 cudaError_t adj_step(const DevGeom& G, const PhysParams& P, double dt, const StepTape& t, const AdjScratch& X,
                      double* lam, cudaStream_t st) {
-  const int nb = adj::blocks_for(G.n_faces);
+  const int nb = adj::rev_blocks_for(G.n_faces);
+  constexpr int B = adj::kRevBlock;
   // stage 2: U2 = floor(U + dt Phi(W1, P1))
-  adj::adj_flux_kernel<<<nb, adj::kBlock, 0, st>>>(G, P, dt, t.P1, lam, t.mask, 2, X.la2, X.A, X.B);
-  adj::adj_recon_kernel<<<nb, adj::kBlock, 0, st>>>(G, P, dt, t.W1, X.A, X.B, X.PU, X.Lw);
-  adj::adj_face_kernel<2><<<nb, adj::kBlock, 0, st>>>(G, P, dt, X, t.W1, t.U1, X.la2, X.lam1);
+  adj::adj_flux_kernel<<<nb, B, 0, st>>>(G, P, dt, t.P1, lam, t.mask, 2, X.la2, X.A, X.B);
+  adj::adj_recon_kernel<<<nb, B, 0, st>>>(G, P, dt, t.W1, t.P1, t.J1, X.A, X.B, X.PU, X.Lw);
+  adj::adj_face_kernel<2><<<nb, B, 0, st>>>(G, P, dt, X, t.W1, t.U1, X.la2, X.lam1);
   // stage 1: U1 = floor(U + dt/2 Phi(W0, P0))
   const double dt_half = dt / 2;
-  adj::adj_flux_kernel<<<nb, adj::kBlock, 0, st>>>(G, P, dt_half, t.P0, X.lam1, t.mask, 1, X.la1, X.A, X.B);
-  adj::adj_recon_kernel<<<nb, adj::kBlock, 0, st>>>(G, P, dt, t.W0, X.A, X.B, X.PU, X.Lw);
-  adj::adj_face_kernel<1><<<nb, adj::kBlock, 0, st>>>(G, P, dt_half, X, t.W0, t.U, X.la1, lam);
+  adj::adj_flux_kernel<<<nb, B, 0, st>>>(G, P, dt_half, t.P0, X.lam1, t.mask, 1, X.la1, X.A, X.B);
+  adj::adj_recon_kernel<<<nb, B, 0, st>>>(G, P, dt, t.W0, t.P0, t.J0, X.A, X.B, X.PU, X.Lw);
+  adj::adj_face_kernel<1><<<nb, B, 0, st>>>(G, P, dt_half, X, t.W0, t.U, X.la1, lam);
   return cudaGetLastError();
 }
 

@@ -18,6 +18,8 @@
 
 namespace splash {
 
+constexpr int kTapeJ = 16;  // limiter-Jacobian tape planes per slot and stage
+
 // Tangents of the TLM beside a value DevState.
 struct TlmTangents {
   double* dU;
@@ -30,7 +32,8 @@ struct TlmTangents {
 
 // Primal data of one step, stored by the recomputation: the step's input
 // state and its stage-1 state, their (Sigma, l, Pi), both stages' edge
-// states and the density-floor bits (1: stage 1, 2: stage 2).
+// states, both stages' limiter Jacobians (16 planes per slot, see
+// adjoint_rev.cuh) and the density-floor bits (1: stage 1, 2: stage 2).
 struct StepTape {
   double* U;
   double* W0;
@@ -38,6 +41,8 @@ struct StepTape {
   double* W1;
   double* P0;
   double* P1;
+  double* J0;
+  double* J1;
   uint8_t* mask;
 };
 

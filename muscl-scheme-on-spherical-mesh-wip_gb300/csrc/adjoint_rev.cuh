@@ -11,9 +11,9 @@
 //   flux_star_rev     hand-written reverse of the three Riemann solvers
 //                     (HLLE_p.hpp:19-58, HLLC.hpp:138-242,
 //                     HLLCplus.hpp:17-177, char_vel adiabatic.hpp:594-683)
-//   recon_slot_rev    reverse of find_U_edges for one slot
-//                     (MUSCL_base.hpp:361-434, limiter adiabatic.hpp:685-828);
-//                     the scalar limiter chain uses Dual<3> locally
+//   recon_face_tape   find_U_edges (MUSCL_base.hpp:361-434) with the local
+//                     limiter Jacobian (adiabatic.hpp:685-828) taped per slot
+//   recon_face_rev    reverse of the reconstruction from that tape
 //   source_rev        reverse of the source term (adiabatic.hpp:396-541)
 //                     from a Dual<10> Jacobian of its 5 state and 5
 //                     parameter inputs
@@ -424,73 +424,74 @@ SPLASH_HD void flux_star_rev(const double* uL, const double* uR, const SlotGeom&
 }
 
 // ---------------------------------------------------------------------
-// Reverse of find_U_edges for one slot of a face.
-//   w      the face's (Sigma, l, Pi)          (primal)
-//   Up, Um the stencil interpolants bp0 W[ia] + bp1 W[ib], bm0 W[ic] + bm1 W[id]
-//   c      the face's sound speed, as a Dual<5> over w
-//   upb    adjoint of the slot's edge state (Sigma, l, E)
-// Outputs: Upb, Umb (adjoints of the interpolants) and wb += (own face).
-struct SlotRecon {
-  D3 ec, en;
-  double ecn, arc_a, eta_p, eta_m, hp, hm, bmd;
-};
+// Reconstruction with its reverse-sweep tape, and the reverse from the tape.
+//
+// Per slot and field the limited edge state is up = w + pp phi(r, nu) bmd
+// with pp = (Up - w)/H+, pm = (w - Um)/H-, r = pm/pp and nu the slot's
+// Courant factor (MUSCL_base.hpp:361-434, adiabatic.hpp:685-828).  The
+// recomputation evaluates phi once on Dual<2> over (r, nu) -- its value is
+// the primal's, bit for bit -- and stores the three partials
+//   d up / d pp = bmd (phi - r phi_r),  d up / d pm = bmd phi_r,
+//   d up / d nu = pp bmd phi_nu
+// so that the reverse sweep needs no transcendental.  Where phi is flat in r
+// (r = +-inf or NaN) d up / d pp = bmd phi.
+constexpr int kTapePlanes = 16;  // 3 per field + the edge pressure before Pi -> E
 
-SPLASH_HD void recon_slot_rev(const double* w, const double* Up, const double* Um, const Dual<5>& c,
-                              const SlotRecon& q, double twoN, double dt, double gam, const double* upb,
-                              double* Upb, double* Umb, double* wb) {
-  const double ihp = 1.0 / q.hp, ihm = 1.0 / q.hm;
-  // Courant factor as a function of w
-  Dual<5> wd[kDim];
+SPLASH_HD void recon_face_tape(const DevGeom& G, const PhysParams& P, double dt, const double* W, double* uplus,
+                               double* LJ, int f) {
+  const int fp = G.fpad;
+  const int PS = G.max_slots * fp;
+  double w[kDim];
 #pragma unroll
-  for (int k = 0; k < kDim; ++k) wd[k] = Dual<5>::seed(w[k], k);
-  V3<Dual<5>> vel = cross3(q.ec, v3(wd[1], wd[2], wd[3]));
-  vel = scal(vel, 1.0 / ((-wd[0] - 0.0) * q.ecn));
-  const Dual<5> nu5 = (c + dot3(vel, q.en)) * dt * q.arc_a;
-  const double nu = nu5.v;
-  // limited states per field, with partials over (pp, pm, nu)
-  double up[kDim], dpp[kDim], dpm[kDim], dnu[kDim];
+  for (int k = 0; k < kDim; ++k) w[k] = W[(size_t)k * fp + f];
+  const int n = G.nslots[f];
+  const double twoN = (double)(2 * n);
+  const double gam = P.gam;
+  const double c = sqrt(gam * (w[4] + 0.0) / (w[0] + 0.0));
+  for (int j = 0; j < n; ++j) {
+    const int s = j * fp + f;
+    const int ia = G.sten[s], ib = G.sten[PS + s], ic = G.sten[2 * PS + s], id = G.sten[3 * PS + s];
+    const double bp0 = G.beta[s], bp1 = G.beta[PS + s], bm0 = G.beta[2 * PS + s], bm1 = G.beta[3 * PS + s];
+    const double hp = G.hpm[s], hm = G.hpm[PS + s], bmd = G.bm[s];
+    const double ihp = 1.0 / hp, ihm = 1.0 / hm;
+    double pp[kDim], r[kDim];
 #pragma unroll
-  for (int k = 0; k < kDim; ++k) {
-    const double pp = (Up[k] - w[k]) * ihp;
-    const double pm = (-Um[k] + w[k]) * ihm;
-    const Dual<3> ppd = Dual<3>::seed(pp, 0);
-    const Dual<3> pmd = Dual<3>::seed(pm, 1);
-    const Dual<3> nud = Dual<3>::seed(nu, 2);
-    const Dual<3> r = pmd / ppd;
-    const Dual<3> sb_scale = q.eta_m / (twoN * nud);
-    const Dual<3> to_scale = (1 + nud) / 3;
-    const Dual<3> lim = limiter_field(r, q.eta_p, sb_scale, to_scale);
-    Dual<3> u;
-    if (k == 0 || k == 4)
-      u = w[k] + 0.0 + ppd * lim * q.bmd;
-    else
-      u = w[k] + ppd * lim * q.bmd;
-    up[k] = u.v;
-    dpp[k] = u.d[0];
-    dpm[k] = u.d[1];
-    dnu[k] = u.d[2];
+    for (int k = 0; k < kDim; ++k) {
+      const double* Wk = W + (size_t)k * fp;
+      const double Up = bp0 * Wk[ia] + bp1 * Wk[ib];
+      pp[k] = (Up - w[k]) * ihp;
+      const double Um = bm0 * Wk[ic] + bm1 * Wk[id];
+      const double pm = (-Um + w[k]) * ihm;
+      r[k] = pm / pp[k];
+    }
+    const D3 ec = plane3(G.ec, PS, s);
+    const double ecn = G.ecn[s];
+    const D3 en = plane3(G.en, PS, s);
+    D3 vel = cross3(ec, d3(w[1], w[2], w[3]));
+    vel = scal(vel, 1.0 / ((-w[0] - 0.0) * ecn));
+    const double nu_plus = (c + dot3(vel, en)) * dt * G.arc_a[s];
+    const double eta_p = G.eta[s];
+    const Dual<2> nud = Dual<2>::seed(nu_plus, 1);
+    const Dual<2> sb_scale = G.eta[PS + s] / (twoN * nud);
+    const Dual<2> to_scale = (1 + nud) / 3;
+    double up[kDim];
+#pragma unroll
+    for (int k = 0; k < kDim; ++k) {
+      const Dual<2> lim = limiter_field(Dual<2>::seed(r[k], 0), eta_p, sb_scale, to_scale);
+      if (k == 0 || k == 4)
+        up[k] = w[k] + 0.0 + pp[k] * lim.v * bmd;
+      else
+        up[k] = w[k] + pp[k] * lim.v * bmd;
+      const double dpp = bmd * ((lim.d[0] != 0.0) ? lim.v - lim.d[0] * r[k] : lim.v);
+      LJ[(size_t)(3 * k) * PS + s] = dpp;
+      LJ[(size_t)(3 * k + 1) * PS + s] = bmd * lim.d[0];
+      LJ[(size_t)(3 * k + 2) * PS + s] = pp[k] * bmd * lim.d[1];
+    }
+    LJ[(size_t)15 * PS + s] = up[4];
+    up[4] = energy_at_edge(up, ec, gam);
+#pragma unroll
+    for (int k = 0; k < kDim; ++k) uplus[(size_t)k * PS + s] = up[k];
   }
-  // energy at the edge centre from the limited (Sigma, l, Pi)
-  Dual<5> ud[kDim];
-#pragma unroll
-  for (int k = 0; k < kDim; ++k) ud[k] = Dual<5>::seed(up[k], k);
-  const Dual<5> E = energy_at_edge(ud, q.ec, gam);
-  double preb[kDim];
-#pragma unroll
-  for (int k = 0; k < 4; ++k) preb[k] = upb[k] + upb[4] * E.d[k];
-  preb[4] = upb[4] * E.d[4];
-  double nub = 0.0;
-#pragma unroll
-  for (int k = 0; k < kDim; ++k) {
-    const double ppb = preb[k] * dpp[k];
-    const double pmb = preb[k] * dpm[k];
-    nub += preb[k] * dnu[k];
-    Upb[k] = ppb * ihp;
-    Umb[k] = -pmb * ihm;
-    wb[k] += preb[k] - ppb * ihp + pmb * ihm;
-  }
-#pragma unroll
-  for (int k = 0; k < kDim; ++k) wb[k] += nub * nu5.d[k];
 }
 
 // Sound speed of a face as a Dual<5> over its (Sigma, l, Pi).
@@ -499,51 +500,58 @@ SPLASH_HD Dual<5> face_sound_speed(const double* w, double gam) {
   return sqrt(gam * (w4 + 0.0) / (w0 + 0.0));
 }
 
-// Reverse of recon_face (step_body_fp64.cuh) for face f.  W holds the
-// primal (Sigma, l, Pi) planes; upb_at(k, s) returns the adjoint of
+// Reverse of recon_face_tape for face f.  W holds the primal (Sigma, l, Pi)
+// planes, uplus and LJ the slot's tape; upb_at(k, s) returns the adjoint of
 // uplus[k * PS + s].  Writes the adjoints of the slot's stencil
 // interpolants to PU (planes 0..4: Up, 5..9: Um, each PS long) and adds the
 // face's own contribution to wb.  The interpolants' adjoints reach the
 // stencil faces through PU times the betas (scattered by the caller).
 template <class UpbFn>
-SPLASH_HD void recon_face_rev(const DevGeom& G, const PhysParams& P, double dt, const double* W, UpbFn upb_at,
-                              double* PU, double* wb, int f) {
+SPLASH_HD void recon_face_rev(const DevGeom& G, const PhysParams& P, double dt, const double* W,
+                              const double* uplus, const double* LJ, UpbFn upb_at, double* PU, double* wb, int f) {
   const int fp = G.fpad;
   const int PS = G.max_slots * fp;
   double w[kDim];
 #pragma unroll
   for (int k = 0; k < kDim; ++k) w[k] = W[(size_t)k * fp + f];
   const int n = G.nslots[f];
-  const double twoN = (double)(2 * n);
   const Dual<5> c = face_sound_speed(w, P.gam);
+  Dual<5> wd[kDim];
+#pragma unroll
+  for (int k = 0; k < kDim; ++k) wd[k] = Dual<5>::seed(w[k], k);
   for (int j = 0; j < n; ++j) {
     const int s = j * fp + f;
-    const int ia = G.sten[s], ib = G.sten[PS + s], ic = G.sten[2 * PS + s], id = G.sten[3 * PS + s];
-    const double bp0 = G.beta[s], bp1 = G.beta[PS + s], bm0 = G.beta[2 * PS + s], bm1 = G.beta[3 * PS + s];
-    double Up[kDim], Um[kDim], upb[kDim], Upb[kDim], Umb[kDim];
+    const D3 ec = plane3(G.ec, PS, s);
+    const D3 en = plane3(G.en, PS, s);
+    // energy at the edge centre from the limited (Sigma, l, Pi)
+    Dual<5> ud[kDim];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) ud[k] = Dual<5>::seed(uplus[(size_t)k * PS + s], k);
+    ud[4] = Dual<5>::seed(LJ[(size_t)15 * PS + s], 4);
+    const Dual<5> E = energy_at_edge(ud, ec, P.gam);
+    double upb[kDim], preb[kDim];
+#pragma unroll
+    for (int k = 0; k < kDim; ++k) upb[k] = upb_at(k, s);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) preb[k] = upb[k] + upb[4] * E.d[k];
+    preb[4] = upb[4] * E.d[4];
+    // Courant factor as a function of w
+    V3<Dual<5>> vel = cross3(ec, v3(wd[1], wd[2], wd[3]));
+    vel = scal(vel, 1.0 / ((-wd[0] - 0.0) * G.ecn[s]));
+    const Dual<5> nu5 = (c + dot3(vel, en)) * dt * G.arc_a[s];
+    const double ihp = 1.0 / G.hpm[s], ihm = 1.0 / G.hpm[PS + s];
+    double nub = 0.0;
 #pragma unroll
     for (int k = 0; k < kDim; ++k) {
-      const double* Wk = W + (size_t)k * fp;
-      Up[k] = bp0 * Wk[ia] + bp1 * Wk[ib];
-      Um[k] = bm0 * Wk[ic] + bm1 * Wk[id];
-      upb[k] = upb_at(k, s);
+      const double ppb = preb[k] * LJ[(size_t)(3 * k) * PS + s];
+      const double pmb = preb[k] * LJ[(size_t)(3 * k + 1) * PS + s];
+      nub += preb[k] * LJ[(size_t)(3 * k + 2) * PS + s];
+      PU[(size_t)k * PS + s] = ppb * ihp;
+      PU[(size_t)(kDim + k) * PS + s] = -pmb * ihm;
+      wb[k] += preb[k] - ppb * ihp + pmb * ihm;
     }
-    SlotRecon q;
-    q.ec = plane3(G.ec, PS, s);
-    q.en = plane3(G.en, PS, s);
-    q.ecn = G.ecn[s];
-    q.arc_a = G.arc_a[s];
-    q.eta_p = G.eta[s];
-    q.eta_m = G.eta[PS + s];
-    q.hp = G.hpm[s];
-    q.hm = G.hpm[PS + s];
-    q.bmd = G.bm[s];
-    recon_slot_rev(w, Up, Um, c, q, twoN, dt, P.gam, upb, Upb, Umb, wb);
 #pragma unroll
-    for (int k = 0; k < kDim; ++k) {
-      PU[(size_t)k * PS + s] = Upb[k];
-      PU[(size_t)(kDim + k) * PS + s] = Umb[k];
-    }
+    for (int k = 0; k < kDim; ++k) wb[k] += nub * nu5.d[k];
   }
 }
 

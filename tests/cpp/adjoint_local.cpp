@@ -2,7 +2,8 @@
 // (adjoint_rev.cuh), for CPU checks of the hand-written adjoints:
 //   * full Jacobians of the Riemann fluxes, forward duals vs reverse sweep;
 //   * the reconstruction of one face, tangent-linear (recon_face on
-//     Dual<1>) vs reverse (recon_face_rev + the beta scatter) dot products;
+//     Dual<1>) vs reverse (recon_face_tape, recon_face_rev and the beta
+//     scatter) dot products; the taped edge states equal recon_face's;
 //   * source term and pressure conversion, reverse vs plain evaluations
 //     (the test takes central finite differences of the latter).
 // Compiled by the test with g++ -ffp-contract=off (no FMA contraction, as
@@ -126,13 +127,22 @@ int adj_recon_dot(int n, int nf, const int* sten, const double* beta, const doub
       uplus[k * n + j] = upv[s];
       if (std::memcmp(&up[s], &upv[s], sizeof(double)) != 0) mismatch = 1;
     }
+  // the recomputation's tape: edge states bit-identical to recon_face
+  std::vector<double> upt((size_t)kDim * PS, 0.0), LJ((size_t)rev::kTapePlanes * PS, 0.0);
+  rev::recon_face_tape(G, P, dt, Wv.data(), upt.data(), LJ.data(), 0);
+  for (int k = 0; k < kDim; ++k)
+    for (int j = 0; j < n; ++j) {
+      const size_t s = (size_t)k * PS + (size_t)j * fp;
+      if (std::memcmp(&upt[s], &upv[s], sizeof(double)) != 0) mismatch |= 2;
+    }
   // reverse
   std::vector<double> UPB((size_t)kDim * PS, 0.0), PU((size_t)2 * kDim * PS, 0.0), Wb((size_t)kDim * fp, 0.0);
   for (int k = 0; k < kDim; ++k)
     for (int j = 0; j < n; ++j) UPB[(size_t)k * PS + (size_t)j * fp] = upb[k * n + j];
   double wb[kDim] = {0, 0, 0, 0, 0};
   rev::recon_face_rev(
-      G, P, dt, Wv.data(), [&](int k, int s) { return UPB[(size_t)k * PS + s]; }, PU.data(), wb, 0);
+      G, P, dt, Wv.data(), upt.data(), LJ.data(), [&](int k, int s) { return UPB[(size_t)k * PS + s]; }, PU.data(),
+      wb, 0);
   for (int k = 0; k < kDim; ++k) Wb[(size_t)k * fp] += wb[k];
   for (int j = 0; j < n; ++j) {
     const size_t s = (size_t)j * fp;
