@@ -37,7 +37,7 @@ namespace {
 using namespace splash::f64;
 using D1 = Dual<1>;
 static_assert(kTapeJ == rev::kTapePlanes, "tape plane count");
-constexpr int kBlock = 128;    // TLM kernels: must match the FP64 step (partials per block)
+constexpr int kBlock = 64;     // TLM kernels: must match the FP64 step (partials per block)
 constexpr int kRevBlock = 64;  // recomputation and reverse kernels (FP64-bound, register-heavy:
                                // small blocks spread the faces evenly over the SMs)
 

@@ -28,7 +28,7 @@ namespace splash {
 namespace f64 {
 namespace {
 
-constexpr int kBlock = 128;
+constexpr int kBlock = 64;  // FP64-pipe bound, register-heavy: small blocks balance the SMs
 
 // ---------------------------------------------------------------------
 // W = (Sigma, l, Pi) of the conserved state and the partials of it
