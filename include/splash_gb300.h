@@ -64,9 +64,10 @@ typedef enum splash_mesh_kind {
 } splash_mesh_kind;
 
 typedef enum splash_solver_kind {
-  SPLASH_SOLVER_HLLE_P = 1,  /* MUSCL_HLLE_p   Riemann_solvers/HLLE_p.hpp:6-59 */
-  SPLASH_SOLVER_HLLC = 2,    /* MUSCL_HLLC     Riemann_solvers/HLLC.hpp:6-122 */
-  SPLASH_SOLVER_HLLCPLUS = 3 /* MUSCL_HLLCplus Riemann_solvers/HLLCplus.hpp:6-177 */
+  SPLASH_SOLVER_HLLE_P = 1,   /* MUSCL_HLLE_p   Riemann_solvers/HLLE_p.hpp:6-59 */
+  SPLASH_SOLVER_HLLC = 2,     /* MUSCL_HLLC     Riemann_solvers/HLLC.hpp:6-122 */
+  SPLASH_SOLVER_HLLCPLUS = 3, /* MUSCL_HLLCplus Riemann_solvers/HLLCplus.hpp:6-177 */
+  SPLASH_SOLVER_HLLE = 4      /* MUSCL_HLLE     Riemann_solvers/HLLE.hpp:6-62, isothermal, dim 4 */
 } splash_solver_kind;
 
 typedef enum splash_precision {
@@ -116,10 +117,18 @@ SPLASH_API const char* splash_version(void);
  * geometry/MUSCL_geometry.hpp:43-225).  `U_in` is [n_faces][dim] in the
  * reference face order; `params` replaces the parameters.json read.
  * `device` selects the CUDA device; `threads` sizes host-side helpers
- * (geometry precompute) only, 0 = all cores.  dim != 5 is rejected with
- * SPLASH_E_UNSUPPORTED: the reference prints "check dim", latches
- * stop_check and then indexes past the state vector
- * (physics/adiabatic.hpp:26-30, Riemann_solvers/HLLC.hpp:208). */
+ * (geometry precompute) only, 0 = all cores.  The adiabatic solvers need
+ * dim 5 and the isothermal SPLASH_SOLVER_HLLE (MUSCL_HLLE, HLLE.hpp:11-13,
+ * physics/isothermal.hpp:13-40) dim 4; other combinations are rejected with
+ * SPLASH_E_UNSUPPORTED (the reference prints "check dim", latches stop_check
+ * and, for the adiabatic solvers, then indexes past the state vector,
+ * physics/adiabatic.hpp:26-30, Riemann_solvers/HLLC.hpp:208).  The
+ * isothermal solver ignores omega_ns, accretion_on and params (its
+ * constructor takes none of them) and runs in FP64.  Its reference path reads
+ * and writes a fifth state field and an uninitialised limiter variable
+ * (MUSCL_base.hpp:203, 324, 368-370; isothermal.hpp:272, 307); the GPU path
+ * is the defined form: no fifth field, CFL sound speed a = 1, etha_minus =
+ * H_minus / BM_dist. */
 SPLASH_API int splash_create(const splash_mesh_desc* mesh, const double* U_in, int dim, double gam,
                   double omega_ns, int accretion_on, const splash_params* params,
                   int solver_kind, int precision, int device, int threads,

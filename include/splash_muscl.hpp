@@ -206,6 +206,30 @@ class Solver {
     for (const char* f : {"results/rho.dat", "results/curl.dat", "results/p.dat", "results/omega.dat",
                           "results/Lx.dat", "results/Ly.dat", "results/Lz.dat"})
       std::ofstream(f, std::ios::out | std::ios::trunc);
+    create(U_in, dim, gam, omega_ns, accretion_on, threads, solver_kind, precision, device, par);
+  }
+  Solver(const Solver&) = delete;
+  Solver& operator=(const Solver&) = delete;
+  virtual ~Solver() { splash_destroy(h_); }
+
+ protected:
+  // The isothermal constructor (physics/isothermal.hpp:13-40): no
+  // parameters.json, four output files truncated.
+  struct IsothermalTag {};
+  Solver(const Mesh& mesh, const std::vector<std::vector<double>>& U_in, int dim, double gam, size_t threads,
+         int precision, int device, IsothermalTag)
+      : mesh_(mesh), dim_(dim) {
+    for (const char* f : {"results/rho.dat", "results/curl.dat", "results/p.dat", "results/omega.dat"})
+      std::ofstream(f, std::ios::out | std::ios::trunc);
+    splash_params par{};
+    par.acc_width = 0.1;
+    create(U_in, dim, gam, 0.0, false, threads, SPLASH_SOLVER_HLLE, precision, device, par);
+  }
+
+ private:
+  void create(const std::vector<std::vector<double>>& U_in, int dim, double gam, double omega_ns,
+              bool accretion_on, size_t threads, int solver_kind, int precision, int device,
+              const splash_params& par) {
     std::vector<double> flat;
     flat.reserve(U_in.size() * (size_t)dim);
     for (const auto& row : U_in) {
@@ -217,10 +241,8 @@ class Solver {
                         precision, device, (int)threads, &h_),
           "splash_create");
   }
-  Solver(const Solver&) = delete;
-  Solver& operator=(const Solver&) = delete;
-  virtual ~Solver() { splash_destroy(h_); }
 
+ public:
   void do_step(double dt0) { check(splash_do_step(h_, dt0), "do_step"); }
   double time() {
     double t = 0;
@@ -321,6 +343,15 @@ class Solver {
   splash_solver* h_ = nullptr;
 };
 
+// Riemann_solvers/HLLE.hpp:11-13: the isothermal solver, dim 4 (its
+// writers are write_t_rho, write_t_p, write_t_curl and write_t_omega_z)
+class MUSCL_HLLE : public Solver {
+ public:
+  MUSCL_HLLE(const Mesh& mesh, const std::vector<std::vector<double>>& U_in, int dim, double gam, size_t threads,
+             int precision = SPLASH_PREC_FP64, int device = 0)
+      : Solver(mesh, U_in, dim, gam, threads, precision, device, IsothermalTag{}) {}
+};
+
 // Riemann_solvers/HLLE_p.hpp:11-13
 class MUSCL_HLLE_p : public Solver {
  public:
@@ -367,6 +398,7 @@ using splash::icosphere_hex;
 using splash::quad_sphere;
 }  // namespace pmp
 using json = splash::Json;
+using splash::MUSCL_HLLE;
 using splash::MUSCL_HLLC;
 using splash::MUSCL_HLLCplus;
 using splash::MUSCL_HLLE_p;

@@ -363,6 +363,8 @@ int splash_adjoint_create(splash_solver* base_h, int checkpoint_every, splash_ad
   if (base->precision != SPLASH_PREC_FP64)
     return splash::set_error(SPLASH_E_UNSUPPORTED, "the adjoint differentiates the FP64 step: create the base "
                                                    "solver with SPLASH_PREC_FP64");
+  if (base->dim != splash::kDim)
+    return splash::set_error(SPLASH_E_UNSUPPORTED, "the adjoint differentiates the adiabatic (dim 5) step");
   if (checkpoint_every <= 0) return splash::set_error(SPLASH_E_INVALID, "checkpoint_every must be > 0");
   if (cudaSetDevice(base->device) != cudaSuccess) return splash::set_error(SPLASH_E_CUDA, "cudaSetDevice failed");
   std::unique_ptr<Adjoint> a(new (std::nothrow) Adjoint());

@@ -228,20 +228,20 @@ cudaError_t Solver::launch_step(cudaEvent_t* ev, double dt0) {
 }
 
 int Solver::upload_state(const double* U_ref) {
-  std::memcpy(h_stage, U_ref, (size_t)n_faces * kDim * sizeof(double));
-  SPLASH_CUDA(cudaMemcpyAsync(d_stage, h_stage, (size_t)n_faces * kDim * sizeof(double),
+  std::memcpy(h_stage, U_ref, (size_t)n_faces * dim * sizeof(double));
+  SPLASH_CUDA(cudaMemcpyAsync(d_stage, h_stage, (size_t)n_faces * dim * sizeof(double),
                               cudaMemcpyHostToDevice, stream));
-  SPLASH_CUDA(fp64_scatter_state(d_stage, d_perm, S.U, n_faces, fpad, stream));
+  SPLASH_CUDA(fp64_scatter_state(d_stage, d_perm, S.U, n_faces, fpad, stream, dim));
   SPLASH_CUDA(launch_prepare());
   return SPLASH_OK;
 }
 
 int Solver::download_state(double* U_ref) {
-  SPLASH_CUDA(fp64_gather_state(S.U, d_perm, d_stage, n_faces, fpad, stream));
-  SPLASH_CUDA(cudaMemcpyAsync(h_stage, d_stage, (size_t)n_faces * kDim * sizeof(double),
+  SPLASH_CUDA(fp64_gather_state(S.U, d_perm, d_stage, n_faces, fpad, stream, dim));
+  SPLASH_CUDA(cudaMemcpyAsync(h_stage, d_stage, (size_t)n_faces * dim * sizeof(double),
                               cudaMemcpyDeviceToHost, stream));
   SPLASH_CUDA(cudaStreamSynchronize(stream));
-  std::memcpy(U_ref, h_stage, (size_t)n_faces * kDim * sizeof(double));
+  std::memcpy(U_ref, h_stage, (size_t)n_faces * dim * sizeof(double));
   return SPLASH_OK;
 }
 
@@ -320,13 +320,20 @@ int splash_create(const splash_mesh_desc* mesh, const double* U_in, int dim, dou
   if (!out) return fail(SPLASH_E_INVALID, "out is NULL");
   *out = nullptr;
   if (!mesh || !U_in || !params) return fail(SPLASH_E_INVALID, "mesh, U_in and params must be non-NULL");
-  if (dim != splash::kDim)
+  if (solver_kind < SPLASH_SOLVER_HLLE_P || solver_kind > SPLASH_SOLVER_HLLE)
+    return fail(SPLASH_E_INVALID, "unknown solver kind %d", solver_kind);
+  if (solver_kind == SPLASH_SOLVER_HLLE && dim != 4)
+    return fail(SPLASH_E_UNSUPPORTED,
+                "dim=%d: the isothermal solver needs dim=4 (the reference prints \"check dim\" and "
+                "latches stop_check, physics/isothermal.hpp:18-22)",
+                dim);
+  if (solver_kind != SPLASH_SOLVER_HLLE && dim != splash::kDim)
     return fail(SPLASH_E_UNSUPPORTED,
                 "dim=%d: the adiabatic solvers need dim=5 (the reference latches stop_check and "
                 "then indexes out of bounds, physics/adiabatic.hpp:26-30)",
                 dim);
-  if (solver_kind < SPLASH_SOLVER_HLLE_P || solver_kind > SPLASH_SOLVER_HLLCPLUS)
-    return fail(SPLASH_E_INVALID, "unknown solver kind %d", solver_kind);
+  if (solver_kind == SPLASH_SOLVER_HLLE && precision == SPLASH_PREC_MIXED)
+    return fail(SPLASH_E_UNSUPPORTED, "the isothermal solver runs in FP64 only");
   if (precision != SPLASH_PREC_FP64 && precision != SPLASH_PREC_MIXED)
     return fail(SPLASH_E_INVALID, "unknown precision %d", precision);
   if (precision == SPLASH_PREC_MIXED && !splash::mixed_available())
@@ -339,7 +346,9 @@ int splash_create(const splash_mesh_desc* mesh, const double* U_in, int dim, dou
     splash::MeshArrays arrays = mesh_from_desc(mesh);
     RefGeometry g = splash::build_ref_geometry(arrays, threads);
     s->par = *params;
-    s->accretion_on = accretion_on != 0;
+    s->dim = dim;
+    // the isothermal solver has no source term (physics/isothermal.hpp:199-208)
+    s->accretion_on = accretion_on != 0 && solver_kind != SPLASH_SOLVER_HLLE;
     s->precision = precision;
     s->solver_kind = solver_kind;
     s->device = device;
@@ -399,14 +408,14 @@ int splash_create(const splash_mesh_desc* mesh, const double* U_in, int dim, dou
     S.scal = s->dalloc<double>(splash::kScCount);
     S.err = s->dalloc<unsigned int>(4);
     S.keys = s->dalloc<unsigned long long>(2);
-    s->d_stage = s->dalloc<double>((size_t)s->n_faces * splash::kDim);
+    s->d_stage = s->dalloc<double>((size_t)s->n_faces * dim);
     s->d_perm = s->upload(s->perm);
     SPLASH_CUDA(cudaMemset(S.U, 0, splash::kDim * fp * sizeof(double)));
     SPLASH_CUDA(cudaMemset(S.W0, 0, splash::kDim * fp * sizeof(double)));
     SPLASH_CUDA(cudaMemset(S.W1, 0, splash::kDim * fp * sizeof(double)));
     SPLASH_CUDA(cudaMemset(S.scal, 0, splash::kScCount * sizeof(double)));
     SPLASH_CUDA(cudaMemset(S.err, 0, 4 * sizeof(unsigned int)));
-    SPLASH_CUDA(cudaMallocHost(&s->h_stage, (size_t)s->n_faces * splash::kDim * sizeof(double)));
+    SPLASH_CUDA(cudaMallocHost(&s->h_stage, (size_t)s->n_faces * dim * sizeof(double)));
 
     int rc = s->upload_state(U_in);
     if (rc) return rc;
@@ -557,7 +566,7 @@ int splash_n_faces(splash_solver* h, int* n) {
 int splash_dim(splash_solver* h, int* d) {
   Solver* s = reinterpret_cast<Solver*>(h);
   if (!s || !d) return fail(SPLASH_E_INVALID, "NULL argument");
-  *d = splash::kDim;
+  *d = s->dim;
   return SPLASH_OK;
 }
 
@@ -579,17 +588,17 @@ int splash_set_state(splash_solver* h, const double* U) {
 int splash_diagnostics(splash_solver* h, double out[5]) {
   GET_SOLVER(h);
   if (!out) return fail(SPLASH_E_INVALID, "out is NULL");
-  std::vector<double> U((size_t)s->n_faces * splash::kDim);
+  std::vector<double> U((size_t)s->n_faces * s->dim);
   int rc = s->download_state(U.data());
   if (rc) return rc;
   double m = 0, l1 = 0, l2 = 0, l3 = 0, e = 0;
   for (int i = 0; i < s->n_faces; ++i) {
-    const double* u = &U[(size_t)i * splash::kDim];
+    const double* u = &U[(size_t)i * s->dim];
     m += u[0] * s->wr_area[i];
     l1 += u[1] * s->wr_area[i];
     l2 += u[2] * s->wr_area[i];
     l3 += u[3] * s->wr_area[i];
-    e += u[4] * s->wr_area[i];
+    if (s->dim > 4) e += u[4] * s->wr_area[i];
   }
   out[0] = m;
   out[1] = l1;
@@ -619,12 +628,12 @@ int splash_write_t_rho(splash_solver* h, const char* path) {
   std::ofstream os;
   int rc = open_append(os, path);
   if (rc) return rc;
-  std::vector<double> U((size_t)s->n_faces * splash::kDim);
+  std::vector<double> U((size_t)s->n_faces * s->dim);
   if ((rc = s->download_state(U.data()))) return rc;
   double t;
   if ((rc = splash_time(h, &t))) return rc;
   os << t << "  ";
-  for (int i = 0; i < s->n_faces; ++i) os << U[(size_t)i * splash::kDim] << " ";
+  for (int i = 0; i < s->n_faces; ++i) os << U[(size_t)i * s->dim] << " ";
   os << "\n";
   return SPLASH_OK;
 }
@@ -634,13 +643,17 @@ int splash_write_t_p(splash_solver* h, const char* path) {
   std::ofstream os;
   int rc = open_append(os, path);
   if (rc) return rc;
-  std::vector<double> U((size_t)s->n_faces * splash::kDim);
+  std::vector<double> U((size_t)s->n_faces * s->dim);
   if ((rc = s->download_state(U.data()))) return rc;
   double t;
   if ((rc = splash_time(h, &t))) return rc;
   os << t << "  ";
   for (int i = 0; i < s->n_faces; ++i) {
-    const double* u = &U[(size_t)i * splash::kDim];
+    const double* u = &U[(size_t)i * s->dim];
+    if (s->dim == 4) {  // physics/isothermal.hpp:63-73: a * a * Sigma, a = 1
+      os << 1.0 * 1.0 * u[0] << " ";
+      continue;
+    }
     const V3 fc = at3(s->wr_face_centers, i);
     V3 vel = vcross(vdiv(fc, vnorm(fc)), V3{u[1], u[2], u[3]});
     vel = vdiv(vel, -u[0]);
@@ -656,7 +669,7 @@ int splash_write_t_curl(splash_solver* h, const char* path) {
   std::ofstream os;
   int rc = open_append(os, path);
   if (rc) return rc;
-  std::vector<double> U((size_t)s->n_faces * splash::kDim);
+  std::vector<double> U((size_t)s->n_faces * s->dim);
   if ((rc = s->download_state(U.data()))) return rc;
   // U_plus of the last stage, slot planes -> host
   const size_t PS = (size_t)s->max_slots * s->fpad;
@@ -683,7 +696,7 @@ int splash_write_t_curl(splash_solver* h, const char* path) {
       V3 ec = vdiv(vadd(at3(s->wr_vertices, va), at3(s->wr_vertices, vb)), 2.);
       ec = vdiv(ec, vnorm(ec));
       V3 vel = vcross(ec, l);
-      vel = vdiv(vel, -U[(size_t)r * splash::kDim]);
+      vel = vdiv(vel, -U[(size_t)r * s->dim]);
       const V3 rr = vsub(at3(s->wr_vertices, va), at3(s->wr_vertices, vb));
       vort += vdot(vel, rr);
     }
@@ -695,7 +708,8 @@ int splash_write_t_curl(splash_solver* h, const char* path) {
 
 int splash_write_t_L(splash_solver* h, const char* px, const char* py, const char* pz) {
   GET_SOLVER(h);
-  std::vector<double> U((size_t)s->n_faces * splash::kDim);
+  if (s->dim == 4) return fail(SPLASH_E_UNSUPPORTED, "the isothermal solver has no such member (physics/isothermal.hpp)");
+  std::vector<double> U((size_t)s->n_faces * s->dim);
   int rc;
   if ((rc = s->download_state(U.data()))) return rc;
   double t;
@@ -705,7 +719,7 @@ int splash_write_t_L(splash_solver* h, const char* px, const char* py, const cha
     std::ofstream os;
     if ((rc = open_append(os, paths[k]))) return rc;
     os << t << "  ";
-    for (int i = 0; i < s->n_faces; ++i) os << U[(size_t)i * splash::kDim + k + 1] << " ";
+    for (int i = 0; i < s->n_faces; ++i) os << U[(size_t)i * s->dim + k + 1] << " ";
     os << "\n";
   }
   return SPLASH_OK;
@@ -716,18 +730,22 @@ int splash_write_t_omega_z(splash_solver* h, const char* path) {
   std::ofstream os;
   int rc = open_append(os, path);
   if (rc) return rc;
-  std::vector<double> U((size_t)s->n_faces * splash::kDim);
+  std::vector<double> U((size_t)s->n_faces * s->dim);
   if ((rc = s->download_state(U.data()))) return rc;
   double t;
   if ((rc = splash_time(h, &t))) return rc;
   os << t << "  ";
   for (int i = 0; i < s->n_faces; ++i) {
-    const double* u = &U[(size_t)i * splash::kDim];
+    const double* u = &U[(size_t)i * s->dim];
     const V3 fc = at3(s->wr_face_centers, i);
     const double theta = std::acos(fc.z / vnorm(fc));
     const V3 fcn = vdiv(fc, vnorm(fc));
     V3 vel = vcross(fcn, V3{u[1], u[2], u[3]});
     vel = vdiv(vel, -u[0]);
+    if (s->dim == 4) {  // physics/isothermal.hpp:112-133: z of (face centre x v)
+      os << vcross(fc, vel).z << " ";
+      continue;
+    }
     const V3 rxv = vcross(fcn, vel);
     double om_z = rxv.z / (std::sin(theta) * std::sin(theta));
     if (std::isnan(om_z) || std::isinf(om_z) || std::abs(om_z) > 1e4) om_z = 0;
@@ -739,8 +757,9 @@ int splash_write_t_omega_z(splash_solver* h, const char* path) {
 
 int splash_get_light_curves(splash_solver* h, double out[4]) {
   GET_SOLVER(h);
+  if (s->dim == 4) return fail(SPLASH_E_UNSUPPORTED, "the isothermal solver has no such member (physics/isothermal.hpp)");
   if (!out) return fail(SPLASH_E_INVALID, "out is NULL");
-  std::vector<double> U((size_t)s->n_faces * splash::kDim);
+  std::vector<double> U((size_t)s->n_faces * s->dim);
   int rc;
   if ((rc = s->download_state(U.data()))) return rc;
   // observers of physics/adiabatic.hpp:233-245
@@ -751,7 +770,7 @@ int splash_get_light_curves(splash_solver* h, double out[4]) {
   const V3 o180{0, 0, -9.4 * 3 * 1e19 / 15000};
   double f0 = 0, f45 = 0, f90 = 0, f180 = 0;
   for (int i = 0; i < s->n_faces; ++i) {
-    const double* u = &U[(size_t)i * splash::kDim];
+    const double* u = &U[(size_t)i * s->dim];
     const V3 fc = at3(s->wr_face_centers, i);
     const double phi_fc = std::atan2(fc.y / vnorm(fc), fc.x / vnorm(fc));
     const double theta_fc = std::acos(fc.z / vnorm(fc));
@@ -775,14 +794,15 @@ int splash_get_light_curves(splash_solver* h, double out[4]) {
 
 int splash_write_final_state(splash_solver* h, const char* path) {
   GET_SOLVER(h);
+  if (s->dim == 4) return fail(SPLASH_E_UNSUPPORTED, "the isothermal solver has no such member (physics/isothermal.hpp)");
   if (!path) return fail(SPLASH_E_INVALID, "path is NULL");
-  std::vector<double> U((size_t)s->n_faces * splash::kDim);
+  std::vector<double> U((size_t)s->n_faces * s->dim);
   int rc;
   if ((rc = s->download_state(U.data()))) return rc;
   std::ofstream os(path, std::ios::out | std::ios::trunc);
   if (!os) return fail(SPLASH_E_INVALID, "cannot open %s", path);
   for (int i = 0; i < s->n_faces; ++i) {
-    for (int k = 0; k < splash::kDim; ++k) os << U[(size_t)i * splash::kDim + k] << " ";
+    for (int k = 0; k < s->dim; ++k) os << U[(size_t)i * s->dim + k] << " ";
     os << "\n";
   }
   return SPLASH_OK;

@@ -20,10 +20,12 @@ cudaError_t fp64_dt(const DevState& S, const PhysParams& P, int n_faces, cudaStr
 // an event is recorded before the first and after every launch.
 cudaError_t fp64_step(const DevGeom& G, const DevState& S, const PhysParams& P, cudaStream_t st,
                       cudaEvent_t* ev = nullptr);
+// reference-order [n_faces][dim] <-> internal planes (dim 5, or 4 for the
+// isothermal solver, whose fifth plane is zero)
 cudaError_t fp64_scatter_state(const double* aos, const int* perm, double* U, int n_faces, int fpad,
-                               cudaStream_t st);
+                               cudaStream_t st, int dim = kDim);
 cudaError_t fp64_gather_state(const double* U, const int* perm, double* aos, int n_faces, int fpad,
-                              cudaStream_t st);
+                              cudaStream_t st, int dim = kDim);
 
 // ---- FP32/FP64 mixed path (step_mixed.cu) ----
 cudaError_t mixed_prepare(const DevGeomMixed& G, const DevState& S, const PhysParams& P,

@@ -36,8 +36,10 @@ struct PhysParams {
   double round_diff;     // arc/chord of face 0 edge (1,2)
   int accretion_on;
   int friction_on;
-  int solver;            // 1 HLLE_p, 2 HLLC, 3 HLLC+
+  int solver;            // 1 HLLE_p, 2 HLLC, 3 HLLC+, 4 HLLE (isothermal)
 };
+
+constexpr int kSolverIsoHLLE = 4;  // the isothermal solver (4 state fields)
 
 // FP64 geometry, slot planes of length max_slots * fpad unless noted.
 struct DevGeom {

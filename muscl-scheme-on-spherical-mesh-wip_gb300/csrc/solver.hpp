@@ -26,6 +26,7 @@ struct Solver {
   bool accretion_on = false;
   int precision = SPLASH_PREC_FP64;
   int solver_kind = SPLASH_SOLVER_HLLCPLUS;
+  int dim = 5;  // state fields: 5 adiabatic, 4 isothermal (MUSCL_HLLE)
   int device = -1;
   double area_coeff = 0.0;
   double total_mass = 0.0;

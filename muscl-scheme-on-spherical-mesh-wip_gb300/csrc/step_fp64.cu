@@ -21,6 +21,7 @@
 
 #include "kernels.hpp"
 #include "physics_fp64.cuh"
+#include "physics_iso.cuh"
 #include "step_body_fp64.cuh"
 #include "reduce.cuh"
 
@@ -136,24 +137,136 @@ __global__ void __launch_bounds__(kBlock) flux_update_kernel(DevGeom G, DevState
   if (STAGE == 2) red::block_partials<kBlock>(vmax, dmin, sums, S.partial + (size_t)blockIdx.x * kPartialStride);
 }
 
+// ---- isothermal solver (MUSCL_HLLE, 4 fields; planes 0..3 of U/W/U+) ----
+// W of a 4-field state is the state itself (find_U_edges subtracts the
+// zero profile rho_an from field 0, MUSCL_base.hpp:366-371).
+__global__ void __launch_bounds__(kBlock) iso_prepare_kernel(DevGeom G, DevState S) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  double vmax = 0.0, dmin = 1e20, sums[5] = {0, 0, 0, 0, 0};
+  if (f < G.n_faces) {
+    double u[kDim];
+#pragma unroll
+    for (int k = 0; k < iso::kIsoDim; ++k) u[k] = S.U[k * G.fpad + f];
+    u[4] = 0.0;
+    S.W0[f] = u[0] - 0.0;
+#pragma unroll
+    for (int k = 1; k < iso::kIsoDim; ++k) S.W0[k * G.fpad + f] = u[k];
+    iso::dt_candidates(u, plane3(G.fcn, G.fpad, f), G.area[f], vmax, dmin, sums);
+  }
+  red::block_partials<kBlock>(vmax, dmin, sums, S.partial + (size_t)blockIdx.x * kPartialStride);
+}
+
+// find_U_edges with the isothermal limiter (MUSCL_base.hpp:361-434,
+// physics/isothermal.hpp:269-320) for every slot of one face
+__global__ void __launch_bounds__(kBlock) iso_reconstruct_kernel(DevGeom G, const double* __restrict__ W,
+                                                                 double* __restrict__ uplus,
+                                                                 const double* __restrict__ sc) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= G.n_faces) return;
+  const int fp = G.fpad;
+  const int PS = G.max_slots * fp;
+  const double dt = sc[kScDt];
+  double w[iso::kIsoDim];
+#pragma unroll
+  for (int k = 0; k < iso::kIsoDim; ++k) w[k] = W[k * fp + f];
+  const int n = G.nslots[f];
+  const double twoN = (double)(2 * n);
+  for (int j = 0; j < n; ++j) {
+    const int s = j * fp + f;
+    const int ia = G.sten[s], ib = G.sten[PS + s], ic = G.sten[2 * PS + s], id = G.sten[3 * PS + s];
+    const double bp0 = G.beta[s], bp1 = G.beta[PS + s], bm0 = G.beta[2 * PS + s], bm1 = G.beta[3 * PS + s];
+    const double hp = G.hpm[s], hm = G.hpm[PS + s], bmd = G.bm[s];
+    const D3 ec = plane3(G.ec, PS, s);
+    const D3 en = plane3(G.en, PS, s);
+    const double nu_plus = iso::courant(w, ec, en, dt, G.arc_a[s]);
+    const double eta = G.eta[PS + s];
+#pragma unroll
+    for (int k = 0; k < iso::kIsoDim; ++k) {
+      const double* Wk = W + k * fp;
+      const double Up = bp0 * Wk[ia] + bp1 * Wk[ib];
+      const double pp = (Up - w[k]) / hp;
+      const double Um = bm0 * Wk[ic] + bm1 * Wk[id];
+      const double pm = (-Um + w[k]) / hm;
+      const double lim = iso::limiter_field(pm / pp, eta, twoN, nu_plus);
+      uplus[k * PS + s] = (k == 0) ? w[k] + 0.0 + pp * lim * bmd : w[k] + pp * lim * bmd;
+    }
+  }
+}
+
+// find_flux_var + res2d + the RK combine (zero source) for one face;
+// stage 1: dt/2, writes W1; stage 2: dt, writes U, W0 and the partials
+template <int STAGE>
+__global__ void __launch_bounds__(kBlock) iso_flux_update_kernel(DevGeom G, DevState S, PhysParams P) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  double vmax = 0.0, dmin = 1e20, sums[5] = {0, 0, 0, 0, 0};
+  if (f < G.n_faces) {
+    const int fp = G.fpad;
+    const int PS = G.max_slots * fp;
+    const double dt = S.scal[kScDt];
+    const double dt_here = (STAGE == 1) ? dt / 2 : dt;
+    const double area = G.area[f];
+    double acc[iso::kIsoDim];
+#pragma unroll
+    for (int k = 0; k < iso::kIsoDim; ++k) acc[k] = dt_here * 0.0;
+    const double rd_dt = P.round_diff * dt_here;
+    const int n = G.nslots[f];
+    unsigned bits = 0;
+    for (int j = 0; j < n; ++j) {
+      const int s = j * fp + f;
+      const int rv = G.rev[s];
+      double uL[iso::kIsoDim], uR[iso::kIsoDim], F[iso::kIsoDim];
+#pragma unroll
+      for (int k = 0; k < iso::kIsoDim; ++k) {
+        uL[k] = S.uplus[k * PS + s];
+        uR[k] = S.uplus[k * PS + rv];
+      }
+      bits |= iso::flux_star(uL, uR, plane3(G.ec, PS, s), G.ecn[s], plane3(G.en, PS, s), F);
+      const double coef = rd_dt * G.chord[s] / area;
+#pragma unroll
+      for (int k = 0; k < iso::kIsoDim; ++k) {
+        if (isnan(F[k])) bits |= 1u;
+        acc[k] -= coef * F[k];
+      }
+    }
+    if (bits) atomicOr(S.err, bits);
+    double u[kDim];
+#pragma unroll
+    for (int k = 0; k < iso::kIsoDim; ++k) u[k] = acc[k] + S.U[k * fp + f];
+    u[4] = 0.0;
+    if (u[0] < 1e-8) u[0] = 1e-8;
+    double* Wout = (STAGE == 1) ? S.W1 : S.W0;
+    Wout[f] = u[0] - 0.0;
+#pragma unroll
+    for (int k = 1; k < iso::kIsoDim; ++k) Wout[k * fp + f] = u[k];
+    if (STAGE == 2) {
+#pragma unroll
+      for (int k = 0; k < iso::kIsoDim; ++k) S.U[k * fp + f] = u[k];
+      iso::dt_candidates(u, plane3(G.fcn, fp, f), area, vmax, dmin, sums);
+    }
+  }
+  if (STAGE == 2) red::block_partials<kBlock>(vmax, dmin, sums, S.partial + (size_t)blockIdx.x * kPartialStride);
+}
+
 __global__ void set_scalar_kernel(double* dst, double v) { *dst = v; }
 
 // reference order [F][dim] <-> internal planes
+// (dim = 4: the fifth plane is zero)
 __global__ void scatter_state_kernel(const double* __restrict__ aos, const int* __restrict__ perm,
-                                     double* __restrict__ U, int n_faces, int fpad) {
+                                     double* __restrict__ U, int n_faces, int fpad, int dim) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_faces) return;
   const int r = perm[i];
 #pragma unroll
-  for (int k = 0; k < kDim; ++k) U[k * fpad + i] = aos[(size_t)r * kDim + k];
+  for (int k = 0; k < kDim; ++k) U[k * fpad + i] = (k < dim) ? aos[(size_t)r * dim + k] : 0.0;
 }
 __global__ void gather_state_kernel(const double* __restrict__ U, const int* __restrict__ perm,
-                                    double* __restrict__ aos, int n_faces, int fpad) {
+                                    double* __restrict__ aos, int n_faces, int fpad, int dim) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_faces) return;
   const int r = perm[i];
 #pragma unroll
-  for (int k = 0; k < kDim; ++k) aos[(size_t)r * kDim + k] = U[k * fpad + i];
+  for (int k = 0; k < kDim; ++k)
+    if (k < dim) aos[(size_t)r * dim + k] = U[k * fpad + i];
 }
 
 inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
@@ -166,7 +279,10 @@ int fp64_partial_blocks(int n_faces) { return f64::blocks_for(n_faces); }
 
 cudaError_t fp64_prepare(const DevGeom& G, const DevState& S, const PhysParams& P,
                          cudaStream_t st) {
-  f64::prepare_kernel<<<f64::blocks_for(G.n_faces), f64::kBlock, 0, st>>>(G, S, P);
+  if (P.solver == kSolverIsoHLLE)
+    f64::iso_prepare_kernel<<<f64::blocks_for(G.n_faces), f64::kBlock, 0, st>>>(G, S);
+  else
+    f64::prepare_kernel<<<f64::blocks_for(G.n_faces), f64::kBlock, 0, st>>>(G, S, P);
   return cudaGetLastError();
 }
 
@@ -186,6 +302,17 @@ cudaError_t fp64_step(const DevGeom& G, const DevState& S, const PhysParams& P, 
   if (ev) cudaEventRecord(ev[0], st);
   f64::dt_kernel<<<1, 256, 0, st>>>(S, P, nb);
   if (ev) cudaEventRecord(ev[1], st);
+  if (P.solver == kSolverIsoHLLE) {
+    f64::iso_reconstruct_kernel<<<nb, f64::kBlock, 0, st>>>(G, S.W0, S.uplus, S.scal);
+    if (ev) cudaEventRecord(ev[2], st);
+    f64::iso_flux_update_kernel<1><<<nb, f64::kBlock, 0, st>>>(G, S, P);
+    if (ev) cudaEventRecord(ev[3], st);
+    f64::iso_reconstruct_kernel<<<nb, f64::kBlock, 0, st>>>(G, S.W1, S.uplus, S.scal);
+    if (ev) cudaEventRecord(ev[4], st);
+    f64::iso_flux_update_kernel<2><<<nb, f64::kBlock, 0, st>>>(G, S, P);
+    if (ev) cudaEventRecord(ev[5], st);
+    return cudaGetLastError();
+  }
   f64::reconstruct_kernel<<<nb, f64::kBlock, 0, st>>>(G, S.W0, S.uplus, S.scal, P);
   if (ev) cudaEventRecord(ev[2], st);
   f64::flux_update_kernel<1><<<nb, f64::kBlock, 0, st>>>(G, S, P);
@@ -198,14 +325,14 @@ cudaError_t fp64_step(const DevGeom& G, const DevState& S, const PhysParams& P, 
 }
 
 cudaError_t fp64_scatter_state(const double* aos, const int* perm, double* U, int n_faces,
-                               int fpad, cudaStream_t st) {
-  f64::scatter_state_kernel<<<f64::blocks_for(n_faces), f64::kBlock, 0, st>>>(aos, perm, U, n_faces, fpad);
+                               int fpad, cudaStream_t st, int dim) {
+  f64::scatter_state_kernel<<<f64::blocks_for(n_faces), f64::kBlock, 0, st>>>(aos, perm, U, n_faces, fpad, dim);
   return cudaGetLastError();
 }
 
 cudaError_t fp64_gather_state(const double* U, const int* perm, double* aos, int n_faces,
-                              int fpad, cudaStream_t st) {
-  f64::gather_state_kernel<<<f64::blocks_for(n_faces), f64::kBlock, 0, st>>>(U, perm, aos, n_faces, fpad);
+                              int fpad, cudaStream_t st, int dim) {
+  f64::gather_state_kernel<<<f64::blocks_for(n_faces), f64::kBlock, 0, st>>>(U, perm, aos, n_faces, fpad, dim);
   return cudaGetLastError();
 }
 

@@ -31,6 +31,7 @@ MESH_ICOSPHERE = 2
 SOLVER_HLLE_P = 1
 SOLVER_HLLC = 2
 SOLVER_HLLCPLUS = 3
+SOLVER_HLLE = 4  # isothermal, dim 4
 
 PREC_FP64 = 0
 PREC_MIXED = 1
@@ -443,6 +444,16 @@ class _Named(Solver):
                  device: int = 0):
         super().__init__(mesh, U_in, dim, gam, omega_ns, accretion_on, params=params,
                          solver=self._KIND, precision=precision, device=device, threads=threads)
+
+
+class MUSCL_HLLE(Solver):
+    """Riemann_solvers/HLLE.hpp:11-13 (mesh, U_in, dim, gam, threads): the
+    isothermal solver (dim 4; pressure a^2 Sigma with a = 1, no source)."""
+
+    def __init__(self, mesh: Mesh, U_in, dim: int, gam: float, threads: int = 0, *,
+                 precision: int = PREC_FP64, device: int = 0):
+        super().__init__(mesh, U_in, dim, gam, 0.0, False, params=SolverParams(), solver=SOLVER_HLLE,
+                         precision=precision, device=device, threads=threads)
 
 
 class MUSCL_HLLE_p(_Named):

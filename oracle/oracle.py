@@ -43,6 +43,8 @@ def library() -> C.CDLL:
         lib.oracle_flux_star.restype = C.c_int
         lib.oracle_limiter.argtypes = [C.c_void_p, dp, dp, C.c_int, C.c_int, C.c_double, dp]
         lib.oracle_source.argtypes = [C.c_void_p, dp, C.c_int, dp]
+        lib.oracle_iso_flux.argtypes = [C.c_void_p, dp, C.c_int, C.c_int, dp]
+        lib.oracle_iso_char_vel.argtypes = [C.c_void_p, dp, dp, C.c_int, C.c_int, dp]
         _lib = lib
     return _lib
 
@@ -142,4 +144,18 @@ class Oracle:
         out = np.empty(self.dim)
         dp = C.POINTER(C.c_double)
         self._lib.oracle_source(self.h, _d(u).ctypes.data_as(dp), face, out.ctypes.data_as(dp))
+        return out
+
+    # isothermal solver (solver 4, dim 4)
+    def iso_flux(self, u, face: int, edge: int) -> np.ndarray:
+        out = np.empty(4)
+        dp = C.POINTER(C.c_double)
+        self._lib.oracle_iso_flux(self.h, _d(u).ctypes.data_as(dp), face, edge, out.ctypes.data_as(dp))
+        return out
+
+    def iso_char_vel(self, uL, uR, face: int, edge: int) -> np.ndarray:
+        out = np.empty(2)
+        dp = C.POINTER(C.c_double)
+        self._lib.oracle_iso_char_vel(self.h, _d(uL).ctypes.data_as(dp), _d(uR).ctypes.data_as(dp), face, edge,
+                                      out.ctypes.data_as(dp))
         return out

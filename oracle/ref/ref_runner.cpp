@@ -186,6 +186,51 @@ class Probe : public Base {
   }
 };
 
+// Isothermal solver (MUSCL_HLLE, dim 4): its flux (isothermal.hpp:141-195),
+// char_vel (:211-260) and flux_star (HLLE.hpp:17-59) are defined for 4-field
+// states and are dumped on seeded inputs; its limiter reads an
+// uninitialised variable (:272, 301-307) and its step reads and writes a
+// fifth field (MUSCL_base.hpp:203, 324, 368-370), so neither is dumped.
+// Each record: face, edge, uL[4], uR[4], flux(uL)[4], char_vel[2],
+// flux_star[4].
+template <class Base>
+class IsoProbe : public Base {
+ public:
+  using Base::Base;
+  void dump_iso_functions(const std::string& path, uint64_t seed, int nsamp) {
+    FILE* f = open_out(path);
+    std::mt19937_64 rng(seed);
+    std::uniform_real_distribution<double> uni(0.0, 1.0);
+    const int nf = (int)this->faces.size();
+    put_i64(f, nsamp);
+    for (int s = 0; s < nsamp; ++s) {
+      int face = (int)(uni(rng) * nf);
+      if (face >= nf) face = nf - 1;
+      int edge = (int)(uni(rng) * this->faces[face].size());
+      if (edge >= (int)this->faces[face].size()) edge = 0;
+      std::vector<double> ul(4), ur(4);
+      // speeds up to a few times the sound speed a = 1, both signs
+      const double shear = (s % 3 == 0) ? 6.0 : 1.0;
+      for (auto* u : {&ul, &ur}) {
+        (*u)[0] = 0.3 + 1.7 * uni(rng);
+        for (int k = 1; k < 4; ++k) (*u)[k] = shear * (uni(rng) - 0.5);
+      }
+      if (s % 7 == 0) ur = ul;
+      std::vector<double> fl = this->flux(ul, face, edge);
+      std::vector<double> cv = this->char_vel(ul, ur, face, edge);
+      std::vector<double> F = this->flux_star(ul, ur, face, edge);
+      put_i64(f, face);
+      put_i64(f, edge);
+      for (double v : ul) put_f64(f, v);
+      for (double v : ur) put_f64(f, v);
+      for (double v : fl) put_f64(f, v);
+      for (double v : cv) put_f64(f, v);
+      for (double v : F) put_f64(f, v);
+    }
+    std::fclose(f);
+  }
+};
+
 template <class Solver>
 int run(SurfaceMesh& mesh, const std::vector<std::vector<double>>& U_in, int dim, double gam,
         double omega_ns, bool acc, size_t threads, double dt, int nsteps, int dump_every,
@@ -302,6 +347,15 @@ int main(int argc, char** argv) {
       for (int k = 0; k < dim; ++k) U_in[i][k] = tmp[i * dim + k];
   }
 
+  if (solver == "HLLE") {
+    if (mode != "iso_functions") {
+      std::fprintf(stderr, "the isothermal solver supports only mode iso_functions\n");
+      return 1;
+    }
+    IsoProbe<MUSCL_HLLE> s(mesh, U_in, dim, gam, threads);
+    s.dump_iso_functions(out + "_isofuncs.bin", seed, nsamp);
+    return 0;
+  }
   if (solver == "HLLE_p")
     return run<MUSCL_HLLE_p>(mesh, U_in, dim, gam, omega_ns, acc, threads, dt, nsteps, dump_every,
                              out, mode, seed, nsamp);

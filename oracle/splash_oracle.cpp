@@ -26,16 +26,33 @@
 //   flux_star HLLC+ ............. Riemann_solvers/HLLCplus.hpp:17-177
 //   area_coeff, total_mass ...... physics/adiabatic.hpp:70-90
 //
+// and the isothermal solver MUSCL_HLLE (dim 4, solver kind 4):
+//   flux ........................ physics/isothermal.hpp:141-195
+//   source (zero) ............... physics/isothermal.hpp:199-208
+//   char_vel .................... physics/isothermal.hpp:211-260
+//   extra_dt_constr (1e20) ...... physics/isothermal.hpp:262-267
+//   limiter ..................... physics/isothermal.hpp:269-320
+//   flux_star HLLE .............. Riemann_solvers/HLLE.hpp:17-59
+//
 // Geometry arrays are taken in the reference numbering (the layout of
 // geometry/MUSCL_geometry.hpp:23-40 flattened per slot); they are produced by
 // the library's host geometry builder, which the test-suite pins bit-exactly
 // against the reference's own members.
 //
-// Two reference defects are restated in their defined form:
+// Reference defects restated in a defined form:
 //   * the area_coeff loop counter is uninitialised (adiabatic.hpp:75); it is
 //     taken to start at 0 (the built reference behaves that way);
 //   * the static mass counters in source() (adiabatic.hpp:400-401,452,536)
-//     are racy and never read; they are omitted.
+//     are racy and never read; they are omitted;
+//   * the isothermal path (dim 4) reads and writes a fifth state field that
+//     a 4-field state does not have (MUSCL_base.hpp:203, 324, 368-370, 538)
+//     and its limiter reads an uninitialised etha_minus (isothermal.hpp:272,
+//     307).  Restated: no fifth field (no E <-> Pi conversion, no energy
+//     sum), the CFL sound speed of find_v_max is the isothermal a = 1 (the
+//     speed the isothermal char_vel and limiter use), etha_minus is
+//     H_minus / BM_dist (its value in the adiabatic superbee,
+//     adiabatic.hpp:813) and etha_plus keeps its value as written (the
+//     second assignment, H_minus / BM_dist, isothermal.hpp:301-302).
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -95,7 +112,9 @@ struct Oracle {
   bool accretion_on = false, friction_on = true;
   double acc_rate = 0, e_acc = 0, omega_acc_abs = 0, tilt_angle = 0, acc_width = 0.1, alpha = 1e-6;
   double area_coeff = 0, total_mass = 0;
-  int solver = 3;  // 1 HLLE_p, 2 HLLC, 3 HLLC+
+  int solver = 3;  // 1 HLLE_p, 2 HLLC, 3 HLLC+, 4 HLLE (isothermal, dim 4)
+  static constexpr double a_iso = 1;  // isothermal sound speed (isothermal.hpp:138)
+  bool iso() const { return solver == 4; }
 
   // state
   std::vector<double> U, U_temp, source_plus, U_plus, U_minus, flux_var;
@@ -190,8 +209,72 @@ struct Oracle {
     return std::isnan(S_L) || std::isnan(S_R);
   }
 
+  // ---- physics/isothermal.hpp:141-195 (4 fields)
+  void iso_flux(const double* u, int f, int j, double* res) const {
+    const int s = face_off[f] + j;
+    const V ec = edge_center(f, j);
+    const double PI = a_iso * a_iso * u[0];
+    V vel = cross(ec, V{u[1], u[2], u[3]});
+    vel = vel / (-u[0]);
+    const double ndv = dot(en(s), vel);
+    const V nxR = cross(en(s), ec);
+    res[0] = u[0] * dot(vel, en(s));
+    res[1] = u[1] * ndv - nxR.x * PI;
+    res[2] = u[2] * ndv - nxR.y * PI;
+    res[3] = u[3] * ndv - nxR.z * PI;
+  }
+  // ---- physics/isothermal.hpp:211-260
+  void iso_char_vel(const double* uL, const double* uR, int f, int j, double& S_L, double& S_R) const {
+    const int s = face_off[f] + j;
+    const V ec = edge_center(f, j);
+    V vel_l = cross(ec, V{uL[1], uL[2], uL[3]});
+    vel_l = vel_l / ((-uL[0]) * norm(ec));
+    V vel_r = cross(ec, V{uR[1], uR[2], uR[3]});
+    vel_r = vel_r / ((-uR[0]) * norm(ec));
+    const double vl = dot(vel_l, en(s)), vr = dot(vel_r, en(s));
+    S_L = smin(vl, vr) - smax(a_iso, a_iso);
+    S_R = smax(vl, vr) + smax(a_iso, a_iso);
+  }
+  // ---- Riemann_solvers/HLLE.hpp:17-59 ; returns stop bits (2 = order)
+  int iso_flux_star(const double* uL, const double* uR, int f, int j, double* F) const {
+    double S_L, S_R, FL[4], FR[4];
+    iso_char_vel(uL, uR, f, j, S_L, S_R);
+    iso_flux(uL, f, j, FL);
+    iso_flux(uR, f, j, FR);
+    int bits = (std::isnan(S_L) || std::isnan(S_R)) ? 1 : 0;
+    if (S_L >= 0) {
+      for (int i = 0; i < 4; ++i) F[i] = FL[i];
+    } else if (S_L < 0 && S_R > 0) {
+      for (int i = 0; i < 4; ++i) F[i] = (S_R * FL[i] - S_L * FR[i] + S_R * S_L * (uR[i] - uL[i])) / (S_R - S_L);
+    } else if (S_R <= 0) {
+      for (int i = 0; i < 4; ++i) F[i] = FR[i];
+    } else {
+      for (int i = 0; i < 4; ++i) F[i] = FR[i];
+      bits |= 2;
+    }
+    return bits;
+  }
+  // ---- physics/isothermal.hpp:269-320 (defined form, see the header)
+  void iso_limiter(const double* r, const double* w, int f, int j, double* res) const {
+    const int s = face_off[f] + j;
+    const V ec = edge_center(f, j);
+    V vel = cross(ec, V{w[1], w[2], w[3]});
+    vel = vel / (-w[0]);
+    const double c = a_iso;
+    const double nu_plus = (c + dot(vel, en(s))) * dt *
+                           (gc_distance(vtx(vslot(f, j)), vtx(vslot1(f, j))) / area[f]);
+    const double etha_plus = hm[s] / bm[s];
+    const double etha_minus = hm[s] / bm[s];
+    const double twoN = (double)(2 * (size_t)nsl(f));
+    for (int i = 0; i < 4; ++i) {
+      res[i] = smax(0., smax(smin(1., etha_minus * r[i] * 2 / (twoN * nu_plus)), smin(r[i], etha_plus)));
+      if (std::isnan(r[i])) res[i] = 0;
+    }
+  }
+
   // ---- Riemann solvers; returns stop bits (1 = NaN wave speed, 2 = order)
   int flux_star(const double* uL, const double* uR, int f, int j, double* F) const {
+    if (iso()) return iso_flux_star(uL, uR, f, j, F);
     int bits = 0;
     double S_L, S_R;
     if (solver == 1) {  // HLLE_p.hpp:19-58
@@ -302,6 +385,10 @@ struct Oracle {
 
   // ---- physics/adiabatic.hpp:685-828 ; w = U[face] with w[4] the pressure
   void limiter(const double* r, const double* w, int f, int j, double* res) const {
+    if (iso()) {
+      iso_limiter(r, w, f, j, res);
+      return;
+    }
     auto h = [](double x) {
       double o = 0;
       if (x < 1 && x > 0) o = (1 - std::tanh(4 * std::pow(x, 2.0) * std::pow(1 - x, 0.1)));
@@ -333,6 +420,7 @@ struct Oracle {
   // ---- physics/adiabatic.hpp:396-541 ; u[4] is the pressure
   void source(const double* u, int f, double* res) const {
     for (int i = 0; i < dim; ++i) res[i] = 0;
+    if (iso()) return;  // isothermal.hpp:199-208
     V fcn = fc(f);
     fcn = fcn / norm(fcn);
     V vel = cross(fcn, V{u[1], u[2], u[3]});
@@ -403,6 +491,7 @@ struct Oracle {
   // ---- physics/adiabatic.hpp:543-580 (u[4] is the energy)
   double extra_dt_constr() {
     double dt_new = 1e20;
+    if (iso()) return dt_new;  // isothermal.hpp:262-267
     for (int i = 0; i < nf; ++i) {
       const double* u = &U[(size_t)i * dim];
       V fcn = fc(i);
@@ -436,8 +525,8 @@ struct Oracle {
       r = r / norm(r);
       V vel = cross(r, V{u[1], u[2], u[3]});
       vel = vel / u[0];
-      const double p = pressure_fc(u, i);
-      const double c_s = std::sqrt(gam * p / u[0]);
+      // isothermal: the sound speed a (the reference reads a fifth field here)
+      const double c_s = iso() ? a_iso : std::sqrt(gam * pressure_fc(u, i) / u[0]);
       if (norm(vel) > mx) mx = norm(vel);
       if (c_s > mx) mx = c_s;
     }
@@ -448,6 +537,10 @@ struct Oracle {
   void find_U_edges() {
     for (int i = 0; i < nf; ++i) {
       double* u = &U[(size_t)i * dim];
+      if (iso()) {
+        u[0] -= 0.0;  // rho_an
+        continue;
+      }
       u[4] = pressure_fc(u, i);
       u[0] -= 0.0;  // rho_an
       u[4] -= 0.0;  // p_an
@@ -567,7 +660,7 @@ struct Oracle {
       l1 += u[1] * area[i];
       l2 += u[2] * area[i];
       l3 += u[3] * area[i];
-      e += u[4] * area[i];
+      if (!iso()) e += u[4] * area[i];
     }
     diag[0] = m;
     diag[1] = l1;
@@ -596,8 +689,9 @@ void* oracle_create(int nv, int nf, int ns, const double* vertices, const int* f
                     double h0, double round_diff, const double* U_in, int dim, double gam,
                     double omega_ns, int accretion_on, const double* params, int solver_kind,
                     int threads) {
-  if (dim != 5 || nf <= 0 || ns <= 0) return nullptr;
-  if (solver_kind < 1 || solver_kind > 3) return nullptr;
+  if (nf <= 0 || ns <= 0) return nullptr;
+  if (solver_kind < 1 || solver_kind > 4) return nullptr;
+  if (dim != (solver_kind == 4 ? 4 : 5)) return nullptr;
   Oracle* o = new Oracle();
   o->nv = nv;
   o->nf = nf;
@@ -733,6 +827,14 @@ void oracle_limiter(void* h, const double* r, const double* w, int face, int edg
 
 void oracle_source(void* h, const double* u, int face, double* out) {
   static_cast<Oracle*>(h)->source(u, face, out);
+}
+
+// isothermal solver functions: physical flux and wave speeds (S_L, S_R)
+void oracle_iso_flux(void* h, const double* u, int face, int edge, double* out) {
+  static_cast<Oracle*>(h)->iso_flux(u, face, edge, out);
+}
+void oracle_iso_char_vel(void* h, const double* uL, const double* uR, int face, int edge, double* out) {
+  static_cast<Oracle*>(h)->iso_char_vel(uL, uR, face, edge, out[0], out[1]);
 }
 
 }  // extern "C"

@@ -8,6 +8,8 @@ directory (input/parameters.json, input/input.dat, results/), and stores:
 * geom_<mesh><n>.npz     full geometry members (geometry/MUSCL_geometry.hpp:23-40)
 * geom_hashes.json       SHA-256 of every geometry array for larger meshes
 * funcs_<case>.npz       per-function known answers: flux_star, limiter, source
+* isofuncs_<case>.npz    isothermal solver (MUSCL_HLLE, dim 4): flux,
+                         char_vel and flux_star known answers
 * state_<case>.npz       conserved state after selected steps of do_step
 
 Usage:  python tests/golden/gen_golden.py [--ref-root /path/to/reference]
@@ -44,7 +46,7 @@ def params_json(p: dict) -> dict:
 
 
 def run(mode, mesh, level, solver, gam, omega_ns, acc, dt, nsteps, dump_every, U, params,
-        seed=0, nsamp=0, threads=8):
+        seed=0, nsamp=0, threads=8, dim=5):
     with tempfile.TemporaryDirectory() as td:
         td = Path(td)
         (td / "input").mkdir()
@@ -53,12 +55,12 @@ def run(mode, mesh, level, solver, gam, omega_ns, acc, dt, nsteps, dump_every, U
         if U is not None:
             ic.write_input_dat(td / "input" / "input.dat", U)
         out = td / "out"
-        cmd = [str(RUNNER), mode, mesh, str(level), solver, "5", repr(gam), repr(omega_ns),
+        cmd = [str(RUNNER), mode, mesh, str(level), solver, str(dim), repr(gam), repr(omega_ns),
                "1" if acc else "0", str(threads), repr(dt), str(nsteps), str(dump_every), str(out),
                str(seed), str(nsamp)]
         subprocess.run(cmd, cwd=td, check=True, stdout=subprocess.DEVNULL)
         res = {}
-        for suffix in ("_geom.bin", "_states.bin", "_funcs.bin", "_scalars.txt"):
+        for suffix in ("_geom.bin", "_states.bin", "_funcs.bin", "_isofuncs.bin", "_scalars.txt"):
             p = Path(str(out) + suffix)
             if p.exists():
                 res[suffix] = p.read_bytes()
@@ -183,6 +185,22 @@ def funcs_case(name, solver, params, acc=True, mesh="hex", level=3, nsamp=300, s
     print(f"funcs_{name}: {nsamp} samples")
 
 
+def iso_funcs_case(name, mesh="hex", level=3, nsamp=400, seed=13, gam=1.25):
+    """Known answers of the isothermal solver's defined functions (flux,
+    char_vel, HLLE flux_star) on seeded 4-field states."""
+    res = run("iso_functions", mesh, level, "HLLE", gam, 0.0, False, 7e-4, 0, 0, None, ACC_PARAMS,
+              seed=seed, nsamp=nsamp, dim=4)
+    b = res["_isofuncs.bin"]
+    n = int(np.frombuffer(b, dtype="<i8", count=1)[0])
+    rec = np.dtype([("face", "<i8"), ("edge", "<i8"), ("ul", "<f8", 4), ("ur", "<f8", 4), ("fl", "<f8", 4),
+                    ("cv", "<f8", 2), ("F", "<f8", 4)])
+    a = np.frombuffer(b, dtype=rec, count=n, offset=8)
+    out = {k: np.array(a[k]) for k in rec.names}
+    out.update({"gam": np.float64(gam), "mesh": mesh, "level": level})
+    np.savez_compressed(HERE / f"isofuncs_{name}.npz", **out)
+    print(f"isofuncs_{name}: {n} samples")
+
+
 def writers_case(name, mesh, level, solver, gam, acc, params, dt, nsteps, recipe, seed):
     """The reference's own output files (results/*.dat, light curves) for the
     driver sequence of test.cpp:84-149, stored as text."""
@@ -208,9 +226,15 @@ def writers_case(name, mesh, level, solver, gam, acc, params, dt, nsteps, recipe
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.parse_args()
+    ap.add_argument("--only", choices=["isothermal"], default=None,
+                    help="regenerate one group of fixtures only")
+    a = ap.parse_args()
     if not RUNNER.exists():
         sys.exit(f"{RUNNER} missing: make -C oracle/ref REF=<reference checkout>")
+    if a.only == "isothermal":
+        iso_funcs_case("hlle_hex3")
+        iso_funcs_case("hlle_quad3", mesh="quad", seed=17)
+        return
     # geometry: full arrays for small meshes, hashes for larger ones
     scal = {}
     for mesh, level in (("hex", 2), ("hex", 3), ("quad", 3)):
@@ -230,6 +254,8 @@ def main():
     funcs_case("hllc", "HLLC", ACC_PARAMS)
     funcs_case("hllcp", "HLLCplus", ACC_PARAMS)
     funcs_case("hllcp_nofric", "HLLCplus", nofric)
+    iso_funcs_case("hlle_hex3")
+    iso_funcs_case("hlle_quad3", mesh="quad", seed=17)
 
     gam = ic.gam2d(4 / 3)
     # small plain-method workload: hex(4), HLLE_p, accretion off, dt 1e-3, 100 steps

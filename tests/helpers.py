@@ -33,8 +33,8 @@ def rel_linf(a: np.ndarray, b: np.ndarray) -> np.ndarray:
     return np.max(np.abs(a - b), axis=0) / scale
 
 
-def make_oracle(geom, case: dict, threads: int = 0):
+def make_oracle(geom, case: dict, threads: int = 0, dim: int = 5):
     from oracle.oracle import Oracle
 
     return Oracle(geom, case["U0"], float(case["gam"]), 0.0, bool(case["accretion_on"]),
-                  [float(x) for x in case["params"]], int(case["solver"]), threads=threads)
+                  [float(x) for x in case["params"]], int(case["solver"]), threads=threads, dim=dim)

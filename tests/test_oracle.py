@@ -46,6 +46,27 @@ def test_functions_known_answers(case, geoms):
         assert _same(src, f["src"][i]), (case, "source", i, src, f["src"][i])
 
 
+@pytest.mark.parametrize("case", ["hlle_hex3", "hlle_quad3"])
+def test_isothermal_functions_known_answers(case, geoms):
+    """The isothermal solver's defined functions (flux, char_vel, HLLE
+    flux_star; MUSCL_HLLE, dim 4) against the reference's own outputs."""
+    f = load(f"isofuncs_{case}.npz")
+    g = geoms[(str(f["mesh"]), int(f["level"]))]
+    o = make_oracle(g, {"U0": np.ones((g.n_faces, 4)), "gam": f["gam"], "accretion_on": False,
+                        "params": np.array([0, 0, 0, 0, 0.1, 1e-6, 1.0]), "solver": 4}, dim=4)
+    kinds = set()
+    for i in range(len(f["face"])):
+        face, edge = int(f["face"][i]), int(f["edge"][i])
+        fl = o.iso_flux(f["ul"][i], face, edge)
+        assert _same(fl, f["fl"][i]), (case, "flux", i, fl, f["fl"][i])
+        cv = o.iso_char_vel(f["ul"][i], f["ur"][i], face, edge)
+        assert _same(cv, f["cv"][i]), (case, "char_vel", i, cv, f["cv"][i])
+        F, _ = o.flux_star(f["ul"][i], f["ur"][i], face, edge)
+        assert _same(F, f["F"][i]), (case, "flux_star", i, F, f["F"][i])
+        kinds.add("left" if cv[0] >= 0 else ("right" if cv[1] <= 0 else "star"))
+    assert kinds == {"left", "right", "star"}, kinds
+
+
 @pytest.mark.parametrize("case", STATE_CASES)
 def test_states_match_reference(case, geoms):
     c = load(f"state_{case}.npz")
