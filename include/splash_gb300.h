@@ -217,7 +217,9 @@ SPLASH_API int splash_geometry_get(const splash_geometry* g, const char* name, v
 typedef struct splash_member {
   int mesh_kind;        /* splash_mesh_kind */
   int level;            /* subdivision level */
-  const double* U_in;   /* [n_faces][5] conserved state, reference face order */
+  const double* U_in;   /* [n_faces][dim] conserved state, reference face order;
+                           dim = 4 for SPLASH_SOLVER_HLLE (isothermal, no source:
+                           accretion_on and params are ignored), else 5 */
   double gam;
   double omega_ns;
   int accretion_on;

@@ -332,8 +332,6 @@ int splash_create(const splash_mesh_desc* mesh, const double* U_in, int dim, dou
                 "dim=%d: the adiabatic solvers need dim=5 (the reference latches stop_check and "
                 "then indexes out of bounds, physics/adiabatic.hpp:26-30)",
                 dim);
-  if (solver_kind == SPLASH_SOLVER_HLLE && precision == SPLASH_PREC_MIXED)
-    return fail(SPLASH_E_UNSUPPORTED, "the isothermal solver runs in FP64 only");
   if (precision != SPLASH_PREC_FP64 && precision != SPLASH_PREC_MIXED)
     return fail(SPLASH_E_INVALID, "unknown precision %d", precision);
   if (precision == SPLASH_PREC_MIXED && !splash::mixed_available())
@@ -382,7 +380,7 @@ int splash_create(const splash_mesh_desc* mesh, const double* U_in, int dim, dou
     P.total_mass = s->total_mass;
     P.h0 = g.h0;
     P.round_diff = g.round_diff;
-    P.accretion_on = accretion_on ? 1 : 0;
+    P.accretion_on = s->accretion_on ? 1 : 0;
     P.friction_on = params->friction_on ? 1 : 0;
     P.solver = solver_kind;
 

@@ -261,7 +261,7 @@ int splash_ensemble_create(const splash_member* members, int n, int device, int 
   for (int i = 0; i < n; ++i) {
     const splash_member& m = members[i];
     if (!m.U_in) return set_error(SPLASH_E_INVALID, "member %d: U_in is NULL", i);
-    if (m.solver_kind < SPLASH_SOLVER_HLLE_P || m.solver_kind > SPLASH_SOLVER_HLLCPLUS)
+    if (m.solver_kind < SPLASH_SOLVER_HLLE_P || m.solver_kind > SPLASH_SOLVER_HLLE)
       return set_error(SPLASH_E_INVALID, "member %d: unknown solver kind %d", i, m.solver_kind);
     if (!(m.gam > 1.0 && m.gam < 2.0)) return set_error(SPLASH_E_INVALID, "member %d: gam outside (1, 2)", i);
   }
@@ -351,7 +351,11 @@ int splash_ensemble_create(const splash_member* members, int n, int device, int 
       I.G = L.G;
       // the member's accretion source (depends on its tilt, rate and width)
       const double ac = area_coefficient(L.geom, m.params.acc_width);
-      const std::vector<double> acc = accretion_source(L.sp, m.params, ac, m.accretion_on != 0);
+      // the isothermal solver (4 state fields) has no source term
+      const bool iso = m.solver_kind == SPLASH_SOLVER_HLLE;
+      const int mdim = iso ? 4 : kDim;
+      const bool acc_on = m.accretion_on != 0 && !iso;
+      const std::vector<double> acc = accretion_source(L.sp, m.params, ac, acc_on);
       ENS_CUDA(cudaMemcpy(e->acc + e->off_face[i], acc.data(), fp * sizeof(double), cudaMemcpyHostToDevice));
       I.G.acc_src = e->acc + e->off_face[i];
       I.S.U = e->U + e->off_face[i] * kDim;
@@ -361,7 +365,7 @@ int splash_ensemble_create(const splash_member* members, int n, int device, int 
       I.S.err = e->err + (size_t)i * 4;
       I.S.keys = e->keys + (size_t)i * 2;
       double tm = 0;
-      for (int r = 0; r < nf; ++r) tm += m.U_in[(size_t)r * kDim] * L.geom.area[r];
+      for (int r = 0; r < nf; ++r) tm += m.U_in[(size_t)r * mdim] * L.geom.area[r];
       PhysParams& P = I.P;
       P.gam = m.gam;
       P.omega_ns = m.omega_ns;
@@ -374,13 +378,13 @@ int splash_ensemble_create(const splash_member* members, int n, int device, int 
       P.total_mass = tm;
       P.h0 = L.geom.h0;
       P.round_diff = L.geom.round_diff;
-      P.accretion_on = m.accretion_on ? 1 : 0;
+      P.accretion_on = acc_on ? 1 : 0;
       P.friction_on = m.params.friction_on ? 1 : 0;
       P.solver = m.solver_kind;
       // state, reference order -> internal planes
       std::vector<double> planes((size_t)fp * kDim, 0.0);
       for (int q = 0; q < nf; ++q)
-        for (int k = 0; k < kDim; ++k) planes[(size_t)k * fp + q] = m.U_in[(size_t)L.sp.perm[q] * kDim + k];
+        for (int k = 0; k < mdim; ++k) planes[(size_t)k * fp + q] = m.U_in[(size_t)L.sp.perm[q] * mdim + k];
       ENS_CUDA(cudaMemcpy(I.S.U, planes.data(), planes.size() * sizeof(double), cudaMemcpyHostToDevice));
       e->inst.push_back(I);
     }
@@ -443,12 +447,12 @@ int splash_ensemble_get_state(splash_ensemble* h, int member, double* U) {
   if (member < 0 || member >= e->n || !U) return splash::set_error(SPLASH_E_INVALID, "bad member or U");
   const splash::Level& L = e->levels[e->member_level[member]];
   const int nf = L.sp.n_faces, fp = L.sp.fpad;
+  const int mdim = (e->inst[member].P.solver == splash::kSolverIsoHLLE) ? 4 : splash::kDim;
   ENS_CUDA(cudaMemcpyAsync(e->h_stage, e->inst[member].S.U, (size_t)fp * splash::kDim * sizeof(double),
                            cudaMemcpyDeviceToHost, e->stream));
   ENS_CUDA(cudaStreamSynchronize(e->stream));
   for (int q = 0; q < nf; ++q)
-    for (int k = 0; k < splash::kDim; ++k)
-      U[(size_t)L.sp.perm[q] * splash::kDim + k] = e->h_stage[(size_t)k * fp + q];
+    for (int k = 0; k < mdim; ++k) U[(size_t)L.sp.perm[q] * mdim + k] = e->h_stage[(size_t)k * fp + q];
   return SPLASH_OK;
 }
 

@@ -44,6 +44,7 @@ uint64_t hilbert_key3(double x, double y, double z, int bits) {
 
 std::vector<int> hilbert_order(const double* xyz, int n) {
   std::vector<uint64_t> key(n);
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < n; ++i) {
     const double* p = xyz + 3 * (size_t)i;
     const double r = std::sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);

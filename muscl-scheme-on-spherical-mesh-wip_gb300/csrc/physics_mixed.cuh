@@ -182,6 +182,53 @@ __device__ __forceinline__ unsigned flux_star(const float* uL, const float* uR, 
   return bits;
 }
 
+// Isothermal solver (MUSCL_HLLE, 4 fields, pressure a^2 Sigma with a = 1):
+// physical flux (physics/isothermal.hpp:141-195), wave speeds (:211-260)
+// and the HLLE flux (Riemann_solvers/HLLE.hpp:17-59) in FP32.  In FP32 the
+// unit edge centre needs no |ec| rescale, so one edge velocity serves flux
+// and wave speeds.  F[4] is 0.  Returns the stop bits of splash_gb300.h.
+__device__ __forceinline__ void iso_phys_flux(const float* u, F3 vel, float vn, const SlotGeomF& g, float* F) {
+  const float PI = u[0];
+  F[0] = u[0] * vn;
+  F[1] = u[1] * vn - g.nxr.x * PI;
+  F[2] = u[2] * vn - g.nxr.y * PI;
+  F[3] = u[3] * vn - g.nxr.z * PI;
+  F[4] = 0.f;
+}
+
+__device__ __forceinline__ unsigned iso_flux_star(const float* uL, const float* uR, const SlotGeomF& g, float* F) {
+  const F3 vL = scal(cross3(g.ec, f3(uL[1], uL[2], uL[3])), -1.0f / uL[0]);
+  const F3 vR = scal(cross3(g.ec, f3(uR[1], uR[2], uR[3])), -1.0f / uR[0]);
+  const float vnL = dot3(vL, g.en), vnR = dot3(vR, g.en);
+  const float S_L = smin(vnL, vnR) - 1.f;
+  const float S_R = smax(vnL, vnR) + 1.f;
+  unsigned bits = (isnan(S_L) || isnan(S_R)) ? 2u : 0u;
+  float FL[kDim], FR[kDim];
+  iso_phys_flux(uL, vL, vnL, g, FL);
+  iso_phys_flux(uR, vR, vnR, g, FR);
+  if (S_L >= 0) {
+#pragma unroll
+    for (int i = 0; i < kDim; ++i) F[i] = FL[i];
+  } else if (S_L < 0 && S_R > 0) {
+    const float inv = 1.0f / (S_R - S_L);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) F[i] = (S_R * FL[i] - S_L * FR[i] + S_R * S_L * (uR[i] - uL[i])) * inv;
+    F[4] = 0.f;
+  } else {
+    if (!(S_R <= 0)) bits |= 4u;
+#pragma unroll
+    for (int i = 0; i < kDim; ++i) F[i] = FR[i];
+  }
+  return bits;
+}
+
+// isothermal limiter (physics/isothermal.hpp:269-320, etha_minus taken as
+// H_minus / BM_dist) for one field; sb_scale = 2 eta / (2 N nu_plus)
+__device__ __forceinline__ float iso_limiter_field(float r, float eta, float sb_scale) {
+  if (isnan(r)) return 0.f;
+  return smax(0.f, smax(smin(1.f, r * sb_scale), smin(r, eta)));
+}
+
 // h(r) switch and the blended limiter (physics/adiabatic.hpp:685-828).
 // On (0, 1) the switch is 1 - tanh(y) = 2 / (1 + e^{2y}) (no cancellation);
 // for r >= 1 it is tanh(y)^6 = ((e^{2y} - 1) / (e^{2y} + 1))^6.

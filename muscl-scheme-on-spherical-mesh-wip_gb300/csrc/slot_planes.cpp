@@ -39,12 +39,15 @@ SlotPlanes make_slot_planes(const RefGeometry& g) {
 
   sp.perm = hilbert_order(g.face_centers.data(), nf);
   sp.iperm.assign(nf, 0);
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < nf; ++i) sp.iperm[sp.perm[i]] = i;
   const std::vector<int>& perm = sp.perm;
   const std::vector<int>& iperm = sp.iperm;
 
   // reference-order reverse slot (std::find of MUSCL_base.hpp:383-384)
   std::vector<int> j0_of(g.n_slots, -1);
+  bool asymmetric = false;
+#pragma omp parallel for schedule(static) reduction(|| : asymmetric)
   for (int f = 0; f < nf; ++f) {
     for (int s = g.face_off[f]; s < g.face_off[f + 1]; ++s) {
       const int nb = g.nbr_edge[s];
@@ -54,10 +57,11 @@ SlotPlanes make_slot_planes(const RefGeometry& g) {
           j0 = q - g.face_off[nb];
           break;
         }
-      if (j0 < 0) throw std::runtime_error("edge neighbour relation is not symmetric");
+      if (j0 < 0) asymmetric = true;
       j0_of[s] = j0;
     }
   }
+  if (asymmetric) throw std::runtime_error("edge neighbour relation is not symmetric");
 
   sp.nslots.assign(fpad, 0);
   sp.fcn.assign(3 * (size_t)fpad, 0.0);
@@ -75,6 +79,8 @@ SlotPlanes make_slot_planes(const RefGeometry& g) {
   sp.nxr.assign(3 * PS, 0.0);
   sp.chord.assign(PS, 0.0);
 
+  // every face writes only its own entries: the fill is order-independent
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < nf; ++i) {
     const int r = perm[i];
     const int n = g.face_off[r + 1] - g.face_off[r];
@@ -164,6 +170,7 @@ std::vector<double> accretion_source_fcn(const std::vector<double>& fcn, int n_f
   const double sigma = par.acc_width / 2.355;
   const double mu = M_PI / 2;
   const double st = std::sin(par.tilt_angle), ct = std::cos(par.tilt_angle);
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < n_faces; ++i) {
     const V3 c{fcn[i], fcn[fpad + i], fcn[2 * (size_t)fpad + i]};
     const double x = c.y * std::sin(par.tilt_angle) + c.z * std::cos(par.tilt_angle);

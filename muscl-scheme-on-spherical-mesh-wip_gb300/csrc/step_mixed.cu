@@ -176,6 +176,21 @@ __device__ __forceinline__ void source_f32(const float* w, F3 fcn, float acc0, c
   }
 }
 
+// Isothermal state (4 fields): W32 is the state itself (field 4 unused) and
+// the CFL candidate is max(|v|^2, a^2) with a = 1 (find_v_max with the
+// isothermal sound speed); no extra constraint (isothermal.hpp:262-267).
+__device__ __forceinline__ void iso_w32_candidates(const double* u, f64::D3 r, float* W32, int fp, int f,
+                                                   double& vmax2, double& dmin) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) W32[k * fp + f] = (float)u[k];
+  W32[4 * fp + f] = 0.f;
+  const f64::D3 c = f64::cross3(r, f64::d3(u[1], u[2], u[3]));
+  const double inv_rho = 1.0 / u[0];
+  const double v2 = (c.x * c.x + c.y * c.y + c.z * c.z) * inv_rho * inv_rho;
+  vmax2 = fmax(v2, 1.0);
+  dmin = 1e20;
+}
+
 // W32 and the dt candidates of the current U for face f (all 32 lanes of a
 // warp call it; lanes past the last face contribute neutral values).
 __device__ __forceinline__ void prepare_body(const DevGeomMixed& G, const DevState& S,
@@ -186,10 +201,14 @@ __device__ __forceinline__ void prepare_body(const DevGeomMixed& G, const DevSta
 #pragma unroll
     for (int k = 0; k < kDim; ++k) u[k] = S.U[k * G.fpad + f];
     const f64::D3 r = plane3d(G.fcn, G.fpad, f);
-    double v2, inv_rho;
-    const double p = pressure_recover(u, r, P.gam, v2, inv_rho);
-    store_w32(S.W32, G.fpad, f, u, p);
-    dt_candidates_sq(u, r, p, v2, inv_rho, P, vmax, dmin);
+    if (P.solver == kSolverIsoHLLE) {
+      iso_w32_candidates(u, r, S.W32, G.fpad, f, vmax, dmin);
+    } else {
+      double v2, inv_rho;
+      const double p = pressure_recover(u, r, P.gam, v2, inv_rho);
+      store_w32(S.W32, G.fpad, f, u, p);
+      dt_candidates_sq(u, r, p, v2, inv_rho, P, vmax, dmin);
+    }
   }
   fold_candidates(vmax, dmin, S.keys);
 }
@@ -242,6 +261,30 @@ __device__ __forceinline__ void recon_body(const DevGeomMixed& G, const DevState
   const float* __restrict__ W = S.W32;
   const float dt = (float)S.scal[kScDt];
   const float gam = (float)P.gam;
+  if (P.solver == kSolverIsoHLLE) {
+    // isothermal: 4 fields, superbee limiter with the Courant factor
+    // (a + v.n) dt arc / area (physics/isothermal.hpp:269-320)
+    float w[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) w[k] = W[k * fp + f];
+    const int s = j * fp + f;
+    const int ia = G.sten[s], ib = G.sten[PS + s], ic = G.sten[2 * PS + s], id = G.sten[3 * PS + s];
+    const float bp0 = G.beta[s], bp1 = G.beta[PS + s], bm0 = G.beta[2 * PS + s], bm1 = G.beta[3 * PS + s];
+    const float ihp = G.inv_h[s], ihm = G.inv_h[PS + s], bmd = G.bm[s];
+    const F3 vel = scal(cross3(plane3f(G.ec, PS, s), f3(w[1], w[2], w[3])), -1.0f / w[0]);
+    const float nu_plus = (1.f + dot3(vel, plane3f(G.en, PS, s))) * dt * G.arc_a[s];
+    const float eta = G.eta[PS + s];
+    const float sb_scale = eta * 2.f / ((float)(2 * n) * nu_plus);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const float* Wk = W + k * fp;
+      const float pp = (bp0 * Wk[ia] + bp1 * Wk[ib] - w[k]) * ihp;
+      const float pm = (w[k] - (bm0 * Wk[ic] + bm1 * Wk[id])) * ihm;
+      const float lim = iso_limiter_field(pm / pp, eta, sb_scale);
+      S.uplus32[k * PS + s] = w[k] + pp * lim * bmd;
+    }
+    return;
+  }
   float w[kDim];
 #pragma unroll
   for (int k = 0; k < kDim; ++k) w[k] = W[k * fp + f];
@@ -316,7 +359,8 @@ __device__ __forceinline__ void flux_body(const DevGeomMixed& G, const DevState&
       g.ec = plane3f(G.ec, PS, s);
       g.en = plane3f(G.en, PS, s);
       g.nxr = plane3f(G.nxr, PS, s);
-      unsigned bits = flux_star(uL, uR, g, gam, P.solver, F);
+      unsigned bits = (P.solver == kSolverIsoHLLE) ? iso_flux_star(uL, uR, g, F)
+                                                   : flux_star(uL, uR, g, gam, P.solver, F);
 #pragma unroll
       for (int k = 0; k < kDim; ++k)
         if (isnan(F[k])) bits |= 1u;
@@ -357,13 +401,25 @@ __device__ __forceinline__ void flux_body(const DevGeomMixed& G, const DevState&
     if (P.accretion_on) u[0] += dt_here * acc0;  // accretion mass source in FP64
     if (u[0] < 1e-8) u[0] = 1e-8;
     const f64::D3 r = plane3d(G.fcn, fp, f);
-    double v2, inv_rho;
-    const double p = pressure_recover(u, r, P.gam, v2, inv_rho);
-    store_w32(S.W32, fp, f, u, p);
-    if (STAGE == 2) {
+    if (P.solver == kSolverIsoHLLE) {
+      u[4] = 0.0;
+      double vm, dm;
+      iso_w32_candidates(u, r, S.W32, fp, f, vm, dm);
+      if (STAGE == 2) {
 #pragma unroll
-      for (int k = 0; k < kDim; ++k) S.U[k * fp + f] = u[k];
-      dt_candidates_sq(u, r, p, v2, inv_rho, P, vmax, dmin);
+        for (int k = 0; k < kDim; ++k) S.U[k * fp + f] = u[k];
+        vmax = vm;
+        dmin = dm;
+      }
+    } else {
+      double v2, inv_rho;
+      const double p = pressure_recover(u, r, P.gam, v2, inv_rho);
+      store_w32(S.W32, fp, f, u, p);
+      if (STAGE == 2) {
+#pragma unroll
+        for (int k = 0; k < kDim; ++k) S.U[k * fp + f] = u[k];
+        dt_candidates_sq(u, r, p, v2, inv_rho, P, vmax, dmin);
+      }
     }
   }
   if (STAGE == 2) fold_candidates(vmax, dmin, S.keys);

@@ -484,6 +484,7 @@ class Ensemble:
         self._keep = []
         arr = (Member * len(members))()
         self.n_faces = []
+        self.dims = []
         for i, m in enumerate(members):
             U = np.ascontiguousarray(m["U_in"], dtype=np.float64)
             self._keep.append(U)
@@ -497,6 +498,7 @@ class Ensemble:
             arr[i].params = (m.get("params") or SolverParams()).to_c()
             arr[i].solver_kind = m.get("solver", SOLVER_HLLCPLUS)
             self.n_faces.append(U.shape[0])
+            self.dims.append(4 if arr[i].solver_kind == SOLVER_HLLE else 5)
         _check(lib.splash_ensemble_create(arr, len(members), device, 1 if autotune else 0,
                                           C.byref(self.handle)))
         self._keep = []
@@ -524,7 +526,7 @@ class Ensemble:
         return int(p.value or 0)
 
     def get_state(self, member: int) -> np.ndarray:
-        U = np.empty((self.n_faces[member], 5))
+        U = np.empty((self.n_faces[member], self.dims[member]))
         _check(self._lib.splash_ensemble_get_state(self.handle, member, _dptr(U)))
         return U
 

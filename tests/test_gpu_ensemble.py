@@ -1,7 +1,8 @@
 """Ensembles: every member advanced by the shared batched launches must
 compute exactly what a standalone mixed-precision solver computes (same
 kernels, same per-face arithmetic), whatever block schedule the autotuner
-picked."""
+picked.  Members mix the adiabatic solvers (dim 5) and the isothermal one
+(dim 4) in the same launches."""
 import numpy as np
 import pytest
 
@@ -26,8 +27,11 @@ def members(seed=7, count=10):
                                  omega_acc_abs=float(rng.uniform(0, 1)),
                                  tilt_angle=float(rng.uniform(0, np.pi / 2)), acc_width=0.1,
                                  alpha=1e-6, friction_on=bool(i % 3))
+        solver = [1, 2, 3][i % 3]
+        if i % 4 == 1:  # isothermal members: 4 state fields, no source
+            solver, U = sg.SOLVER_HLLE, np.ascontiguousarray(U[:, :4])
         out.append({"mesh": mesh, "U_in": U, "gam": gam, "omega_ns": 0.0, "accretion_on": True,
-                    "params": params, "solver": [1, 2, 3][i % 3]})
+                    "params": params, "solver": solver})
     return out
 
 
@@ -44,7 +48,7 @@ def test_ensemble_members_equal_standalone_solvers():
     ens.do_steps(25, 1e-2)  # dt0 large: every member takes its own CFL dt
     dts = set()
     for i, m in enumerate(ms):
-        s = sg.Solver(m["mesh"], m["U_in"], 5, m["gam"], 0.0, True, params=m["params"],
+        s = sg.Solver(m["mesh"], m["U_in"], m["U_in"].shape[1], m["gam"], 0.0, True, params=m["params"],
                       solver=m["solver"], precision=sg.PREC_MIXED)
         s.do_steps(25, 1e-2)
         info = ens.member_info(i)

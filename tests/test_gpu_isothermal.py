@@ -73,3 +73,25 @@ def test_isothermal_writers(tmp_path):
     with pytest.raises(sg.SplashError):
         s.get_light_curves()  # the isothermal class has none
     assert s.diagnostics()[4] == 0.0
+
+
+def test_isothermal_mixed_close_to_fp64():
+    """FP32 reconstruction and HLLE fluxes with the FP64 state, against the
+    FP64 isothermal path: shear layer on quad(5), 300 steps."""
+    import splash_gb300 as sg
+
+    mesh = mesh_of("quad", 5)
+    g = sg.Geometry(mesh)
+    U0 = _state(g, "shear", 2)
+    a = sg.MUSCL_HLLE(mesh, U0, 4, GAM)
+    b = sg.MUSCL_HLLE(mesh, U0, 4, GAM, precision=sg.PREC_MIXED)
+    a.do_steps(300, 1e-3)
+    b.do_steps(300, 1e-3)
+    Ua, Ub = a.get_state(), b.get_state()
+    area = g["area"]
+    l1 = np.sum(area * np.abs(Ub[:, 0] - Ua[:, 0])) / np.sum(area * np.abs(Ua[:, 0]))
+    assert l1 < 1e-5, l1
+    mom = np.sum(area[:, None] * np.abs(Ub[:, 1:] - Ua[:, 1:])) / np.sum(area[:, None] * np.abs(Ua[:, 1:]))
+    assert mom < 1e-4, mom
+    assert abs(b.time() - a.time()) <= 1e-6 * a.time()
+    assert not a.get_stop_check() and not b.get_stop_check()
