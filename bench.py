@@ -330,6 +330,55 @@ def adjoint_workload(sg, torch, steps=1000, checkpoint_every=50, level=6, seed=4
     return out
 
 
+def shear_workload(sg, torch, fp64_steps=20, mixed_steps=200, level=9, seed=2, dt0=1e-4):
+    """The large-mesh shear layer at reduced length: icosphere_hex(9)
+    (2,621,442 faces), MUSCL_HLLCplus, dim 5, no accretion, u_phi = 0.5
+    tanh(latitude / 0.05), Sigma = 1 + 1e-2 random Y_lm (l <= 8, seed 2),
+    Pi = Sigma^gam2d, do_step(1e-4) with the CFL clip.  Both precisions run
+    `fp64_steps` steps from the same state (face-updates/s of each and the
+    mixed state's error against FP64 after those steps); the mixed path then
+    runs `mixed_steps` more for its rate.  The 1000-step comparison of the
+    full workload is shear_check.py."""
+    gam = sg.initial_conditions.gam2d(4 / 3)
+    mesh = sg.icosphere_hex(level)
+    nf = 10 * 4 ** level + 2
+    t0 = time.perf_counter()
+    fp64 = sg.MUSCL_HLLCplus(mesh, np.ones((nf, 5)), 5, gam, 0.0, False, precision=sg.PREC_FP64)
+    r, area = fp64.face_geometry()
+    U0 = sg.initial_conditions.shear_layer(r, gam, seed=seed)
+    mixed = sg.MUSCL_HLLCplus(mesh, U0, 5, gam, 0.0, False, precision=sg.PREC_MIXED)
+    setup = time.perf_counter() - t0
+
+    def timed(s, n):
+        stream = torch.cuda.ExternalStream(s.stream())
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        s.do_steps(n, dt0)
+        b.record(stream)
+        b.synchronize()
+        return a.elapsed_time(b) / 1e3
+
+    for s in (fp64, mixed):
+        s.do_steps(3, dt0)
+        s.synchronize()
+        s.set_state(U0)
+    t64 = timed(fp64, fp64_steps)
+    t32 = timed(mixed, fp64_steps)
+    U64, U32 = fp64.get_state(), mixed.get_state()
+    t32b = timed(mixed, mixed_steps)
+    out = {"workload": f"icosphere_hex({level}) {nf} faces, HLLC+, shear layer, dt0={dt0} (CFL-clipped)",
+           "fp64": {"value": nf * fp64_steps / t64, "ms_per_step": t64 / fp64_steps * 1e3, "steps": fp64_steps},
+           "mixed": {"value": nf * mixed_steps / t32b, "ms_per_step": t32b / mixed_steps * 1e3,
+                     "steps": mixed_steps},
+           "unit": METRIC, "mixed_over_fp64": (nf * mixed_steps / t32b) / (nf * fp64_steps / t64),
+           "l1_rel_per_field_after_fp64_steps": l1_rel(U32, U64, area).tolist(),
+           "last_dt": fp64.last_dt(), "setup_s": setup}
+    fp64.close()
+    mixed.close()
+    return out
+
+
 def l1_rel(a, b, area):
     num = np.sum(area[:, None] * np.abs(a - b), axis=0)
     den = np.sum(area[:, None] * np.abs(b), axis=0)
@@ -417,6 +466,8 @@ def run_ours(args):
         line["ensemble"] = ensemble_workload(sg, torch)
     if not args.no_adjoint:
         line["adjoint"] = adjoint_workload(sg, torch)
+    if not args.no_shear:
+        line["shear_layer"] = shear_workload(sg, torch)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(geom, U0, gam)
     if rank == 0:
@@ -469,6 +520,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-shear", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

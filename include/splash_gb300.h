@@ -124,7 +124,7 @@ SPLASH_API const char* splash_version(void);
  * and, for the adiabatic solvers, then indexes past the state vector,
  * physics/adiabatic.hpp:26-30, Riemann_solvers/HLLC.hpp:208).  The
  * isothermal solver ignores omega_ns, accretion_on and params (its
- * constructor takes none of them) and runs in FP64.  Its reference path reads
+ * constructor takes none of them).  Its reference path reads
  * and writes a fifth state field and an uninitialised limiter variable
  * (MUSCL_base.hpp:203, 324, 368-370; isothermal.hpp:272, 307); the GPU path
  * is the defined form: no fifth field, CFL sound speed a = 1, etha_minus =
@@ -173,6 +173,12 @@ SPLASH_API int splash_set_state(splash_solver* s, const double* U);
 SPLASH_API int splash_diagnostics(splash_solver* s, double out[5]);
 /* Internal (space-filling-curve) position -> reference face id, [n_faces]. */
 SPLASH_API int splash_get_permutation(splash_solver* s, int* internal_to_ref);
+/* The solver's unit face centres fc/|fc| ([n_faces][3]) and face areas
+ * ([n_faces]) in reference face order (MUSCL_geometry.hpp:1069-1077 writes the
+ * same centres); either pointer may be NULL.  No counterpart member in the
+ * reference: an accessor so that a caller can build initial states without
+ * a second geometry build. */
+SPLASH_API int splash_face_geometry(splash_solver* s, double* unit_centres, double* area);
 
 /* ---- writers (physics/adiabatic.hpp:101-348) ---------------------------- */
 /* Each appends one line "t  v0 v1 ... " to `path` with the reference's

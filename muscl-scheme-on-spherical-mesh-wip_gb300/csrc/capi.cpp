@@ -613,6 +613,22 @@ int splash_get_permutation(splash_solver* h, int* internal_to_ref) {
   return SPLASH_OK;
 }
 
+int splash_face_geometry(splash_solver* h, double* unit_centres, double* area) {
+  Solver* s = reinterpret_cast<Solver*>(h);
+  if (!s) return fail(SPLASH_E_INVALID, "solver handle is NULL");
+  for (int i = 0; i < s->n_faces; ++i) {
+    if (unit_centres) {
+      const V3 fc = at3(s->wr_face_centers, i);
+      const V3 u = vdiv(fc, vnorm(fc));
+      unit_centres[3 * (size_t)i] = u.x;
+      unit_centres[3 * (size_t)i + 1] = u.y;
+      unit_centres[3 * (size_t)i + 2] = u.z;
+    }
+    if (area) area[i] = s->wr_area[i];
+  }
+  return SPLASH_OK;
+}
+
 // ---------------- writers (physics/adiabatic.hpp:101-348) ----------------
 static int open_append(std::ofstream& os, const char* path) {
   if (!path) return fail(SPLASH_E_INVALID, "path is NULL");

@@ -58,7 +58,7 @@ EXPORTED = (
     "splash_cfl_dt_noalloc",
     "splash_adjoint_create", "splash_adjoint_destroy", "splash_adjoint_forward",
     "splash_adjoint_backward", "splash_adjoint_run", "splash_tlm_run", "splash_adjoint_info",
-    "splash_adjoint_error_word", "splash_adjoint_dt_schedule",
+    "splash_adjoint_error_word", "splash_adjoint_dt_schedule", "splash_face_geometry",
 )
 
 
@@ -147,6 +147,7 @@ def library(path: str | os.PathLike | None = None) -> C.CDLL:
         "splash_adjoint_info": [vp, dp],
         "splash_adjoint_error_word": [vp, C.POINTER(C.c_uint32)],
         "splash_adjoint_dt_schedule": [vp, dp, C.c_int],
+        "splash_face_geometry": [vp, dp, dp],
     }.items():
         fn = getattr(lib, name)
         fn.argtypes = args
@@ -403,6 +404,13 @@ class Solver:
         out = np.zeros(5)
         _check(self._lib.splash_diagnostics(self.handle, _dptr(out)))
         return out
+
+    def face_geometry(self) -> tuple[np.ndarray, np.ndarray]:
+        """(unit face centres [F, 3], areas [F]) in reference face order."""
+        c = np.empty((self.n_faces, 3))
+        a = np.empty(self.n_faces)
+        _check(self._lib.splash_face_geometry(self.handle, _dptr(c), _dptr(a)))
+        return c, a
 
     def permutation(self) -> np.ndarray:
         p = np.empty(self.n_faces, dtype=np.int32)

@@ -57,13 +57,10 @@ def test_invalid_arguments_rejected_without_gpu():
     rc = lib.splash_create(C.byref(m), U5.ctypes.data_as(C.POINTER(C.c_double)), 5, 3.0, 0.0, 0,
                            C.byref(p), sg.SOLVER_HLLC, 0, 0, 0, C.byref(h))
     assert rc == 1
-    # the isothermal solver needs dim 4 and runs in FP64
+    # the isothermal solver needs dim 4
     rc = lib.splash_create(C.byref(m), U5.ctypes.data_as(C.POINTER(C.c_double)), 5, 1.25, 0.0, 0,
                            C.byref(p), sg.SOLVER_HLLE, 0, 0, 0, C.byref(h))
     assert rc == 5 and b"dim=5" in lib.splash_last_error()
-    rc = lib.splash_create(C.byref(m), U.ctypes.data_as(C.POINTER(C.c_double)), 4, 1.25, 0.0, 0,
-                           C.byref(p), sg.SOLVER_HLLE, sg.PREC_MIXED, 0, 0, C.byref(h))
-    assert rc == 5 and b"FP64" in lib.splash_last_error()
     # the adjoint needs a solver
     a = C.c_void_p()
     assert lib.splash_adjoint_create(None, 50, C.byref(a)) == 1
