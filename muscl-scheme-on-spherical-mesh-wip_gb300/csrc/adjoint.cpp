@@ -135,6 +135,7 @@ struct Adjoint {
     P.omega_acc_y = std::sin(par.tilt_angle) * par.omega_acc_abs;
     P.omega_acc_z = std::cos(par.tilt_angle) * par.omega_acc_abs;
     P.acc_rate = par.accretion_rate;
+    derive_params(P);
   }
   int upload_profile(const double* dtheta) {
     const std::vector<double> acc = accretion_source_fcn(fcn_h, n_faces, fpad, par, base->area_coeff,
@@ -203,6 +204,7 @@ int Adjoint::forward(const double* U0, const double* theta, int n, double dt0_, 
   int rc = upload_profile(nullptr);
   if (rc) return rc;
   P.total_mass = total_mass(U0);
+  derive_params(P);
   try {
     rc = ensure_capacity(n);
   } catch (const std::bad_alloc&) {
@@ -309,6 +311,7 @@ int Adjoint::tlm(const double* U0, const double* theta, const double* dU0, const
   int rc = upload_profile(dtheta);
   if (rc) return rc;
   P.total_mass = total_mass(U0);
+  derive_params(P);
   T.d_total_mass = dU0 ? total_mass(dU0) : 0.0;
   const double st_ = std::sin(par.tilt_angle), ct = std::cos(par.tilt_angle), om = par.omega_acc_abs;
   const double dr = dtheta ? dtheta[0] : 0.0, dti = dtheta ? dtheta[1] : 0.0, dom = dtheta ? dtheta[2] : 0.0;

@@ -383,6 +383,7 @@ int splash_create(const splash_mesh_desc* mesh, const double* U_in, int dim, dou
     P.accretion_on = s->accretion_on ? 1 : 0;
     P.friction_on = params->friction_on ? 1 : 0;
     P.solver = solver_kind;
+    splash::derive_params(P);
 
     const size_t fp = (size_t)s->fpad;
     const size_t PS = (size_t)s->max_slots * fp;
@@ -691,9 +692,13 @@ int splash_write_t_curl(splash_solver* h, const char* path) {
   if (s->S.uplus) {
     SPLASH_CUDA(cudaMemcpy(up.data(), s->S.uplus, up.size() * sizeof(double), cudaMemcpyDeviceToHost));
   } else {
+    // packed FP32 edge states: [PS][4] (Sigma, l) then the Pi plane
     std::vector<float> up32(splash::kDim * PS);
     SPLASH_CUDA(cudaMemcpy(up32.data(), s->S.uplus32, up32.size() * sizeof(float), cudaMemcpyDeviceToHost));
-    std::copy(up32.begin(), up32.end(), up.begin());
+    for (size_t q = 0; q < PS; ++q) {
+      for (int k = 0; k < 4; ++k) up[k * PS + q] = up32[4 * q + k];
+      up[4 * PS + q] = up32[4 * PS + q];
+    }
   }
   double t;
   if ((rc = splash_time(h, &t))) return rc;

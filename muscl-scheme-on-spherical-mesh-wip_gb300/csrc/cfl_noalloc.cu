@@ -149,6 +149,7 @@ extern "C" int splash_cfl_dt_noalloc(const double* U, const double* unit_centres
   P.omega_ns = omega_ns;
   P.alpha = alpha;
   P.h0 = h0;
+  derive_params(P);
   const int nb = (n_faces + kBlock - 1) / kBlock;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   candidates_kernel<<<nb, kBlock, 0, st>>>(U, unit_centres, area, n_faces, P, scratch);

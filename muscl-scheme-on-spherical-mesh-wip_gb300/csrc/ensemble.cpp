@@ -381,6 +381,7 @@ int splash_ensemble_create(const splash_member* members, int n, int device, int 
       P.accretion_on = acc_on ? 1 : 0;
       P.friction_on = m.params.friction_on ? 1 : 0;
       P.solver = m.solver_kind;
+      derive_params(P);
       // state, reference order -> internal planes
       std::vector<double> planes((size_t)fp * kDim, 0.0);
       for (int q = 0; q < nf; ++q)

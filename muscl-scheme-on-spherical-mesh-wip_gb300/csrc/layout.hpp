@@ -37,7 +37,28 @@ struct PhysParams {
   int accretion_on;
   int friction_on;
   int solver;            // 1 HLLE_p, 2 HLLC, 3 HLLC+, 4 HLLE (isothermal)
+  // derived once on the host (derive_params) so that no thread re-derives a
+  // uniform constant: gam3d / (2 gam3d - 1) with gam3d = 1 / (2 - gam)
+  // (physics/adiabatic.hpp:563-566), and FP32 copies for the mixed path
+  double fric_k;
+  float gam_f, e_acc_f, alpha_f, omega_ns_f;
+  float omega_acc_f[3];
+  float depletion_f;     // -(acc_rate 4 pi) / total_mass (adiabatic.hpp:430-436)
 };
+
+// Fills the derived fields of P from its primary ones.
+inline void derive_params(PhysParams& P) {
+  const double gam3d = 1 / (2 - P.gam);
+  P.fric_k = gam3d / (2 * gam3d - 1);
+  P.gam_f = (float)P.gam;
+  P.e_acc_f = (float)P.e_acc;
+  P.alpha_f = (float)P.alpha;
+  P.omega_ns_f = (float)P.omega_ns;
+  P.omega_acc_f[0] = (float)P.omega_acc_x;
+  P.omega_acc_f[1] = (float)P.omega_acc_y;
+  P.omega_acc_f[2] = (float)P.omega_acc_z;
+  P.depletion_f = (P.total_mass != 0) ? (float)(-(P.acc_rate * 4 * 3.14159265358979323846) / P.total_mass) : 0.f;
+}
 
 constexpr int kSolverIsoHLLE = 4;  // the isothermal solver (4 state fields)
 
@@ -97,8 +118,8 @@ struct DevState {
   double* W0;     // (Sigma, l, Pi) of U, kDim planes
   double* W1;     // (Sigma, l, Pi) after stage 1, kDim planes
   double* uplus;  // reconstructed edge states, kDim * max_slots planes of fpad
-  float* W32;     // mixed path: (Sigma, l, Pi) in FP32, kDim planes
-  float* uplus32; // mixed path: edge states (Sigma, l, Pi) in FP32
+  float* W32;     // mixed path: (Sigma, l, Pi) in FP32: [fpad] float4 (Sigma, l), then a Pi plane
+  float* uplus32; // mixed path: edge states, same packing over max_slots * fpad slots
   double* partial;  // per-block partial records (kPartialStride doubles)
   double* scal;   // device scalars, see ScalarSlot
   unsigned int* err;  // stop bits
@@ -121,6 +142,7 @@ enum ScalarSlot : int {
   kScExtraDt = 3,  // extra_dt_constr of the step's input state
   kScMass = 4,     // 4..8: sum Sigma A, l_x A, l_y A, l_z A, E A of the step's input state
   kScDt0 = 9,      // dt0 requested by the caller
+  kScDtF = 10,     // mixed path: (float dt, float dt/2) packed in one slot
   kScCount = 16
 };
 

@@ -310,10 +310,10 @@ SPLASH_HD void dt_candidates(const double* u, D3 r, double area, const PhysParam
   const D3 vel0 = cross3(omega0, r);
   const double nvel = norm3(vel);
   const double press = pressure(u, nvel, P.gam);
-  const double gam3d = 1 / (2 - P.gam);
   const double GM = 0.217909;
   const double g_eff = GM - nvel * nvel;
-  const double rho = gam3d / (2 * gam3d - 1) * g_eff * u[0] * u[0] / press;
+  // P.fric_k = gam3d / (2 gam3d - 1), gam3d = 1 / (2 - gam), the same IEEE value
+  const double rho = P.fric_k * g_eff * u[0] * u[0] / press;
   dmin = 0.01 * u[0] / (P.alpha * rho * norm3(sub(vel, vel0)));
 #pragma unroll
   for (int k = 0; k < 5; ++k) sums[k] = u[k] * area;
@@ -381,8 +381,7 @@ SPLASH_HD void source_term(const T* w, const D3& fcn, const SrcParams<Q>& sp, co
   if (beta > beta_ceil) beta = T(beta_ceil);
   res[4] -= g_eff / kappa * (1 - beta);
   if (P.friction_on) {
-    const double gam3d = 1 / (2 - P.gam);
-    const T rho = gam3d / (2 * gam3d - 1) * g_eff * w[0] * w[0] / w[4];
+    const T rho = P.fric_k * g_eff * w[0] * w[0] / w[4];  // fric_k = gam3d / (2 gam3d - 1)
     const D3 omega0 = d3(0, 0, P.omega_ns);
     const D3 vel0 = cross3(omega0, fcn);
     const T dv = norm3(sub(vel, vel0));

@@ -33,6 +33,26 @@ constexpr int kBlock = 128;
 __device__ __forceinline__ F3 plane3f(const float* p, int stride, int i) {
   return F3{p[i], p[stride + i], p[2 * stride + i]};
 }
+// Packed FP32 states (face states W32 and edge states uplus32): entry i of
+// an n-entry array is a float4 (Sigma, l_x, l_y, l_z) at base + 4 i and Pi
+// at base + 4 n + i, so a gather of one state is one 16-byte load (plus one
+// for Pi; the isothermal solver needs none).
+__device__ __forceinline__ float4 ld4(const float* base, int i) {
+  return __ldg(reinterpret_cast<const float4*>(base) + i);
+}
+__device__ __forceinline__ void ld5(const float* base, int n, int i, float* v) {
+  const float4 a = ld4(base, i);
+  v[0] = a.x;
+  v[1] = a.y;
+  v[2] = a.z;
+  v[3] = a.w;
+  v[4] = __ldg(base + 4 * (size_t)n + i);
+}
+__device__ __forceinline__ void st5(float* base, int n, int i, const float* v) {
+  reinterpret_cast<float4*>(base)[i] = make_float4(v[0], v[1], v[2], v[3]);
+  base[4 * (size_t)n + i] = v[4];
+}
+
 __device__ __forceinline__ f64::D3 plane3d(const double* p, int stride, int i) {
   return f64::D3{p[i], p[stride + i], p[2 * stride + i]};
 }
@@ -81,9 +101,8 @@ __device__ __forceinline__ double pressure_recover(const double* u, f64::D3 r, d
 }
 
 __device__ __forceinline__ void store_w32(float* W32, int fp, int f, const double* u, double p) {
-#pragma unroll
-  for (int k = 0; k < 4; ++k) W32[k * fp + f] = (float)u[k];
-  W32[4 * fp + f] = (float)p;
+  const float v[kDim] = {(float)u[0], (float)u[1], (float)u[2], (float)u[3], (float)p};
+  st5(W32, fp, f, v);
 }
 
 // dt candidates in FP64 with one sqrt and one division: the CFL maximum is
@@ -101,10 +120,8 @@ __device__ __forceinline__ void dt_candidates_sq(const double* u, f64::D3 r, dou
   const double vy = -c.y * inv_rho - P.omega_ns * r.x;
   const double vz = -c.z * inv_rho;
   const double dv = sqrt(vx * vx + vy * vy + vz * vz);
-  const double gam3d = 1 / (2 - P.gam);
-  const double k = gam3d / (2 * gam3d - 1);
   const double g_eff = 0.217909 - v2;
-  dmin = 0.01 * p / (P.alpha * k * g_eff * u[0] * dv);
+  dmin = 0.01 * p / (P.alpha * P.fric_k * g_eff * u[0] * dv);
 }
 
 // physics/adiabatic.hpp:396-541 in FP32, except the accretion mass source
@@ -114,20 +131,20 @@ __device__ __forceinline__ void source_f32(const float* w, F3 fcn, float acc0, c
 #pragma unroll
   for (int i = 0; i < kDim; ++i) res[i] = 0.f;
   if (!P.accretion_on) return;
-  const float gam = (float)P.gam;
+  const float gam = P.gam_f;
   const F3 vel = scal(cross3(fcn, f3(w[1], w[2], w[3])), -1.0f / w[0]);
-  const F3 omega_acc = f3((float)P.omega_acc_x, (float)P.omega_acc_y, (float)P.omega_acc_z);
+  const F3 omega_acc = f3(P.omega_acc_f[0], P.omega_acc_f[1], P.omega_acc_f[2]);
   const F3 omxr = cross3(omega_acc, fcn);
   const F3 rxo = cross3(fcn, omxr);
   res[1] = acc0 * rxo.x;
   res[2] = acc0 * rxo.y;
   res[3] = acc0 * rxo.z;
   const F3 dvo = sub(omxr, vel);
-  res[4] = acc0 * ((float)P.e_acc + 0.5f * dot3(dvo, dvo));
+  res[4] = acc0 * (P.e_acc_f + 0.5f * dot3(dvo, dvo));
   const F3 rxv = cross3(fcn, vel);
   const float v2 = dot3(vel, vel);
   if (!P.friction_on) {
-    const float dmdt = (float)(-(P.acc_rate * 4 * M_PI) / P.total_mass) * w[0];
+    const float dmdt = P.depletion_f * w[0];
     res[0] += dmdt;
     res[1] += dmdt * rxv.x;
     res[2] += dmdt * rxv.y;
@@ -158,10 +175,10 @@ __device__ __forceinline__ void source_f32(const float* w, F3 fcn, float acc0, c
   if (P.friction_on) {
     const float gam3d = 1.f / (2.f - gam);
     const float rho = gam3d / (2.f * gam3d - 1.f) * g_eff * w[0] * w[0] / w[4];
-    const F3 vel0 = cross3(f3(0.f, 0.f, (float)P.omega_ns), fcn);
+    const F3 vel0 = cross3(f3(0.f, 0.f, P.omega_ns_f), fcn);
     const F3 dv = sub(vel, vel0);
     const float dvn = norm3(dv);
-    const float ar = (float)P.alpha * rho * dvn;
+    const float ar = P.alpha_f * rho * dvn;
     const F3 wr = scal(dv, -ar);
     const F3 l_fr = cross3(fcn, wr);
     res[1] += l_fr.x;
@@ -181,9 +198,8 @@ __device__ __forceinline__ void source_f32(const float* w, F3 fcn, float acc0, c
 // isothermal sound speed); no extra constraint (isothermal.hpp:262-267).
 __device__ __forceinline__ void iso_w32_candidates(const double* u, f64::D3 r, float* W32, int fp, int f,
                                                    double& vmax2, double& dmin) {
-#pragma unroll
-  for (int k = 0; k < 4; ++k) W32[k * fp + f] = (float)u[k];
-  W32[4 * fp + f] = 0.f;
+  const float v[kDim] = {(float)u[0], (float)u[1], (float)u[2], (float)u[3], 0.f};
+  st5(W32, fp, f, v);
   const f64::D3 c = f64::cross3(r, f64::d3(u[1], u[2], u[3]));
   const double inv_rho = 1.0 / u[0];
   const double v2 = (c.x * c.x + c.y * c.y + c.z * c.z) * inv_rho * inv_rho;
@@ -237,6 +253,7 @@ __device__ __forceinline__ void finalize_body(const DevState& S, const PhysParam
   if (dt > P.h0 * 0.1 / max_vel) dt = P.h0 * 0.1 / max_vel;
   if (dt > extra) dt = extra;
   S.scal[kScDt] = dt;
+  *reinterpret_cast<float2*>(S.scal + kScDtF) = make_float2((float)dt, (float)(dt / 2));
   S.scal[kScDt0] = dt0;
   S.scal[kScMaxVel] = max_vel;
   S.scal[kScExtraDt] = extra;
@@ -259,59 +276,66 @@ __device__ __forceinline__ void recon_body(const DevGeomMixed& G, const DevState
   const int fp = G.fpad;
   const int PS = G.max_slots * fp;
   const float* __restrict__ W = S.W32;
-  const float dt = (float)S.scal[kScDt];
-  const float gam = (float)P.gam;
-  if (P.solver == kSolverIsoHLLE) {
-    // isothermal: 4 fields, superbee limiter with the Courant factor
-    // (a + v.n) dt arc / area (physics/isothermal.hpp:269-320)
-    float w[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) w[k] = W[k * fp + f];
-    const int s = j * fp + f;
-    const int ia = G.sten[s], ib = G.sten[PS + s], ic = G.sten[2 * PS + s], id = G.sten[3 * PS + s];
-    const float bp0 = G.beta[s], bp1 = G.beta[PS + s], bm0 = G.beta[2 * PS + s], bm1 = G.beta[3 * PS + s];
-    const float ihp = G.inv_h[s], ihm = G.inv_h[PS + s], bmd = G.bm[s];
-    const F3 vel = scal(cross3(plane3f(G.ec, PS, s), f3(w[1], w[2], w[3])), -1.0f / w[0]);
-    const float nu_plus = (1.f + dot3(vel, plane3f(G.en, PS, s))) * dt * G.arc_a[s];
-    const float eta = G.eta[PS + s];
-    const float sb_scale = eta * 2.f / ((float)(2 * n) * nu_plus);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const float* Wk = W + k * fp;
-      const float pp = (bp0 * Wk[ia] + bp1 * Wk[ib] - w[k]) * ihp;
-      const float pm = (w[k] - (bm0 * Wk[ic] + bm1 * Wk[id])) * ihm;
-      const float lim = iso_limiter_field(pm / pp, eta, sb_scale);
-      S.uplus32[k * PS + s] = w[k] + pp * lim * bmd;
-    }
-    return;
-  }
-  float w[kDim];
-#pragma unroll
-  for (int k = 0; k < kDim; ++k) w[k] = W[k * fp + f];
-  const float inv_rho = -1.0f / w[0];
-  const float c = sqrtf(gam * w[4] / w[0]);
+  const float dt = reinterpret_cast<const float2*>(S.scal + kScDtF)->x;
   const int s = j * fp + f;
   const int ia = G.sten[s], ib = G.sten[PS + s], ic = G.sten[2 * PS + s], id = G.sten[3 * PS + s];
   const float bp0 = G.beta[s], bp1 = G.beta[PS + s], bm0 = G.beta[2 * PS + s], bm1 = G.beta[3 * PS + s];
   const float ihp = G.inv_h[s], ihm = G.inv_h[PS + s], bmd = G.bm[s];
   const F3 ec = plane3f(G.ec, PS, s);
   const F3 en = plane3f(G.en, PS, s);
+  // the face and its four stencil faces: one 16-byte gather each for
+  // (Sigma, l), one more each for Pi (adiabatic only)
+  const float4 w4 = ld4(W, f), a4 = ld4(W, ia), b4 = ld4(W, ib), c4 = ld4(W, ic), d4 = ld4(W, id);
+  const float w[4] = {w4.x, w4.y, w4.z, w4.w};
+  const float wa[4] = {a4.x, a4.y, a4.z, a4.w}, wb[4] = {b4.x, b4.y, b4.z, b4.w};
+  const float wc[4] = {c4.x, c4.y, c4.z, c4.w}, wd[4] = {d4.x, d4.y, d4.z, d4.w};
+  float4 o;
+  float* up = reinterpret_cast<float*>(&o);
+  if (P.solver == kSolverIsoHLLE) {
+    // isothermal: 4 fields, superbee limiter with the Courant factor
+    // (a + v.n) dt arc / area (physics/isothermal.hpp:269-320)
+    const F3 vel = scal(cross3(ec, f3(w[1], w[2], w[3])), -1.0f / w[0]);
+    const float nu_plus = (1.f + dot3(vel, en)) * dt * G.arc_a[s];
+    const float eta = G.eta[PS + s];
+    const float sb_scale = eta * 2.f / ((float)(2 * n) * nu_plus);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const float pp = (bp0 * wa[k] + bp1 * wb[k] - w[k]) * ihp;
+      const float pm = (w[k] - (bm0 * wc[k] + bm1 * wd[k])) * ihm;
+      const float lim = iso_limiter_field(pm / pp, eta, sb_scale);
+      up[k] = w[k] + pp * lim * bmd;
+    }
+    reinterpret_cast<float4*>(S.uplus32)[s] = o;
+    return;
+  }
+  const float* __restrict__ Wp = W + 4 * (size_t)fp;
+  const float wp = __ldg(Wp + f);
+  const float gam = P.gam_f;
+  const float inv_rho = -1.0f / w[0];
+  const float c = sqrtf(gam * wp / w[0]);
   const F3 vel = scal(cross3(ec, f3(w[1], w[2], w[3])), inv_rho);
   const float nu_plus = (c + dot3(vel, en)) * dt * G.arc_a[s];
   const float eta_p = G.eta[s];
   const float sb_scale = G.eta[PS + s] / ((float)(2 * n) * nu_plus);
 #pragma unroll
-  for (int k = 0; k < kDim; ++k) {
-    const float* Wk = W + k * fp;
-    const float pp = (bp0 * Wk[ia] + bp1 * Wk[ib] - w[k]) * ihp;
-    const float pm = (w[k] - (bm0 * Wk[ic] + bm1 * Wk[id])) * ihm;
-    const float r = pm / pp;
-    const float lim = limiter_field(r, nu_plus, eta_p, sb_scale);
-    S.uplus32[k * PS + s] = w[k] + pp * lim * bmd;
+  for (int k = 0; k < 4; ++k) {
+    const float pp = (bp0 * wa[k] + bp1 * wb[k] - w[k]) * ihp;
+    const float pm = (w[k] - (bm0 * wc[k] + bm1 * wd[k])) * ihm;
+    const float lim = limiter_field(pm / pp, nu_plus, eta_p, sb_scale);
+    up[k] = w[k] + pp * lim * bmd;
+  }
+  reinterpret_cast<float4*>(S.uplus32)[s] = o;
+  {
+    const float pp = (bp0 * __ldg(Wp + ia) + bp1 * __ldg(Wp + ib) - wp) * ihp;
+    const float pm = (wp - (bm0 * __ldg(Wp + ic) + bm1 * __ldg(Wp + id))) * ihm;
+    const float lim = limiter_field(pm / pp, nu_plus, eta_p, sb_scale);
+    S.uplus32[4 * (size_t)PS + s] = wp + pp * lim * bmd;
   }
 }
 
-__global__ void __launch_bounds__(kBlock) reconstruct_kernel(DevGeomMixed G, DevState S, PhysParams P) {
+// at most 51 registers (10 blocks of 128 per SM): the gathers need warps in
+// flight more than registers
+__global__ void __launch_bounds__(kBlock, 10) reconstruct_kernel(DevGeomMixed G, DevState S, PhysParams P) {
   recon_body(G, S, P, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
 }
 
@@ -337,10 +361,9 @@ __device__ __forceinline__ void flux_body(const DevGeomMixed& G, const DevState&
   const int f = face_begin + tx;
   const int fp = G.fpad;
   const int PS = G.max_slots * fp;
-  const double dt = S.scal[kScDt];
-  const double dt_here = (STAGE == 1) ? dt / 2 : dt;
-  const float dtf = (float)dt_here;
-  const float gam = (float)P.gam;
+  const float2 dtf2 = *reinterpret_cast<const float2*>(S.scal + kScDtF);
+  const float dtf = (STAGE == 1) ? dtf2.y : dtf2.x;
+  const float gam = P.gam_f;
   if (tx == 0 && ty == 0) sbits = 0;
   __syncthreads();
   {
@@ -350,11 +373,8 @@ __device__ __forceinline__ void flux_body(const DevGeomMixed& G, const DevState&
       const int s = ty * fp + f;
       const int rv = G.rev[s];
       float uL[kDim], uR[kDim];
-#pragma unroll
-      for (int k = 0; k < kDim; ++k) {
-        uL[k] = S.uplus32[k * PS + s];
-        uR[k] = S.uplus32[k * PS + rv];
-      }
+      ld5(S.uplus32, PS, s, uL);
+      ld5(S.uplus32, PS, rv, uR);
       SlotGeomF g;
       g.ec = plane3f(G.ec, PS, s);
       g.en = plane3f(G.en, PS, s);
@@ -376,8 +396,7 @@ __device__ __forceinline__ void flux_body(const DevGeomMixed& G, const DevState&
   double vmax = 0.0, dmin = 1e20;
   if (f < G.n_faces) {
     float w[kDim], src[kDim];
-#pragma unroll
-    for (int k = 0; k < kDim; ++k) w[k] = S.W32[k * fp + f];
+    ld5(S.W32, fp, f, w);
     const F3 fcn32 = plane3f(G.fcn32, fp, f);
     const double acc0 = G.acc_src[f];
     source_f32(w, fcn32, (float)acc0, P, src);
@@ -398,7 +417,11 @@ __device__ __forceinline__ void flux_body(const DevGeomMixed& G, const DevState&
     double u[kDim];
 #pragma unroll
     for (int k = 0; k < kDim; ++k) u[k] = S.U[k * fp + f] + (double)(acc[k].hi + acc[k].lo);
-    if (P.accretion_on) u[0] += dt_here * acc0;  // accretion mass source in FP64
+    if (P.accretion_on) {  // accretion mass source in FP64
+      const double dt = S.scal[kScDt];
+      const double dt_here = (STAGE == 1) ? dt / 2 : dt;
+      u[0] += dt_here * acc0;
+    }
     if (u[0] < 1e-8) u[0] = 1e-8;
     const f64::D3 r = plane3d(G.fcn, fp, f);
     if (P.solver == kSolverIsoHLLE) {
@@ -456,7 +479,7 @@ __global__ void ens_finalize_kernel(const EnsInstance* __restrict__ inst, int n,
   if (i < n) finalize_body(inst[i].S, inst[i].P, dt0);
 }
 
-__global__ void __launch_bounds__(256) ens_reconstruct_kernel(const EnsInstance* __restrict__ inst,
+__global__ void __launch_bounds__(256, 4) ens_reconstruct_kernel(const EnsInstance* __restrict__ inst,
                                                               const int2* __restrict__ tiles) {
   const int2 t = tiles[blockIdx.x];
   const EnsInstance& I = inst[t.x];

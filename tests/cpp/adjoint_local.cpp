@@ -36,6 +36,7 @@ PhysParams phys_from(const double* p, int accretion_on, int friction_on, int sol
   P.accretion_on = accretion_on;
   P.friction_on = friction_on;
   P.solver = solver;
+  derive_params(P);
   return P;
 }
 
