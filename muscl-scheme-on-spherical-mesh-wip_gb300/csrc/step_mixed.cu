@@ -33,6 +33,18 @@ constexpr int kBlock = 128;
 __device__ __forceinline__ F3 plane3f(const float* p, int stride, int i) {
   return F3{p[i], p[stride + i], p[2 * stride + i]};
 }
+// Programmatic dependent launch.  The step's kernels are launched with
+// programmatic stream serialization: a kernel may start while its
+// predecessor drains, loads what does not depend on it (stencil indices,
+// geometry), then waits in griddep_wait() for the predecessor grid to
+// complete and its writes to be visible.  Every read of state and every
+// write comes after the wait, so no kernel overwrites what its predecessor
+// is still reading.  Without a programmatic predecessor the wait returns at
+// once.  launch_dependents lets the next kernel start as soon as every
+// block of this one has begun.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;"); }
+
 // Packed FP32 states (face states W32 and edge states uplus32): entry i of
 // an n-entry array is a float4 (Sigma, l_x, l_y, l_z) at base + 4 i and Pi
 // at base + 4 n + i, so a gather of one state is one 16-byte load (plus one
@@ -243,6 +255,7 @@ __global__ void reset_keys_kernel(unsigned long long* keys) {
 // dt = min(dt0, 0.1 h0 / max_vel, extra_dt) (MUSCL_base.hpp:100-115), time,
 // and a fresh start for the keys the step's stage-2 launch will fold into.
 __device__ __forceinline__ void finalize_body(const DevState& S, const PhysParams& P, double dt0) {
+  griddep_wait();
   const double max_vel = sqrt(key_value(S.keys[0]));
   double extra = key_value(S.keys[1]);
   if (extra < 0) {
@@ -262,7 +275,10 @@ __device__ __forceinline__ void finalize_body(const DevState& S, const PhysParam
   S.keys[1] = order_key(1e20);
 }
 
-__global__ void finalize_kernel(DevState S, PhysParams P, double dt0) { finalize_body(S, P, dt0); }
+__global__ void finalize_kernel(DevState S, PhysParams P, double dt0) {
+  griddep_launch_dependents();
+  finalize_body(S, P, dt0);
+}
 
 // find_U_edges (MUSCL_base.hpp:361-434) in FP32; edge field 4 stays Pi.
 // One thread per (face, slot): blockIdx.y is the slot plane, so a warp reads
@@ -276,13 +292,15 @@ __device__ __forceinline__ void recon_body(const DevGeomMixed& G, const DevState
   const int fp = G.fpad;
   const int PS = G.max_slots * fp;
   const float* __restrict__ W = S.W32;
-  const float dt = reinterpret_cast<const float2*>(S.scal + kScDtF)->x;
   const int s = j * fp + f;
   const int ia = G.sten[s], ib = G.sten[PS + s], ic = G.sten[2 * PS + s], id = G.sten[3 * PS + s];
   const float bp0 = G.beta[s], bp1 = G.beta[PS + s], bm0 = G.beta[2 * PS + s], bm1 = G.beta[3 * PS + s];
   const float ihp = G.inv_h[s], ihm = G.inv_h[PS + s], bmd = G.bm[s];
   const F3 ec = plane3f(G.ec, PS, s);
   const F3 en = plane3f(G.en, PS, s);
+  const float arc_a = G.arc_a[s], eta_p = G.eta[s], eta_m = G.eta[PS + s];
+  griddep_wait();
+  const float dt = reinterpret_cast<const float2*>(S.scal + kScDtF)->x;
   // the face and its four stencil faces: one 16-byte gather each for
   // (Sigma, l), one more each for Pi (adiabatic only)
   const float4 w4 = ld4(W, f), a4 = ld4(W, ia), b4 = ld4(W, ib), c4 = ld4(W, ic), d4 = ld4(W, id);
@@ -295,8 +313,8 @@ __device__ __forceinline__ void recon_body(const DevGeomMixed& G, const DevState
     // isothermal: 4 fields, superbee limiter with the Courant factor
     // (a + v.n) dt arc / area (physics/isothermal.hpp:269-320)
     const F3 vel = scal(cross3(ec, f3(w[1], w[2], w[3])), -1.0f / w[0]);
-    const float nu_plus = (1.f + dot3(vel, en)) * dt * G.arc_a[s];
-    const float eta = G.eta[PS + s];
+    const float nu_plus = (1.f + dot3(vel, en)) * dt * arc_a;
+    const float eta = eta_m;
     const float sb_scale = eta * 2.f / ((float)(2 * n) * nu_plus);
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
@@ -314,9 +332,8 @@ __device__ __forceinline__ void recon_body(const DevGeomMixed& G, const DevState
   const float inv_rho = -1.0f / w[0];
   const float c = sqrtf(gam * wp / w[0]);
   const F3 vel = scal(cross3(ec, f3(w[1], w[2], w[3])), inv_rho);
-  const float nu_plus = (c + dot3(vel, en)) * dt * G.arc_a[s];
-  const float eta_p = G.eta[s];
-  const float sb_scale = G.eta[PS + s] / ((float)(2 * n) * nu_plus);
+  const float nu_plus = (c + dot3(vel, en)) * dt * arc_a;
+  const float sb_scale = eta_m / ((float)(2 * n) * nu_plus);
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     const float pp = (bp0 * wa[k] + bp1 * wb[k] - w[k]) * ihp;
@@ -336,6 +353,7 @@ __device__ __forceinline__ void recon_body(const DevGeomMixed& G, const DevState
 // at most 51 registers (10 blocks of 128 per SM): the gathers need warps in
 // flight more than registers
 __global__ void __launch_bounds__(kBlock, 10) reconstruct_kernel(DevGeomMixed G, DevState S, PhysParams P) {
+  griddep_launch_dependents();
   recon_body(G, S, P, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
 }
 
@@ -361,31 +379,39 @@ __device__ __forceinline__ void flux_body(const DevGeomMixed& G, const DevState&
   const int f = face_begin + tx;
   const int fp = G.fpad;
   const int PS = G.max_slots * fp;
-  const float2 dtf2 = *reinterpret_cast<const float2*>(S.scal + kScDtF);
-  const float dtf = (STAGE == 1) ? dtf2.y : dtf2.x;
   const float gam = P.gam_f;
   if (tx == 0 && ty == 0) sbits = 0;
+  // the slot's geometry does not depend on the predecessor kernel
+  const bool active = f < G.n_faces && ty < G.nslots[f];
+  const int s = ty * fp + f;
+  int rv = 0;
+  SlotGeomF g;
+  float coef = 0.f;
+  if (active) {
+    rv = G.rev[s];
+    g.ec = plane3f(G.ec, PS, s);
+    g.en = plane3f(G.en, PS, s);
+    g.nxr = plane3f(G.nxr, PS, s);
+    coef = G.coef[s];
+  }
+  griddep_wait();
+  const float2 dtf2 = *reinterpret_cast<const float2*>(S.scal + kScDtF);
+  const float dtf = (STAGE == 1) ? dtf2.y : dtf2.x;
   __syncthreads();
   {
     float F[kDim] = {0.f, 0.f, 0.f, 0.f, 0.f};
     float cf = 0.f;
-    if (f < G.n_faces && ty < G.nslots[f]) {
-      const int s = ty * fp + f;
-      const int rv = G.rev[s];
+    if (active) {
       float uL[kDim], uR[kDim];
       ld5(S.uplus32, PS, s, uL);
       ld5(S.uplus32, PS, rv, uR);
-      SlotGeomF g;
-      g.ec = plane3f(G.ec, PS, s);
-      g.en = plane3f(G.en, PS, s);
-      g.nxr = plane3f(G.nxr, PS, s);
       unsigned bits = (P.solver == kSolverIsoHLLE) ? iso_flux_star(uL, uR, g, F)
                                                    : flux_star(uL, uR, g, gam, P.solver, F);
 #pragma unroll
       for (int k = 0; k < kDim; ++k)
         if (isnan(F[k])) bits |= 1u;
       if (bits) atomicOr(&sbits, bits);
-      cf = dtf * G.coef[s];
+      cf = dtf * coef;
     }
 #pragma unroll
     for (int k = 0; k < kDim; ++k) contrib[ty][k][tx] = -cf * F[k];
@@ -452,6 +478,7 @@ template <int STAGE>
 __global__ void __launch_bounds__(kFaceTile * kMaxSlotLanes) flux_update_kernel(DevGeomMixed G, DevState S,
                                                                                 PhysParams P) {
   __shared__ FluxShared sh;
+  griddep_launch_dependents();
   flux_body<STAGE>(G, S, P, blockIdx.x * kFaceTile, sh);
 }
 
@@ -475,12 +502,14 @@ __global__ void ens_reset_keys_kernel(const EnsInstance* __restrict__ inst, int 
 }
 
 __global__ void ens_finalize_kernel(const EnsInstance* __restrict__ inst, int n, double dt0) {
+  griddep_launch_dependents();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) finalize_body(inst[i].S, inst[i].P, dt0);
 }
 
 __global__ void __launch_bounds__(256, 4) ens_reconstruct_kernel(const EnsInstance* __restrict__ inst,
                                                               const int2* __restrict__ tiles) {
+  griddep_launch_dependents();
   const int2 t = tiles[blockIdx.x];
   const EnsInstance& I = inst[t.x];
   recon_body(I.G, I.S, I.P, t.y + threadIdx.x, blockIdx.y);
@@ -490,6 +519,7 @@ template <int STAGE>
 __global__ void __launch_bounds__(kFaceTile * kMaxSlotLanes) ens_flux_kernel(
     const EnsInstance* __restrict__ inst, const int2* __restrict__ tiles) {
   __shared__ FluxShared sh;
+  griddep_launch_dependents();
   const int2 t = tiles[blockIdx.x];
   const EnsInstance& I = inst[t.x];
   flux_body<STAGE>(I.G, I.S, I.P, t.y, sh);
@@ -513,23 +543,45 @@ cudaError_t mixed_prepare(const DevGeomMixed& G, const DevState& S, const PhysPa
   return cudaGetLastError();
 }
 
+namespace {
+// A launch with programmatic stream serialization (see griddep_wait).
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+}  // namespace
+
 cudaError_t mixed_step(const DevGeomMixed& G, const DevState& S, const PhysParams& P, double dt0,
                        cudaStream_t st, cudaEvent_t* ev) {
   const int ntile = (G.n_faces + mx::kFaceTile - 1) / mx::kFaceTile;
   const dim3 rgrid(mx::blocks_for(G.n_faces), G.max_slots);
   const dim3 fblock(mx::kFaceTile, G.max_slots);
+  cudaError_t e = cudaSuccess;
+  auto chk = [&](cudaError_t r) {
+    if (e == cudaSuccess) e = r;
+  };
   if (ev) cudaEventRecord(ev[0], st);
-  mx::finalize_kernel<<<1, 1, 0, st>>>(S, P, dt0);
+  chk(launch_pdl(mx::finalize_kernel, dim3(1), dim3(1), st, S, P, dt0));
   if (ev) cudaEventRecord(ev[1], st);
-  mx::reconstruct_kernel<<<rgrid, mx::kBlock, 0, st>>>(G, S, P);
+  chk(launch_pdl(mx::reconstruct_kernel, rgrid, dim3(mx::kBlock), st, G, S, P));
   if (ev) cudaEventRecord(ev[2], st);
-  mx::flux_update_kernel<1><<<ntile, fblock, 0, st>>>(G, S, P);
+  chk(launch_pdl(mx::flux_update_kernel<1>, dim3(ntile), fblock, st, G, S, P));
   if (ev) cudaEventRecord(ev[3], st);
-  mx::reconstruct_kernel<<<rgrid, mx::kBlock, 0, st>>>(G, S, P);
+  chk(launch_pdl(mx::reconstruct_kernel, rgrid, dim3(mx::kBlock), st, G, S, P));
   if (ev) cudaEventRecord(ev[4], st);
-  mx::flux_update_kernel<2><<<ntile, fblock, 0, st>>>(G, S, P);
+  chk(launch_pdl(mx::flux_update_kernel<2>, dim3(ntile), fblock, st, G, S, P));
   if (ev) cudaEventRecord(ev[5], st);
-  return cudaGetLastError();
+  return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 cudaError_t ensemble_prepare(const EnsInstance* inst, int n_inst, const int2* ftiles, int n_ftiles,
@@ -544,12 +596,16 @@ cudaError_t ensemble_step(const EnsInstance* inst, int n_inst, const int2* rtile
                           cudaStream_t st) {
   const dim3 rgrid(n_rtiles, max_slots);
   const dim3 fblock(mx::kFaceTile, max_slots);
-  mx::ens_finalize_kernel<<<(n_inst + 127) / 128, 128, 0, st>>>(inst, n_inst, dt0);
-  mx::ens_reconstruct_kernel<<<rgrid, recon_width, 0, st>>>(inst, rtiles);
-  mx::ens_flux_kernel<1><<<n_ftiles, fblock, 0, st>>>(inst, ftiles);
-  mx::ens_reconstruct_kernel<<<rgrid, recon_width, 0, st>>>(inst, rtiles);
-  mx::ens_flux_kernel<2><<<n_ftiles, fblock, 0, st>>>(inst, ftiles);
-  return cudaGetLastError();
+  cudaError_t e = cudaSuccess;
+  auto chk = [&](cudaError_t r) {
+    if (e == cudaSuccess) e = r;
+  };
+  chk(launch_pdl(mx::ens_finalize_kernel, dim3((n_inst + 127) / 128), dim3(128), st, inst, n_inst, dt0));
+  chk(launch_pdl(mx::ens_reconstruct_kernel, rgrid, dim3(recon_width), st, inst, rtiles));
+  chk(launch_pdl(mx::ens_flux_kernel<1>, dim3(n_ftiles), fblock, st, inst, ftiles));
+  chk(launch_pdl(mx::ens_reconstruct_kernel, rgrid, dim3(recon_width), st, inst, rtiles));
+  chk(launch_pdl(mx::ens_flux_kernel<2>, dim3(n_ftiles), fblock, st, inst, ftiles));
+  return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 const void* ensemble_finalize_kernel_ptr() { return (const void*)mx::ens_finalize_kernel; }
