@@ -474,8 +474,10 @@ __device__ __forceinline__ void flux_body(const DevGeomMixed& G, const DevState&
   if (STAGE == 2) fold_candidates(vmax, dmin, S.keys);
 }
 
+// at most 51 registers (5 blocks of up to 256 threads per SM): the measured
+// optimum between occupancy and the small spill it costs
 template <int STAGE>
-__global__ void __launch_bounds__(kFaceTile * kMaxSlotLanes) flux_update_kernel(DevGeomMixed G, DevState S,
+__global__ void __launch_bounds__(kFaceTile * kMaxSlotLanes, 5) flux_update_kernel(DevGeomMixed G, DevState S,
                                                                                 PhysParams P) {
   __shared__ FluxShared sh;
   griddep_launch_dependents();
