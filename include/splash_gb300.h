@@ -166,6 +166,12 @@ SPLASH_API int splash_steps(splash_solver* s, int64_t* steps);         /* MUSCL_
 SPLASH_API int splash_n_faces(splash_solver* s, int* n_faces);
 SPLASH_API int splash_dim(splash_solver* s, int* dim);
 /* [n_faces][dim] conserved state, reference order (MUSCL_base::U). */
+/* State transfers: when the device can access pageable host memory (a
+ * coherent CPU-GPU link, cudaDevAttrPageableMemoryAccess) the state moves
+ * between the caller's array and the device planes in one kernel, without
+ * a staging copy; otherwise through a pinned staging buffer.  Setting the
+ * environment variable SPLASH_STAGED_TRANSFERS before splash_create forces
+ * the staging path.  Both are synchronous and give identical states. */
 SPLASH_API int splash_get_state(splash_solver* s, double* U);
 SPLASH_API int splash_set_state(splash_solver* s, const double* U);
 /* Per-step diagnostics of MUSCL_base.hpp:187-214 for the current state:

@@ -152,12 +152,12 @@ struct Adjoint {
     std::memcpy(h_stage, aos, (size_t)n_faces * kDim * sizeof(double));
     ADJ_CUDA(cudaMemcpyAsync(d_stage, h_stage, (size_t)n_faces * kDim * sizeof(double), cudaMemcpyHostToDevice,
                              stream()));
-    ADJ_CUDA(fp64_scatter_state(d_stage, base->d_perm, planes, n_faces, fpad, stream()));
+    ADJ_CUDA(fp64_scatter_state(d_stage, base->d_iperm, planes, n_faces, fpad, stream()));
     ADJ_CUDA(cudaStreamSynchronize(stream()));
     return SPLASH_OK;
   }
   int from_planes(const double* planes, double* aos) {
-    ADJ_CUDA(fp64_gather_state(planes, base->d_perm, d_stage, n_faces, fpad, stream()));
+    ADJ_CUDA(fp64_gather_state(planes, base->d_iperm, d_stage, n_faces, fpad, stream()));
     ADJ_CUDA(cudaMemcpyAsync(h_stage, d_stage, (size_t)n_faces * kDim * sizeof(double), cudaMemcpyDeviceToHost,
                              stream()));
     ADJ_CUDA(cudaStreamSynchronize(stream()));

@@ -14,6 +14,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <memory>
@@ -228,16 +229,27 @@ cudaError_t Solver::launch_step(cudaEvent_t* ev, double dt0) {
 }
 
 int Solver::upload_state(const double* U_ref) {
+  if (host_direct) {
+    // the scatter kernel reads the caller's array over the coherent link
+    SPLASH_CUDA(fp64_scatter_state(U_ref, d_iperm, S.U, n_faces, fpad, stream, dim));
+    SPLASH_CUDA(launch_prepare());
+    return SPLASH_OK;
+  }
   std::memcpy(h_stage, U_ref, (size_t)n_faces * dim * sizeof(double));
   SPLASH_CUDA(cudaMemcpyAsync(d_stage, h_stage, (size_t)n_faces * dim * sizeof(double),
                               cudaMemcpyHostToDevice, stream));
-  SPLASH_CUDA(fp64_scatter_state(d_stage, d_perm, S.U, n_faces, fpad, stream, dim));
+  SPLASH_CUDA(fp64_scatter_state(d_stage, d_iperm, S.U, n_faces, fpad, stream, dim));
   SPLASH_CUDA(launch_prepare());
   return SPLASH_OK;
 }
 
 int Solver::download_state(double* U_ref) {
-  SPLASH_CUDA(fp64_gather_state(S.U, d_perm, d_stage, n_faces, fpad, stream, dim));
+  if (host_direct) {
+    SPLASH_CUDA(fp64_gather_state(S.U, d_iperm, U_ref, n_faces, fpad, stream, dim));
+    SPLASH_CUDA(cudaStreamSynchronize(stream));
+    return SPLASH_OK;
+  }
+  SPLASH_CUDA(fp64_gather_state(S.U, d_iperm, d_stage, n_faces, fpad, stream, dim));
   SPLASH_CUDA(cudaMemcpyAsync(h_stage, d_stage, (size_t)n_faces * dim * sizeof(double),
                               cudaMemcpyDeviceToHost, stream));
   SPLASH_CUDA(cudaStreamSynchronize(stream));
@@ -409,6 +421,14 @@ int splash_create(const splash_mesh_desc* mesh, const double* U_in, int dim, dou
     S.keys = s->dalloc<unsigned long long>(2);
     s->d_stage = s->dalloc<double>((size_t)s->n_faces * dim);
     s->d_perm = s->upload(s->perm);
+    s->d_iperm = s->upload(s->iperm);
+    {
+      // Grace-class hosts: the device can dereference pageable host memory,
+      // so states cross the boundary without a staging copy
+      int pma = 0;
+      if (cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, device) == cudaSuccess)
+        s->host_direct = pma != 0 && std::getenv("SPLASH_STAGED_TRANSFERS") == nullptr;
+    }
     SPLASH_CUDA(cudaMemset(S.U, 0, splash::kDim * fp * sizeof(double)));
     SPLASH_CUDA(cudaMemset(S.W0, 0, splash::kDim * fp * sizeof(double)));
     SPLASH_CUDA(cudaMemset(S.W1, 0, splash::kDim * fp * sizeof(double)));

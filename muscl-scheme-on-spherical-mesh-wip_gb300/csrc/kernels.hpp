@@ -21,10 +21,11 @@ cudaError_t fp64_dt(const DevState& S, const PhysParams& P, int n_faces, cudaStr
 cudaError_t fp64_step(const DevGeom& G, const DevState& S, const PhysParams& P, cudaStream_t st,
                       cudaEvent_t* ev = nullptr);
 // reference-order [n_faces][dim] <-> internal planes (dim 5, or 4 for the
-// isothermal solver, whose fifth plane is zero)
-cudaError_t fp64_scatter_state(const double* aos, const int* perm, double* U, int n_faces, int fpad,
+// isothermal solver, whose fifth plane is zero); iperm[reference face] =
+// internal face.  aos may be host memory the device can access.
+cudaError_t fp64_scatter_state(const double* aos, const int* iperm, double* U, int n_faces, int fpad,
                                cudaStream_t st, int dim = kDim);
-cudaError_t fp64_gather_state(const double* U, const int* perm, double* aos, int n_faces, int fpad,
+cudaError_t fp64_gather_state(const double* U, const int* iperm, double* aos, int n_faces, int fpad,
                               cudaStream_t st, int dim = kDim);
 
 // ---- FP32/FP64 mixed path (step_mixed.cu) ----

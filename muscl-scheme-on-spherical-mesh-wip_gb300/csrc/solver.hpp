@@ -53,6 +53,8 @@ struct Solver {
   DevState S{};
   double* d_stage = nullptr;  // [n_faces][5] reference-order staging
   int* d_perm = nullptr;
+  int* d_iperm = nullptr;   // reference face -> internal face
+  bool host_direct = false; // the device reads and writes pageable host memory (coherent link)
   double* h_stage = nullptr;  // pinned mirror of d_stage
   std::vector<void*> dev_allocs;
   cudaGraph_t graph = nullptr;

@@ -250,20 +250,23 @@ __global__ void __launch_bounds__(kBlock) iso_flux_update_kernel(DevGeom G, DevS
 __global__ void set_scalar_kernel(double* dst, double v) { *dst = v; }
 
 // reference order [F][dim] <-> internal planes
-// (dim = 4: the fifth plane is zero)
-__global__ void scatter_state_kernel(const double* __restrict__ aos, const int* __restrict__ perm,
+// Threads run in reference order (thread r moves reference face r), so the
+// [n_faces][dim] array -- device memory or, on a coherent host link, the
+// caller's host memory -- is read and written contiguously; the planes
+// take the permuted side.  (dim = 4: the fifth plane is zero.)
+__global__ void scatter_state_kernel(const double* __restrict__ aos, const int* __restrict__ iperm,
                                      double* __restrict__ U, int n_faces, int fpad, int dim) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n_faces) return;
-  const int r = perm[i];
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n_faces) return;
+  const int i = iperm[r];
 #pragma unroll
   for (int k = 0; k < kDim; ++k) U[k * fpad + i] = (k < dim) ? aos[(size_t)r * dim + k] : 0.0;
 }
-__global__ void gather_state_kernel(const double* __restrict__ U, const int* __restrict__ perm,
+__global__ void gather_state_kernel(const double* __restrict__ U, const int* __restrict__ iperm,
                                     double* __restrict__ aos, int n_faces, int fpad, int dim) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n_faces) return;
-  const int r = perm[i];
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n_faces) return;
+  const int i = iperm[r];
 #pragma unroll
   for (int k = 0; k < kDim; ++k)
     if (k < dim) aos[(size_t)r * dim + k] = U[k * fpad + i];
@@ -324,15 +327,15 @@ cudaError_t fp64_step(const DevGeom& G, const DevState& S, const PhysParams& P, 
   return cudaGetLastError();
 }
 
-cudaError_t fp64_scatter_state(const double* aos, const int* perm, double* U, int n_faces,
+cudaError_t fp64_scatter_state(const double* aos, const int* iperm, double* U, int n_faces,
                                int fpad, cudaStream_t st, int dim) {
-  f64::scatter_state_kernel<<<f64::blocks_for(n_faces), f64::kBlock, 0, st>>>(aos, perm, U, n_faces, fpad, dim);
+  f64::scatter_state_kernel<<<f64::blocks_for(n_faces), f64::kBlock, 0, st>>>(aos, iperm, U, n_faces, fpad, dim);
   return cudaGetLastError();
 }
 
-cudaError_t fp64_gather_state(const double* U, const int* perm, double* aos, int n_faces,
+cudaError_t fp64_gather_state(const double* U, const int* iperm, double* aos, int n_faces,
                               int fpad, cudaStream_t st, int dim) {
-  f64::gather_state_kernel<<<f64::blocks_for(n_faces), f64::kBlock, 0, st>>>(U, perm, aos, n_faces, fpad, dim);
+  f64::gather_state_kernel<<<f64::blocks_for(n_faces), f64::kBlock, 0, st>>>(U, iperm, aos, n_faces, fpad, dim);
   return cudaGetLastError();
 }
 
