@@ -141,6 +141,7 @@ template <int N> SPLASH_HD bool is_inf(const Dual<N>& a) { return is_inf(a.v); }
 // the double overloads next to the dual ones, so unqualified calls in
 // templated code resolve for both
 using ::exp;
+using ::expm1;
 using ::log;
 using ::sqrt;
 using ::tanh;
@@ -163,6 +164,12 @@ template <int N>
 SPLASH_HD Dual<N> exp(const Dual<N>& a) {
   const double e = ::exp(a.v);
   return chain(a, e, e);
+}
+template <int N>
+SPLASH_HD Dual<N> expm1(const Dual<N>& a) {
+  const double e = ::expm1(a.v);
+  // saturated (e = inf): the derivative e + 1 is inf as well; keep the chain
+  return chain(a, e, e + 1.0);
 }
 template <int N>
 SPLASH_HD Dual<N> log(const Dual<N>& a) {
