@@ -35,6 +35,7 @@ CXXFLAGS = ["-std=c++17", "-O3", "-fPIC", "-fopenmp", "-ffp-contract=off", "-Wal
 CU_FLAGS = {
     "step_fp64.cu": ["-fmad=false"],
     "adjoint.cu": ["-fmad=false"],
+    "diagnostics.cu": ["-fmad=false"],
     "cfl_noalloc.cu": ["-fmad=false"],
     "step_mixed.cu": ["-fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"],
 }

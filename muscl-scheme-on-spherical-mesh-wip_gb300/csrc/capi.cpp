@@ -23,6 +23,7 @@
 #include <string>
 #include <vector>
 
+#include "diagnostics.hpp"
 #include "geometry.hpp"
 #include "hilbert.hpp"
 #include "kernels.hpp"
@@ -84,6 +85,7 @@ Solver::~Solver() {
   if (graph) cudaGraphDestroy(graph);
   for (void* p : dev_allocs) cudaFree(p);
   if (h_stage) cudaFreeHost(h_stage);
+  if (h_diag) cudaFreeHost(h_diag);
   if (stream) cudaStreamDestroy(stream);
 }
 
@@ -215,6 +217,48 @@ void Solver::build_device_geometry(const RefGeometry& g) {
   wr_face_vtx = g.face_vtx;
   wr_face_centers = g.face_centers;
   wr_area = g.area;
+}
+
+// The light curves' observer geometry (physics/adiabatic.hpp:233-245,
+// 258-322): per observer and face, cos(alpha) = |o . fcn| / |o| where the
+// observer sees the face, 0 elsewhere; internal face order.
+static std::vector<double> observer_planes(const Solver& s) {
+  const double D = 9.4 * 3 * 1e19 / 15000;
+  const V3 obs[4] = {{D, 0, 0},
+                     {std::sqrt(9.4 * 3 * 1e19 / 15000), 0, std::sqrt(9.4 * 3 * 1e19 / 15000)},
+                     {0, 0, D},
+                     {0, 0, -9.4 * 3 * 1e19 / 15000}};
+  std::vector<double> c(4 * (size_t)s.fpad, 0.0);
+  for (int r = 0; r < s.n_faces; ++r) {
+    const int i = s.iperm[r];
+    const V3 fc = at3(s.wr_face_centers, r);
+    const double phi_fc = std::atan2(fc.y / vnorm(fc), fc.x / vnorm(fc));
+    const double theta_fc = std::acos(fc.z / vnorm(fc));
+    const V3 fcn = vdiv(fc, vnorm(fc));
+    const bool seen[4] = {phi_fc < M_PI / 2 && phi_fc > -M_PI / 2, vdot(obs[1], fcn) > 0, theta_fc < M_PI / 2,
+                          theta_fc > M_PI / 2};
+    for (int o = 0; o < 4; ++o)
+      if (seen[o]) c[(size_t)o * s.fpad + i] = std::abs(vdot(obs[o], fcn)) / vnorm(obs[o]);
+  }
+  return c;
+}
+
+int Solver::run_diagnostics(double* out9) {
+  DiagInput in{};
+  in.n_faces = n_faces;
+  in.fpad = fpad;
+  in.dim = dim;
+  in.U = S.U;
+  in.fcn = (precision == SPLASH_PREC_MIXED) ? GM.fcn : G.fcn;
+  in.area = (precision == SPLASH_PREC_MIXED) ? GM.area : G.area;
+  in.cos_obs = d_cos_obs;
+  in.gam = P.gam;
+  in.light_curves = dim == kDim ? 1 : 0;
+  SPLASH_CUDA(diag_launch(in, d_diag_partial, d_diag_out, stream));
+  SPLASH_CUDA(cudaMemcpyAsync(h_diag, d_diag_out, 9 * sizeof(double), cudaMemcpyDeviceToHost, stream));
+  SPLASH_CUDA(cudaStreamSynchronize(stream));
+  std::memcpy(out9, h_diag, 9 * sizeof(double));
+  return SPLASH_OK;
 }
 
 cudaError_t Solver::launch_prepare() {
@@ -422,6 +466,10 @@ int splash_create(const splash_mesh_desc* mesh, const double* U_in, int dim, dou
     s->d_stage = s->dalloc<double>((size_t)s->n_faces * dim);
     s->d_perm = s->upload(s->perm);
     s->d_iperm = s->upload(s->iperm);
+    s->d_cos_obs = s->upload(observer_planes(*s));
+    s->d_diag_partial = s->dalloc<double>((size_t)splash::diag_partial_blocks(s->n_faces) * 9);
+    s->d_diag_out = s->dalloc<double>(9);
+    SPLASH_CUDA(cudaMallocHost(&s->h_diag, 9 * sizeof(double)));
     {
       // Grace-class hosts: the device can dereference pageable host memory,
       // so states cross the boundary without a staging copy
@@ -607,23 +655,10 @@ int splash_set_state(splash_solver* h, const double* U) {
 int splash_diagnostics(splash_solver* h, double out[5]) {
   GET_SOLVER(h);
   if (!out) return fail(SPLASH_E_INVALID, "out is NULL");
-  std::vector<double> U((size_t)s->n_faces * s->dim);
-  int rc = s->download_state(U.data());
+  double v[9];
+  const int rc = s->run_diagnostics(v);
   if (rc) return rc;
-  double m = 0, l1 = 0, l2 = 0, l3 = 0, e = 0;
-  for (int i = 0; i < s->n_faces; ++i) {
-    const double* u = &U[(size_t)i * s->dim];
-    m += u[0] * s->wr_area[i];
-    l1 += u[1] * s->wr_area[i];
-    l2 += u[2] * s->wr_area[i];
-    l3 += u[3] * s->wr_area[i];
-    if (s->dim > 4) e += u[4] * s->wr_area[i];
-  }
-  out[0] = m;
-  out[1] = l1;
-  out[2] = l2;
-  out[3] = l3;
-  out[4] = e;
+  for (int k = 0; k < 5; ++k) out[k] = v[k];
   return SPLASH_OK;
 }
 
@@ -798,36 +833,10 @@ int splash_get_light_curves(splash_solver* h, double out[4]) {
   GET_SOLVER(h);
   if (s->dim == 4) return fail(SPLASH_E_UNSUPPORTED, "the isothermal solver has no such member (physics/isothermal.hpp)");
   if (!out) return fail(SPLASH_E_INVALID, "out is NULL");
-  std::vector<double> U((size_t)s->n_faces * s->dim);
-  int rc;
-  if ((rc = s->download_state(U.data()))) return rc;
-  // observers of physics/adiabatic.hpp:233-245
-  const double D = 9.4 * 3 * 1e19 / 15000;
-  const V3 o0{D, 0, 0};
-  const V3 o45{std::sqrt(9.4 * 3 * 1e19 / 15000), 0, std::sqrt(9.4 * 3 * 1e19 / 15000)};
-  const V3 o90{0, 0, D};
-  const V3 o180{0, 0, -9.4 * 3 * 1e19 / 15000};
-  double f0 = 0, f45 = 0, f90 = 0, f180 = 0;
-  for (int i = 0; i < s->n_faces; ++i) {
-    const double* u = &U[(size_t)i * s->dim];
-    const V3 fc = at3(s->wr_face_centers, i);
-    const double phi_fc = std::atan2(fc.y / vnorm(fc), fc.x / vnorm(fc));
-    const double theta_fc = std::acos(fc.z / vnorm(fc));
-    const V3 fcn = vdiv(fc, vnorm(fc));
-    V3 vel = vcross(fcn, V3{u[1], u[2], u[3]});
-    vel = vdiv(vel, -u[0]);
-    const double vn = vnorm(vel);
-    const double PI = smax(1e-16, (u[4] - u[0] * (vn * vn) / 2) * (s->P.gam - 1));
-    const double area = s->wr_area[i];
-    if (phi_fc < M_PI / 2 && phi_fc > -M_PI / 2) f0 += PI * (std::abs(vdot(o0, fcn)) / vnorm(o0)) * area;
-    if (theta_fc < M_PI / 2) f90 += PI * (std::abs(vdot(o90, fcn)) / vnorm(o90)) * area;
-    if (vdot(o45, fcn) > 0) f45 += PI * (std::abs(vdot(o45, fcn)) / vnorm(o45)) * area;
-    if (theta_fc > M_PI / 2) f180 += PI * (std::abs(vdot(o180, fcn)) / vnorm(o180)) * area;
-  }
-  out[0] = f0;
-  out[1] = f45;
-  out[2] = f90;
-  out[3] = f180;
+  double v[9];
+  const int rc = s->run_diagnostics(v);
+  if (rc) return rc;
+  for (int k = 0; k < 4; ++k) out[k] = v[5 + k];
   return SPLASH_OK;
 }
 

@@ -54,6 +54,12 @@ struct Solver {
   double* d_stage = nullptr;  // [n_faces][5] reference-order staging
   int* d_perm = nullptr;
   int* d_iperm = nullptr;   // reference face -> internal face
+  // device diagnostics (diagnostics.cu): observer planes, partials, results
+  double* d_cos_obs = nullptr;
+  double* d_diag_partial = nullptr;
+  double* d_diag_out = nullptr;
+  double* h_diag = nullptr;  // pinned, 9 doubles
+  int run_diagnostics(double* out9);
   bool host_direct = false; // the device reads and writes pageable host memory (coherent link)
   double* h_stage = nullptr;  // pinned mirror of d_stage
   std::vector<void*> dev_allocs;
