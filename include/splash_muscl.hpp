@@ -243,7 +243,16 @@ class Solver {
   }
 
  public:
-  void do_step(double dt0) { check(splash_do_step(h_, dt0), "do_step"); }
+  void do_step(double dt0) {
+    check(splash_do_step(h_, dt0), "do_step");
+    if (log_) log_step();
+  }
+  // The reference prints one line per do_step (MUSCL_base.hpp:187-213):
+  // "t= <t> mass_relative_gain=<M/M_1 - 1> (l/mass)_total_norm= <|L|>
+  // l_total = (<Lx>,<Ly>,<Lz>)" with M, L the area-weighted sums after the
+  // step and M_1 the mass after the first step.  Here it is off by default
+  // (it synchronises every step); set_step_log(&std::cout) turns it on.
+  void set_step_log(std::ostream* os) { log_ = os; }
   double time() {
     double t = 0;
     check(splash_time(h_, &t), "time");
@@ -338,9 +347,23 @@ class Solver {
     }
   };
 
+  void log_step() {
+    double d[5];
+    check(splash_diagnostics(h_, d), "diagnostics");
+    if (logged_ == 0) mass_first_ = d[0];
+    ++logged_;
+    *log_ << "t= " << time() << " mass_relative_gain=" << d[0] / mass_first_ - 1
+          << " (l/mass)_total_norm= " << std::sqrt(d[1] * d[1] + d[2] * d[2] + d[3] * d[3]) << " l_total = ("
+          << d[1] << "," << d[2] << "," << d[3] << ")"
+          << "\n";
+  }
+
   Mesh mesh_;
   int dim_;
   splash_solver* h_ = nullptr;
+  std::ostream* log_ = nullptr;
+  long logged_ = 0;
+  double mass_first_ = 0.0;
 };
 
 // Riemann_solvers/HLLE.hpp:11-13: the isothermal solver, dim 4 (its

@@ -62,6 +62,8 @@ int main(int argc, char** argv) {
     s->write_t_p();
     s->write_t_omega_z();
     s->write_t_L();
+    std::ofstream steplog("results/steplog.txt");
+    s->set_step_log(&steplog);
     std::ofstream lc("results/lightcurves.txt");
     lc.precision(17);
     std::vector<double> l = s->get_light_curves();

@@ -214,9 +214,11 @@ def writers_case(name, mesh, level, solver, gam, acc, params, dt, nsteps, recipe
         ic.write_input_dat(td / "input" / "input.dat", U0)
         cmd = [str(RUNNER), "writers", mesh, str(level), solver, "5", repr(gam), "0.0",
                "1" if acc else "0", "8", repr(dt), str(nsteps), "0", str(td / "out")]
-        subprocess.run(cmd, cwd=td, check=True, stdout=subprocess.DEVNULL)
+        res = subprocess.run(cmd, cwd=td, check=True, capture_output=True, text=True)
         files = {p.name: p.read_text() for p in sorted((td / "results").iterdir())}
         files["lightcurves.txt"] = (td / "out_lightcurves.txt").read_text()
+        # the reference's per-step line (MUSCL_base.hpp:211-213)
+        files["steplog.txt"] = "".join(l + "\n" for l in res.stdout.splitlines() if l.startswith("t= "))
     rec = {"U0": U0, "gam": np.float64(gam), "dt0": np.float64(dt), "steps": nsteps,
            "solver": SOLVERS[solver], "accretion_on": int(acc), "mesh": mesh, "level": level,
            "files": np.array(list(files.keys())), "texts": np.array(list(files.values()))}
@@ -226,7 +228,7 @@ def writers_case(name, mesh, level, solver, gam, acc, params, dt, nsteps, recipe
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--only", choices=["isothermal"], default=None,
+    ap.add_argument("--only", choices=["isothermal", "writers"], default=None,
                     help="regenerate one group of fixtures only")
     a = ap.parse_args()
     if not RUNNER.exists():
@@ -234,6 +236,10 @@ def main():
     if a.only == "isothermal":
         iso_funcs_case("hlle_hex3")
         iso_funcs_case("hlle_quad3", mesh="quad", seed=17)
+        return
+    if a.only == "writers":
+        writers_case("hex3_hllcp", "hex", 3, "HLLCplus", ic.gam2d(4 / 3), True, ACC_PARAMS, 1e-3, 5,
+                     lambda r, g_, seed: ic.rotating_blob(r, g_, seed=seed), 5)
         return
     # geometry: full arrays for small meshes, hashes for larger ones
     scal = {}

@@ -4,6 +4,7 @@ library, must write the same output files as the reference (golden texts
 produced by the reference itself, tests/golden/gen_golden.py)."""
 import json
 import os
+import re
 import subprocess
 from pathlib import Path
 
@@ -86,6 +87,15 @@ def test_drop_in_driver_writes_reference_files(tmp_path):
         a, b = _numbers((out / name).read_text()), _numbers(files[name])
         assert a.shape == b.shape, name
         assert np.allclose(a, b, rtol=2e-6, atol=1e-300), name
+    # the per-step line (6 significant digits): same times, mass gains and L
+    log_a = [l for l in (out / "steplog.txt").read_text().splitlines() if l]
+    log_b = [l for l in files["steplog.txt"].splitlines() if l]
+    assert len(log_a) == len(log_b) == int(w["steps"])
+    num = re.compile(r"[-+]?(?:\d+\.?\d*|\.\d+)(?:[eE][-+]?\d+)?")
+    for la, lb in zip(log_a, log_b):
+        na, nb = np.array(num.findall(la), dtype=float), np.array(num.findall(lb), dtype=float)
+        assert na.shape == nb.shape == (6,), (la, lb)
+        assert np.allclose(na, nb, rtol=2e-5, atol=1e-9), (la, lb)
     lc_a = _numbers((out / "lightcurves.txt").read_text()).reshape(-1, 5)
     lc_b = _numbers(files["lightcurves.txt"]).reshape(-1, 5)
     assert np.allclose(lc_a, lc_b, rtol=1e-12, atol=0)
