@@ -250,27 +250,28 @@ __global__ void __launch_bounds__(kBlock) iso_flux_update_kernel(DevGeom G, DevS
 __global__ void set_scalar_kernel(double* dst, double v) { *dst = v; }
 
 // reference order [F][dim] <-> internal planes
-// Threads run in reference order (thread r moves reference face r), so the
-// [n_faces][dim] array -- device memory or, on a coherent host link, the
-// caller's host memory -- is read and written contiguously; the planes
-// take the permuted side.  (dim = 4: the fifth plane is zero.)
+// One thread per element of the [n_faces][dim] array, in its memory order,
+// so that every warp reads or writes 256 contiguous bytes of it -- device
+// memory or, on a coherent host link, the caller's host memory, where
+// partial-line accesses are expensive; the planes take the permuted side.
+// (dim = 4: the fifth plane is written as zero by the scatter.)
 __global__ void scatter_state_kernel(const double* __restrict__ aos, const int* __restrict__ iperm,
                                      double* __restrict__ U, int n_faces, int fpad, int dim) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= n_faces) return;
+  const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= (size_t)n_faces * dim) return;
+  const int r = (int)(e / dim), k = (int)(e % dim);
   const int i = iperm[r];
-#pragma unroll
-  for (int k = 0; k < kDim; ++k) U[k * fpad + i] = (k < dim) ? aos[(size_t)r * dim + k] : 0.0;
+  U[(size_t)k * fpad + i] = aos[e];
+  if (dim == 4 && k == 3) U[(size_t)4 * fpad + i] = 0.0;
 }
 __global__ void gather_state_kernel(const double* __restrict__ U, const int* __restrict__ iperm,
                                     double* __restrict__ aos, int n_faces, int fpad, int dim) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= n_faces) return;
-  const int i = iperm[r];
-#pragma unroll
-  for (int k = 0; k < kDim; ++k)
-    if (k < dim) aos[(size_t)r * dim + k] = U[k * fpad + i];
+  const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= (size_t)n_faces * dim) return;
+  const int r = (int)(e / dim), k = (int)(e % dim);
+  aos[e] = U[(size_t)k * fpad + iperm[r]];
 }
+constexpr int kMoveBlock = 256;
 
 inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
 
@@ -329,13 +330,17 @@ cudaError_t fp64_step(const DevGeom& G, const DevState& S, const PhysParams& P, 
 
 cudaError_t fp64_scatter_state(const double* aos, const int* iperm, double* U, int n_faces,
                                int fpad, cudaStream_t st, int dim) {
-  f64::scatter_state_kernel<<<f64::blocks_for(n_faces), f64::kBlock, 0, st>>>(aos, iperm, U, n_faces, fpad, dim);
+  const size_t ne = (size_t)n_faces * dim;
+  f64::scatter_state_kernel<<<(unsigned)((ne + f64::kMoveBlock - 1) / f64::kMoveBlock), f64::kMoveBlock, 0, st>>>(
+      aos, iperm, U, n_faces, fpad, dim);
   return cudaGetLastError();
 }
 
 cudaError_t fp64_gather_state(const double* U, const int* iperm, double* aos, int n_faces,
                               int fpad, cudaStream_t st, int dim) {
-  f64::gather_state_kernel<<<f64::blocks_for(n_faces), f64::kBlock, 0, st>>>(U, iperm, aos, n_faces, fpad, dim);
+  const size_t ne = (size_t)n_faces * dim;
+  f64::gather_state_kernel<<<(unsigned)((ne + f64::kMoveBlock - 1) / f64::kMoveBlock), f64::kMoveBlock, 0, st>>>(
+      U, iperm, aos, n_faces, fpad, dim);
   return cudaGetLastError();
 }
 
