@@ -241,8 +241,8 @@ __device__ __forceinline__ void prepare_body(const DevGeomMixed& G, const DevSta
   fold_candidates(vmax, dmin, S.keys);
 }
 
-__global__ void __launch_bounds__(32) prepare_kernel(DevGeomMixed G, DevState S, PhysParams P) {
-  prepare_body(G, S, P, blockIdx.x * 32 + threadIdx.x);
+__global__ void __launch_bounds__(128) prepare_kernel(DevGeomMixed G, DevState S, PhysParams P) {
+  prepare_body(G, S, P, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // initial keys: max |v|^2 starts at (1e-8)^2 and min extra dt at 1e20, the
@@ -541,7 +541,7 @@ const void* mixed_finalize_kernel_ptr() { return (const void*)mx::finalize_kerne
 cudaError_t mixed_prepare(const DevGeomMixed& G, const DevState& S, const PhysParams& P,
                           cudaStream_t st) {
   mx::reset_keys_kernel<<<1, 1, 0, st>>>(S.keys);
-  mx::prepare_kernel<<<(G.n_faces + 31) / 32, 32, 0, st>>>(G, S, P);
+  mx::prepare_kernel<<<(G.n_faces + 127) / 128, 128, 0, st>>>(G, S, P);
   return cudaGetLastError();
 }
 
