@@ -49,8 +49,16 @@ __device__ __forceinline__ void griddep_launch_dependents() { asm volatile("grid
 // an n-entry array is a float4 (Sigma, l_x, l_y, l_z) at base + 4 i and Pi
 // at base + 4 n + i, so a gather of one state is one 16-byte load (plus one
 // for Pi; the isothermal solver needs none).
+//
+// State loads are ordinary (coherent) loads, never ld.global.nc: under
+// programmatic dependent launch a kernel is resident while its predecessor
+// still writes the state, and the non-coherent path is defined only for data
+// that is read-only for the whole life of the kernel.  griddepcontrol.wait
+// makes the predecessor's writes visible to ordinary loads.  (With __ldg
+// here, batched runs of small meshes read stale face states.)  Only the
+// geometry, which no kernel writes, goes through __ldg.
 __device__ __forceinline__ float4 ld4(const float* base, int i) {
-  return __ldg(reinterpret_cast<const float4*>(base) + i);
+  return reinterpret_cast<const float4*>(base)[i];
 }
 __device__ __forceinline__ void ld5(const float* base, int n, int i, float* v) {
   const float4 a = ld4(base, i);
@@ -58,7 +66,7 @@ __device__ __forceinline__ void ld5(const float* base, int n, int i, float* v) {
   v[1] = a.y;
   v[2] = a.z;
   v[3] = a.w;
-  v[4] = __ldg(base + 4 * (size_t)n + i);
+  v[4] = base[4 * (size_t)n + i];
 }
 __device__ __forceinline__ void st5(float* base, int n, int i, const float* v) {
   reinterpret_cast<float4*>(base)[i] = make_float4(v[0], v[1], v[2], v[3]);
@@ -291,7 +299,7 @@ __device__ __forceinline__ void recon_body(const DevGeomMixed& G, const DevState
   if (j >= n) return;
   const int fp = G.fpad;
   const int PS = G.max_slots * fp;
-  const float* __restrict__ W = S.W32;
+  const float* W = S.W32;
   const int s = j * fp + f;
   const int ia = G.sten[s], ib = G.sten[PS + s], ic = G.sten[2 * PS + s], id = G.sten[3 * PS + s];
   const float bp0 = G.beta[s], bp1 = G.beta[PS + s], bm0 = G.beta[2 * PS + s], bm1 = G.beta[3 * PS + s];
@@ -326,8 +334,8 @@ __device__ __forceinline__ void recon_body(const DevGeomMixed& G, const DevState
     reinterpret_cast<float4*>(S.uplus32)[s] = o;
     return;
   }
-  const float* __restrict__ Wp = W + 4 * (size_t)fp;
-  const float wp = __ldg(Wp + f);
+  const float* Wp = W + 4 * (size_t)fp;
+  const float wp = Wp[f];
   const float gam = P.gam_f;
   const float inv_rho = -1.0f / w[0];
   const float c = sqrtf(gam * wp / w[0]);
@@ -343,8 +351,8 @@ __device__ __forceinline__ void recon_body(const DevGeomMixed& G, const DevState
   }
   reinterpret_cast<float4*>(S.uplus32)[s] = o;
   {
-    const float pp = (bp0 * __ldg(Wp + ia) + bp1 * __ldg(Wp + ib) - wp) * ihp;
-    const float pm = (wp - (bm0 * __ldg(Wp + ic) + bm1 * __ldg(Wp + id))) * ihm;
+    const float pp = (bp0 * Wp[ia] + bp1 * Wp[ib] - wp) * ihp;
+    const float pm = (wp - (bm0 * Wp[ic] + bm1 * Wp[id])) * ihm;
     const float lim = limiter_field(pm / pp, nu_plus, eta_p, sb_scale);
     S.uplus32[4 * (size_t)PS + s] = wp + pp * lim * bmd;
   }
@@ -509,7 +517,7 @@ __global__ void ens_finalize_kernel(const EnsInstance* __restrict__ inst, int n,
   if (i < n) finalize_body(inst[i].S, inst[i].P, dt0);
 }
 
-__global__ void __launch_bounds__(256, 4) ens_reconstruct_kernel(const EnsInstance* __restrict__ inst,
+__global__ void __launch_bounds__(256, 5) ens_reconstruct_kernel(const EnsInstance* __restrict__ inst,
                                                               const int2* __restrict__ tiles) {
   griddep_launch_dependents();
   const int2 t = tiles[blockIdx.x];
@@ -518,7 +526,7 @@ __global__ void __launch_bounds__(256, 4) ens_reconstruct_kernel(const EnsInstan
 }
 
 template <int STAGE>
-__global__ void __launch_bounds__(kFaceTile * kMaxSlotLanes) ens_flux_kernel(
+__global__ void __launch_bounds__(kFaceTile * kMaxSlotLanes, 5) ens_flux_kernel(
     const EnsInstance* __restrict__ inst, const int2* __restrict__ tiles) {
   __shared__ FluxShared sh;
   griddep_launch_dependents();

@@ -70,3 +70,31 @@ def test_ensemble_schedule_does_not_change_results():
     b.do_steps(10, 1e-3)
     for i in range(len(ms)):
         assert np.array_equal(a.get_state(i), b.get_state(i))
+
+
+def test_batched_and_single_runs_repeat_bit_for_bit():
+    """The step's kernels overlap their predecessors (programmatic dependent
+    launch); on small meshes whole grids are resident at once, so a state
+    read that bypassed the predecessor's writes would show here as
+    run-to-run differences."""
+    import splash_gb300 as sg
+
+    ms = members(seed=11)
+    runs = []
+    for _ in range(3):
+        e = sg.Ensemble(ms, autotune=False)
+        e.do_steps(30, 1e-2)
+        runs.append([e.get_state(i) for i in range(len(ms))])
+        e.close()
+    for r in runs[1:]:
+        assert all(np.array_equal(x, y) for x, y in zip(runs[0], r))
+    m = ms[0]
+    single = []
+    for _ in range(3):
+        s = sg.Solver(m["mesh"], m["U_in"], m["U_in"].shape[1], m["gam"], 0.0, True, params=m["params"],
+                      solver=m["solver"], precision=sg.PREC_MIXED)
+        s.do_steps(30, 1e-2)
+        single.append(s.get_state())
+        s.close()
+    assert all(np.array_equal(single[0], x) for x in single[1:])
+    assert np.array_equal(single[0], runs[0][0])
