@@ -447,7 +447,7 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
         "config": {**workload_config(F, "mixed FP32/FP64"), "parallelism": f"replicas{world}",
                    "working_set_mb": round((geo_b + st_b) / 2**20, 1)},
-        "gpu_launches": 5 * args.steps,
+        "gpu_launches": 7 * args.steps,
         "e2e": {"value": F * e2e_steps / e2e_secs, "unit": METRIC, "h2d_bytes_per_step": bytes_io,
                 "d2h_bytes_per_step": bytes_io},
         "fp64": {"value": value64, "ms_per_step": secs64 / args.steps * 1e3, "kernel_ms": kern64},

@@ -450,6 +450,7 @@ int splash_create(const splash_mesh_desc* mesh, const double* U_in, int dim, dou
     if (precision == SPLASH_PREC_MIXED) {
       S.W32 = s->dalloc<float>(splash::kDim * fp);
       S.uplus32 = s->dalloc<float>(splash::kDim * PS);
+      S.inc32 = s->dalloc<float>(splash::kDim * fp);
       S.uplus = nullptr;
       SPLASH_CUDA(cudaMemset(S.W32, 0, splash::kDim * fp * sizeof(float)));
       SPLASH_CUDA(cudaMemset(S.uplus32, 0, splash::kDim * PS * sizeof(float)));

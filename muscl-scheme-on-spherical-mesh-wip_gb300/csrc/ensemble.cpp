@@ -61,7 +61,7 @@ struct Ensemble {
   std::vector<EnsInstance> inst;
   EnsInstance* d_inst = nullptr;
   double *U = nullptr, *acc = nullptr, *scal = nullptr, *U_snap = nullptr, *scal_snap = nullptr;
-  float *W32 = nullptr, *uplus = nullptr;
+  float *W32 = nullptr, *uplus = nullptr, *inc32 = nullptr;
   unsigned int *err = nullptr, *err_snap = nullptr;
   unsigned long long* keys = nullptr;
   int2 *d_rtiles = nullptr, *d_ftiles = nullptr;
@@ -329,6 +329,7 @@ int splash_ensemble_create(const splash_member* members, int n, int device, int 
     e->acc = e->dalloc<double>(faces);
     e->W32 = e->dalloc<float>(faces * kDim);
     e->uplus = e->dalloc<float>(slots * kDim);
+    e->inc32 = e->dalloc<float>(faces * kDim);
     e->scal = e->dalloc<double>((size_t)n * kScCount);
     e->scal_snap = e->dalloc<double>((size_t)n * kScCount);
     e->err = e->dalloc<unsigned int>((size_t)n * 4);
@@ -361,6 +362,7 @@ int splash_ensemble_create(const splash_member* members, int n, int device, int 
       I.S.U = e->U + e->off_face[i] * kDim;
       I.S.W32 = e->W32 + e->off_face[i] * kDim;
       I.S.uplus32 = e->uplus + e->off_slot[i] * kDim;
+      I.S.inc32 = e->inc32 + e->off_face[i] * kDim;
       I.S.scal = e->scal + (size_t)i * kScCount;
       I.S.err = e->err + (size_t)i * 4;
       I.S.keys = e->keys + (size_t)i * 2;

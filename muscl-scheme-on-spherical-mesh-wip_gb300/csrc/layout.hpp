@@ -41,6 +41,7 @@ struct PhysParams {
   // uniform constant: gam3d / (2 gam3d - 1) with gam3d = 1 / (2 - gam)
   // (physics/adiabatic.hpp:563-566), and FP32 copies for the mixed path
   double fric_k;
+  double gam_m1, fric_ak;  // gam - 1 and alpha * fric_k (mixed-path update)
   float gam_f, e_acc_f, alpha_f, omega_ns_f;
   float omega_acc_f[3];
   float depletion_f;     // -(acc_rate 4 pi) / total_mass (adiabatic.hpp:430-436)
@@ -50,6 +51,8 @@ struct PhysParams {
 inline void derive_params(PhysParams& P) {
   const double gam3d = 1 / (2 - P.gam);
   P.fric_k = gam3d / (2 * gam3d - 1);
+  P.gam_m1 = P.gam - 1.0;
+  P.fric_ak = P.alpha * P.fric_k;
   P.gam_f = (float)P.gam;
   P.e_acc_f = (float)P.e_acc;
   P.alpha_f = (float)P.alpha;
@@ -120,6 +123,7 @@ struct DevState {
   double* uplus;  // reconstructed edge states, kDim * max_slots planes of fpad
   float* W32;     // mixed path: (Sigma, l, Pi) in FP32: [fpad] float4 (Sigma, l), then a Pi plane
   float* uplus32; // mixed path: edge states, same packing over max_slots * fpad slots
+  float* inc32;   // mixed path: per-face FP32 flux increment of a stage, kDim planes of fpad
   double* partial;  // per-block partial records (kPartialStride doubles)
   double* scal;   // device scalars, see ScalarSlot
   unsigned int* err;  // stop bits
@@ -143,6 +147,7 @@ enum ScalarSlot : int {
   kScMass = 4,     // 4..8: sum Sigma A, l_x A, l_y A, l_z A, E A of the step's input state
   kScDt0 = 9,      // dt0 requested by the caller
   kScDtF = 10,     // mixed path: (float dt, float dt/2) packed in one slot
+  kScDtHalf = 11,  // mixed path: dt / 2 (FP64)
   kScCount = 16
 };
 

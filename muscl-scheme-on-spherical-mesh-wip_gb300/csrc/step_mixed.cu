@@ -15,6 +15,7 @@
 
 #include <cstdint>
 
+#include "fp_convert.cuh"
 #include "kernels.hpp"
 #include "physics_fp64.cuh"
 #include "physics_mixed.cuh"
@@ -77,6 +78,11 @@ __device__ __forceinline__ f64::D3 plane3d(const double* p, int stride, int i) {
   return f64::D3{p[i], p[stride + i], p[2 * stride + i]};
 }
 
+// The min key holds the signed square of the extra dt; 1e40 = (1e20)^2 is
+// the reference's initial extra dt (adiabatic.hpp:545) and the isothermal
+// solver's only candidate (isothermal.hpp:262-267).
+constexpr double kNoExtraSq = 1e40;
+
 // Order-preserving 64-bit keys of doubles: unsigned comparison of the keys
 // orders the values, so the dt clip's max and min are exact integer
 // atomics (no FP64 work, independent of the reduction order).
@@ -92,8 +98,8 @@ __device__ __forceinline__ double key_value(unsigned long long k) {
 // Warp-reduces the dt candidates (NaN ignored, like the reference's
 // comparisons) and folds them into the global keys with one atomic each.
 __device__ __forceinline__ void fold_candidates(double vmax2, double dmin, unsigned long long* keys) {
-  unsigned long long kmax = isnan(vmax2) ? 0ull : order_key(vmax2);
-  unsigned long long kmin = isnan(dmin) ? ~0ull : order_key(dmin);
+  unsigned long long kmax = fpc::is_nan_bits(vmax2) ? 0ull : order_key(vmax2);
+  unsigned long long kmin = fpc::is_nan_bits(dmin) ? ~0ull : order_key(dmin);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     const unsigned long long a = __shfl_down_sync(0xffffffffu, kmax, o);
@@ -107,41 +113,63 @@ __device__ __forceinline__ void fold_candidates(double vmax2, double dmin, unsig
   }
 }
 
-// FP64 pressure recovery with one division: Pi = (E - |r x l|^2/(2 Sigma))(gam-1),
-// floored at 1e-16 like MUSCL_base.hpp:538.  Also returns |v|^2 and 1/Sigma
-// for the dt candidates.
-__device__ __forceinline__ double pressure_recover(const double* u, f64::D3 r, double gam,
+// 1/x in FP64 by one Newton-Raphson step r1 = r0 + r0 (1 - x r0) from the
+// FP32 reciprocal r0: the step squares the seed's relative error (about
+// 2^-22), so r1 is within about 2^-43 of 1/x, far below the FP32 rounding of
+// every value it feeds (face states) and irrelevant to the dt candidates.
+// Two FP64 fused multiply-adds instead of a correctly rounded division.  An
+// x outside the FP32 range (seed 0, inf or NaN; x = 0 included) takes the
+// exact division, so zeros, infinities and NaN behave as 1.0 / x.
+__device__ __forceinline__ double recip_nr(double x) {
+  const float rf = 1.0f / fpc::d2f(x);
+  if (!(fabsf(rf) <= 3.0e38f) || rf == 0.0f) return 1.0 / x;
+  const double r0 = fpc::f2d(rf);
+  return fma(r0, fma(-x, r0, 1.0), r0);
+}
+
+// FP64 pressure recovery: Pi = (E - |r x l|^2/(2 Sigma))(gam-1), floored at
+// 1e-16 like MUSCL_base.hpp:538.  Also returns |v|^2 and 1/Sigma for the dt
+// candidates.
+__device__ __forceinline__ double pressure_recover(const double* u, f64::D3 r, double gam_m1,
                                                    double& v2, double& inv_rho) {
   const f64::D3 c = f64::cross3(r, f64::d3(u[1], u[2], u[3]));
-  inv_rho = 1.0 / u[0];
+  inv_rho = recip_nr(u[0]);
   const double c2 = c.x * c.x + c.y * c.y + c.z * c.z;
   v2 = c2 * inv_rho * inv_rho;
-  const double p = (u[4] - 0.5 * c2 * inv_rho) * (gam - 1.0);
+  const double p = (u[4] - 0.5 * c2 * inv_rho) * gam_m1;
   return (1e-16 < p) ? p : 1e-16;
 }
 
 __device__ __forceinline__ void store_w32(float* W32, int fp, int f, const double* u, double p) {
-  const float v[kDim] = {(float)u[0], (float)u[1], (float)u[2], (float)u[3], (float)p};
+  const float v[kDim] = {fpc::d2f(u[0]), fpc::d2f(u[1]), fpc::d2f(u[2]), fpc::d2f(u[3]), fpc::d2f(p)};
   st5(W32, fp, f, v);
 }
 
-// dt candidates in FP64 with one sqrt and one division: the CFL maximum is
-// reduced over squared speeds max(|v|^2, gam p / Sigma) (the square root is
-// monotone, so the dt finalize takes one sqrt of the maximum), and
+// dt candidates in FP64 without a square root or a division per face.
+// The CFL maximum is reduced over squared speeds max(|v|^2, gam p / Sigma).
 // extra_dt_constr (physics/adiabatic.hpp:543-580) simplifies to
-// 0.01 p / (alpha k g_eff Sigma |v - v0|) with k = gam3d / (2 gam3d - 1).
+// d = A / (B |v - v0|) with A = 0.01 p, B = alpha k g_eff Sigma and
+// k = gam3d / (2 gam3d - 1); it is reduced as the signed square
+// sgn(d) d^2 = sgn(B) A^2 / (B^2 |v - v0|^2), which orders like d (x |x| is
+// increasing), so the finalize takes one square root of the minimum.  The
+// sign comes from B's sign bit, so the zero-denominator cases give the
+// infinities of the direct quotient with their signs.  Both square roots are
+// exact up to rounding; the candidates are compared, not accumulated.
 __device__ __forceinline__ void dt_candidates_sq(const double* u, f64::D3 r, double p, double v2,
                                                  double inv_rho, const PhysParams& P, double& vmax2,
-                                                 double& dmin) {
+                                                 double& dmin_sq) {
   vmax2 = fmax(v2, P.gam * p * inv_rho);
   const f64::D3 c = f64::cross3(r, f64::d3(u[1], u[2], u[3]));
   // v = (r x l) / (-Sigma) ; v0 = omega_ns z x r
   const double vx = -c.x * inv_rho + P.omega_ns * r.y;
   const double vy = -c.y * inv_rho - P.omega_ns * r.x;
   const double vz = -c.z * inv_rho;
-  const double dv = sqrt(vx * vx + vy * vy + vz * vz);
+  const double d2 = vx * vx + vy * vy + vz * vz;
   const double g_eff = 0.217909 - v2;
-  dmin = 0.01 * p / (P.alpha * P.fric_k * g_eff * u[0] * dv);
+  const double A = 0.01 * p;
+  const double B = P.fric_ak * g_eff * u[0];
+  const double q = (A * A) * recip_nr((B * B) * d2);
+  dmin_sq = signbit(B) ? -q : q;
 }
 
 // physics/adiabatic.hpp:396-541 in FP32, except the accretion mass source
@@ -218,20 +246,20 @@ __device__ __forceinline__ void source_f32(const float* w, F3 fcn, float acc0, c
 // isothermal sound speed); no extra constraint (isothermal.hpp:262-267).
 __device__ __forceinline__ void iso_w32_candidates(const double* u, f64::D3 r, float* W32, int fp, int f,
                                                    double& vmax2, double& dmin) {
-  const float v[kDim] = {(float)u[0], (float)u[1], (float)u[2], (float)u[3], 0.f};
+  const float v[kDim] = {fpc::d2f(u[0]), fpc::d2f(u[1]), fpc::d2f(u[2]), fpc::d2f(u[3]), 0.f};
   st5(W32, fp, f, v);
   const f64::D3 c = f64::cross3(r, f64::d3(u[1], u[2], u[3]));
-  const double inv_rho = 1.0 / u[0];
+  const double inv_rho = recip_nr(u[0]);
   const double v2 = (c.x * c.x + c.y * c.y + c.z * c.z) * inv_rho * inv_rho;
   vmax2 = fmax(v2, 1.0);
-  dmin = 1e20;
+  dmin = kNoExtraSq;
 }
 
 // W32 and the dt candidates of the current U for face f (all 32 lanes of a
 // warp call it; lanes past the last face contribute neutral values).
 __device__ __forceinline__ void prepare_body(const DevGeomMixed& G, const DevState& S,
                                              const PhysParams& P, int f) {
-  double vmax = 0.0, dmin = 1e20;
+  double vmax = 0.0, dmin = kNoExtraSq;
   if (f < G.n_faces) {
     double u[kDim];
 #pragma unroll
@@ -241,7 +269,7 @@ __device__ __forceinline__ void prepare_body(const DevGeomMixed& G, const DevSta
       iso_w32_candidates(u, r, S.W32, G.fpad, f, vmax, dmin);
     } else {
       double v2, inv_rho;
-      const double p = pressure_recover(u, r, P.gam, v2, inv_rho);
+      const double p = pressure_recover(u, r, P.gam_m1, v2, inv_rho);
       store_w32(S.W32, G.fpad, f, u, p);
       dt_candidates_sq(u, r, p, v2, inv_rho, P, vmax, dmin);
     }
@@ -253,11 +281,12 @@ __global__ void __launch_bounds__(128) prepare_kernel(DevGeomMixed G, DevState S
   prepare_body(G, S, P, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
-// initial keys: max |v|^2 starts at (1e-8)^2 and min extra dt at 1e20, the
-// reference's initial values (MUSCL_base.hpp:314, adiabatic.hpp:545)
+// initial keys: max |v|^2 starts at (1e-8)^2 and min extra dt at 1e20 (as
+// its square), the reference's initial values (MUSCL_base.hpp:314,
+// adiabatic.hpp:545)
 __global__ void reset_keys_kernel(unsigned long long* keys) {
   keys[0] = order_key(1e-16);
-  keys[1] = order_key(1e20);
+  keys[1] = order_key(kNoExtraSq);
 }
 
 // dt = min(dt0, 0.1 h0 / max_vel, extra_dt) (MUSCL_base.hpp:100-115), time,
@@ -265,7 +294,8 @@ __global__ void reset_keys_kernel(unsigned long long* keys) {
 __device__ __forceinline__ void finalize_body(const DevState& S, const PhysParams& P, double dt0) {
   griddep_wait();
   const double max_vel = sqrt(key_value(S.keys[0]));
-  double extra = key_value(S.keys[1]);
+  const double xs = key_value(S.keys[1]);
+  double extra = (xs >= kNoExtraSq) ? 1e20 : (xs < 0 ? -sqrt(-xs) : sqrt(xs));
   if (extra < 0) {
     atomicOr(S.err, 8u);  // SPLASH_STOP_NEG_EXTRA_DT
     extra = 1e20;
@@ -274,13 +304,14 @@ __device__ __forceinline__ void finalize_body(const DevState& S, const PhysParam
   if (dt > P.h0 * 0.1 / max_vel) dt = P.h0 * 0.1 / max_vel;
   if (dt > extra) dt = extra;
   S.scal[kScDt] = dt;
+  S.scal[kScDtHalf] = dt / 2;
   *reinterpret_cast<float2*>(S.scal + kScDtF) = make_float2((float)dt, (float)(dt / 2));
   S.scal[kScDt0] = dt0;
   S.scal[kScMaxVel] = max_vel;
   S.scal[kScExtraDt] = extra;
   S.scal[kScTime] = S.scal[kScTime] + dt;
   S.keys[0] = order_key(1e-16);
-  S.keys[1] = order_key(1e20);
+  S.keys[1] = order_key(kNoExtraSq);
 }
 
 __global__ void finalize_kernel(DevState S, PhysParams P, double dt0) {
@@ -368,11 +399,13 @@ __global__ void __launch_bounds__(kBlock, 10) reconstruct_kernel(DevGeomMixed G,
 constexpr int kFaceTile = 32;   // faces per flux block (x)
 constexpr int kMaxSlotLanes = 8;  // slot lanes per face (y), >= max_slots
 
-// find_flux_var + res2d + RK combine (MUSCL_base.hpp:345-359, 238-276,
-// 124-161).  Block = 32 faces x max_slots slot lanes: every (face, slot)
-// thread evaluates one Riemann flux and parks its contribution in shared
-// memory; then one warp sums each face's contributions in slot order
-// (compensated), adds the source and does the FP64 update.
+// find_flux_var + res2d (MUSCL_base.hpp:345-359, 238-276).  Block = 32
+// faces x max_slots slot lanes: every (face, slot) thread evaluates one
+// Riemann flux and parks dt coef F in shared memory; then warp k sums field
+// k of each face over its slots in slot order (compensated) and stores the
+// FP32 flux increment.  The per-face FP64 work (source, RK combine, pressure
+// recovery, dt candidates) is the update launch, one thread per face, so
+// that it runs at full occupancy instead of on one warp per flux block.
 struct FluxShared {
   float contrib[kMaxSlotLanes][kDim][kFaceTile];
   unsigned bits;
@@ -425,39 +458,62 @@ __device__ __forceinline__ void flux_body(const DevGeomMixed& G, const DevState&
     for (int k = 0; k < kDim; ++k) contrib[ty][k][tx] = -cf * F[k];
   }
   __syncthreads();
-  if (ty != 0) return;
-  if (tx == 0 && sbits) atomicOr(S.err, sbits);
-  double vmax = 0.0, dmin = 1e20;
-  if (f < G.n_faces) {
+  if (tx == 0 && ty == 0 && sbits) atomicOr(S.err, sbits);
+  if (f >= G.n_faces) return;
+  const int n = G.nslots[f];
+  for (int k = ty; k < kDim; k += blockDim.y) {
+    Acc acc{0.f, 0.f};
+    for (int j = 0; j < n; ++j) acc.add(contrib[j][k][tx]);
+    S.inc32[(size_t)k * fp + f] = acc.hi + acc.lo;
+  }
+}
+
+// at most 51 registers (5 blocks of up to 256 threads per SM)
+template <int STAGE>
+__global__ void __launch_bounds__(kFaceTile * kMaxSlotLanes, 5) flux_kernel(DevGeomMixed G, DevState S,
+                                                                         PhysParams P) {
+  __shared__ FluxShared sh;
+  griddep_launch_dependents();
+  flux_body<STAGE>(G, S, P, blockIdx.x * kFaceTile, sh);
+}
+
+// RK combine (MUSCL_base.hpp:124-161) of face f: U_stage = U0 + (flux
+// increment + dt_here * source), the source in FP32 from the face state
+// (physics/adiabatic.hpp:396-541) except the accretion mass source, added in
+// FP64; the density floor, FP64 pressure recovery, the FP32 face state of
+// the next stage, and in stage 2 the new U and the dt candidates.  Every
+// lane of the calling warp must call it (the candidates fold per warp).
+template <int STAGE>
+__device__ __forceinline__ void update_body(const DevGeomMixed& G, const DevState& S, const PhysParams& P,
+                                            int f) {
+  const int fp = G.fpad;
+  const bool live = f < G.n_faces;
+  F3 fcn32 = f3(0.f, 0.f, 0.f);
+  double acc0 = 0.0;
+  f64::D3 r{0.0, 0.0, 0.0};
+  if (live) {
+    fcn32 = plane3f(G.fcn32, fp, f);
+    acc0 = G.acc_src[f];
+    r = plane3d(G.fcn, fp, f);
+  }
+  griddep_wait();
+  double vmax = 0.0, dmin = kNoExtraSq;
+  if (live) {
+    const float2 dtf2 = *reinterpret_cast<const float2*>(S.scal + kScDtF);
+    const float dtf = (STAGE == 1) ? dtf2.y : dtf2.x;
     float w[kDim], src[kDim];
     ld5(S.W32, fp, f, w);
-    const F3 fcn32 = plane3f(G.fcn32, fp, f);
-    const double acc0 = G.acc_src[f];
-    source_f32(w, fcn32, (float)acc0, P, src);
-    Acc acc[kDim];
-#pragma unroll
-    for (int k = 0; k < kDim; ++k) {
-      acc[k].hi = dtf * src[k];
-      acc[k].lo = 0.f;
-    }
-    const int n = G.nslots[f];
-    for (int j = 0; j < n; ++j) {
-#pragma unroll
-      for (int k = 0; k < kDim; ++k) acc[k].add(contrib[j][k][tx]);
-    }
-    // the compensated FP32 sum is rounded once to FP32 (an increment of
-    // dt * Phi, small against U) and added to the FP64 state; U0 stays in
-    // S.U until stage 2 overwrites it
+    source_f32(w, fcn32, fpc::d2f(acc0), P, src);
+    // the FP32 increment (flux sum + dt source, one rounding) is added to
+    // the FP64 state; U0 stays in S.U until stage 2 overwrites it
     double u[kDim];
 #pragma unroll
-    for (int k = 0; k < kDim; ++k) u[k] = S.U[k * fp + f] + (double)(acc[k].hi + acc[k].lo);
+    for (int k = 0; k < kDim; ++k) u[k] = S.U[k * fp + f] + fpc::f2d(S.inc32[(size_t)k * fp + f] + dtf * src[k]);
     if (P.accretion_on) {  // accretion mass source in FP64
-      const double dt = S.scal[kScDt];
-      const double dt_here = (STAGE == 1) ? dt / 2 : dt;
+      const double dt_here = S.scal[(STAGE == 1) ? kScDtHalf : kScDt];
       u[0] += dt_here * acc0;
     }
     if (u[0] < 1e-8) u[0] = 1e-8;
-    const f64::D3 r = plane3d(G.fcn, fp, f);
     if (P.solver == kSolverIsoHLLE) {
       u[4] = 0.0;
       double vm, dm;
@@ -470,7 +526,7 @@ __device__ __forceinline__ void flux_body(const DevGeomMixed& G, const DevState&
       }
     } else {
       double v2, inv_rho;
-      const double p = pressure_recover(u, r, P.gam, v2, inv_rho);
+      const double p = pressure_recover(u, r, P.gam_m1, v2, inv_rho);
       store_w32(S.W32, fp, f, u, p);
       if (STAGE == 2) {
 #pragma unroll
@@ -482,14 +538,10 @@ __device__ __forceinline__ void flux_body(const DevGeomMixed& G, const DevState&
   if (STAGE == 2) fold_candidates(vmax, dmin, S.keys);
 }
 
-// at most 51 registers (5 blocks of up to 256 threads per SM): the measured
-// optimum between occupancy and the small spill it costs
 template <int STAGE>
-__global__ void __launch_bounds__(kFaceTile * kMaxSlotLanes, 5) flux_update_kernel(DevGeomMixed G, DevState S,
-                                                                                PhysParams P) {
-  __shared__ FluxShared sh;
+__global__ void __launch_bounds__(kBlock) update_kernel(DevGeomMixed G, DevState S, PhysParams P) {
   griddep_launch_dependents();
-  flux_body<STAGE>(G, S, P, blockIdx.x * kFaceTile, sh);
+  update_body<STAGE>(G, S, P, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // ---------------------------------------------------------------- ensemble
@@ -507,7 +559,7 @@ __global__ void ens_reset_keys_kernel(const EnsInstance* __restrict__ inst, int 
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) {
     inst[i].S.keys[0] = order_key(1e-16);
-    inst[i].S.keys[1] = order_key(1e20);
+    inst[i].S.keys[1] = order_key(kNoExtraSq);
   }
 }
 
@@ -533,6 +585,19 @@ __global__ void __launch_bounds__(kFaceTile * kMaxSlotLanes, 5) ens_flux_kernel(
   const int2 t = tiles[blockIdx.x];
   const EnsInstance& I = inst[t.x];
   flux_body<STAGE>(I.G, I.S, I.P, t.y, sh);
+}
+
+// update: one 32-face tile per warp, kUpdTiles tiles per block
+constexpr int kUpdTiles = kBlock / 32;
+template <int STAGE>
+__global__ void __launch_bounds__(kBlock) ens_update_kernel(const EnsInstance* __restrict__ inst,
+                                                            const int2* __restrict__ tiles, int n_tiles) {
+  griddep_launch_dependents();
+  const int tile = blockIdx.x * kUpdTiles + (threadIdx.x >> 5);
+  if (tile >= n_tiles) return;  // whole warps: the candidates fold per warp
+  const int2 t = tiles[tile];
+  const EnsInstance& I = inst[t.x];
+  update_body<STAGE>(I.G, I.S, I.P, t.y + (threadIdx.x & 31));
 }
 
 inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
@@ -576,6 +641,7 @@ cudaError_t mixed_step(const DevGeomMixed& G, const DevState& S, const PhysParam
   const int ntile = (G.n_faces + mx::kFaceTile - 1) / mx::kFaceTile;
   const dim3 rgrid(mx::blocks_for(G.n_faces), G.max_slots);
   const dim3 fblock(mx::kFaceTile, G.max_slots);
+  const dim3 ugrid(mx::blocks_for(G.n_faces));
   cudaError_t e = cudaSuccess;
   auto chk = [&](cudaError_t r) {
     if (e == cudaSuccess) e = r;
@@ -585,11 +651,13 @@ cudaError_t mixed_step(const DevGeomMixed& G, const DevState& S, const PhysParam
   if (ev) cudaEventRecord(ev[1], st);
   chk(launch_pdl(mx::reconstruct_kernel, rgrid, dim3(mx::kBlock), st, G, S, P));
   if (ev) cudaEventRecord(ev[2], st);
-  chk(launch_pdl(mx::flux_update_kernel<1>, dim3(ntile), fblock, st, G, S, P));
+  chk(launch_pdl(mx::flux_kernel<1>, dim3(ntile), fblock, st, G, S, P));
+  chk(launch_pdl(mx::update_kernel<1>, ugrid, dim3(mx::kBlock), st, G, S, P));
   if (ev) cudaEventRecord(ev[3], st);
   chk(launch_pdl(mx::reconstruct_kernel, rgrid, dim3(mx::kBlock), st, G, S, P));
   if (ev) cudaEventRecord(ev[4], st);
-  chk(launch_pdl(mx::flux_update_kernel<2>, dim3(ntile), fblock, st, G, S, P));
+  chk(launch_pdl(mx::flux_kernel<2>, dim3(ntile), fblock, st, G, S, P));
+  chk(launch_pdl(mx::update_kernel<2>, ugrid, dim3(mx::kBlock), st, G, S, P));
   if (ev) cudaEventRecord(ev[5], st);
   return e != cudaSuccess ? e : cudaGetLastError();
 }
@@ -612,9 +680,12 @@ cudaError_t ensemble_step(const EnsInstance* inst, int n_inst, const int2* rtile
   };
   chk(launch_pdl(mx::ens_finalize_kernel, dim3((n_inst + 127) / 128), dim3(128), st, inst, n_inst, dt0));
   chk(launch_pdl(mx::ens_reconstruct_kernel, rgrid, dim3(recon_width), st, inst, rtiles));
+  const dim3 ugrid((n_ftiles + mx::kUpdTiles - 1) / mx::kUpdTiles);
   chk(launch_pdl(mx::ens_flux_kernel<1>, dim3(n_ftiles), fblock, st, inst, ftiles));
+  chk(launch_pdl(mx::ens_update_kernel<1>, ugrid, dim3(mx::kBlock), st, inst, ftiles, n_ftiles));
   chk(launch_pdl(mx::ens_reconstruct_kernel, rgrid, dim3(recon_width), st, inst, rtiles));
   chk(launch_pdl(mx::ens_flux_kernel<2>, dim3(n_ftiles), fblock, st, inst, ftiles));
+  chk(launch_pdl(mx::ens_update_kernel<2>, ugrid, dim3(mx::kBlock), st, inst, ftiles, n_ftiles));
   return e != cudaSuccess ? e : cudaGetLastError();
 }
 
