@@ -178,13 +178,20 @@ void Solver::build_device_geometry(const RefGeometry& g) {
     GM.arc_a = upload(mp.arc);
     GM.ec = upload(mp.ec);
     GM.en = upload(mp.en);
-    GM.nxr = upload(mp.nxr);
     GM.coef = upload(mp.coef);
-    GM.rev = upload(sp.rev);
+    GM.slot_edge = upload(mp.slot_edge);
+    GM.n_edges = mp.n_edges;
+    GM.epad = mp.epad;
+    GM.e_own = upload(mp.e_own);
+    GM.e_nbr = upload(mp.e_nbr);
+    GM.e_ec = upload(mp.e_ec);
+    GM.e_en = upload(mp.e_en);
+    GM.e_nxr = upload(mp.e_nxr);
     geometry_bytes = sp.nslots.size() + 8 * (sp.fcn.size() + sp.area.size() + acc.size()) +
-                     4 * (sp.sten.size() + sp.rev.size() + mp.fcn32.size() + mp.beta.size() +
-                          mp.inv_h.size() + mp.bm.size() + mp.eta.size() + mp.arc.size() +
-                          mp.ec.size() + mp.en.size() + mp.nxr.size() + mp.coef.size());
+                     4 * (sp.sten.size() + mp.fcn32.size() + mp.beta.size() + mp.inv_h.size() +
+                          mp.bm.size() + mp.eta.size() + mp.arc.size() + mp.ec.size() + mp.en.size() +
+                          mp.coef.size() + mp.slot_edge.size() + mp.e_own.size() + mp.e_nbr.size() +
+                          mp.e_ec.size() + mp.e_en.size() + mp.e_nxr.size());
   } else {
     G.n_faces = n_faces;
     G.fpad = fpad;
@@ -450,7 +457,7 @@ int splash_create(const splash_mesh_desc* mesh, const double* U_in, int dim, dou
     if (precision == SPLASH_PREC_MIXED) {
       S.W32 = s->dalloc<float>(splash::kDim * fp);
       S.uplus32 = s->dalloc<float>(splash::kDim * PS);
-      S.inc32 = s->dalloc<float>(splash::kDim * fp);
+      S.fe32 = s->dalloc<float>(splash::kDim * (size_t)s->GM.epad);
       S.uplus = nullptr;
       SPLASH_CUDA(cudaMemset(S.W32, 0, splash::kDim * fp * sizeof(float)));
       SPLASH_CUDA(cudaMemset(S.uplus32, 0, splash::kDim * PS * sizeof(float)));

@@ -58,14 +58,15 @@ struct Ensemble {
   std::vector<int> member_level;
   std::vector<size_t> off_face;   // member offset into per-face pools (multiples of fpad)
   std::vector<size_t> off_slot;   // member offset into the per-slot pool
+  std::vector<size_t> off_edge;   // member offset into the per-edge pool (multiples of epad)
   std::vector<EnsInstance> inst;
   EnsInstance* d_inst = nullptr;
   double *U = nullptr, *acc = nullptr, *scal = nullptr, *U_snap = nullptr, *scal_snap = nullptr;
-  float *W32 = nullptr, *uplus = nullptr, *inc32 = nullptr;
+  float *W32 = nullptr, *uplus = nullptr, *fe32 = nullptr;
   unsigned int *err = nullptr, *err_snap = nullptr;
   unsigned long long* keys = nullptr;
-  int2 *d_rtiles = nullptr, *d_ftiles = nullptr;
-  int n_rtiles = 0, n_ftiles = 0;
+  int2 *d_rtiles = nullptr, *d_ftiles = nullptr, *d_etiles = nullptr;
+  int n_rtiles = 0, n_ftiles = 0, n_etiles = 0;
   int order = 0, recon_width = 128;
   double tuned_ms[9] = {0};
   std::vector<void*> allocs;
@@ -101,21 +102,23 @@ struct Ensemble {
     return d;
   }
 
-  // Tiles of `width` faces of every member, in schedule order:
-  // 0 member order, 1 largest members first, 2 round-robin across members.
-  std::vector<int2> make_tiles(int width, int ord) const {
+  // Tiles of `width` faces (edges, with `edges`) of every member, in
+  // schedule order: 0 member order, 1 largest members first, 2 round-robin
+  // across members.
+  std::vector<int2> make_tiles(int width, int ord, bool edges = false) const {
+    auto count = [&](int i) { return edges ? inst[i].G.n_edges : inst[i].G.n_faces; };
     std::vector<int> members(n);
     for (int i = 0; i < n; ++i) members[i] = i;
     if (ord != 0)
       std::stable_sort(members.begin(), members.end(), [&](int a, int b) {
-        return inst[a].G.n_faces > inst[b].G.n_faces;
+        return count(a) > count(b);
       });
     std::vector<int2> t;
     if (ord == 2) {
       for (int k = 0;; ++k) {
         bool any = false;
         for (int i : members) {
-          if (k * width < inst[i].G.n_faces) {
+          if (k * width < count(i)) {
             t.push_back(make_int2(i, k * width));
             any = true;
           }
@@ -124,7 +127,7 @@ struct Ensemble {
       }
     } else {
       for (int i : members)
-        for (int f0 = 0; f0 < inst[i].G.n_faces; f0 += width) t.push_back(make_int2(i, f0));
+        for (int f0 = 0; f0 < count(i); f0 += width) t.push_back(make_int2(i, f0));
     }
     return t;
   }
@@ -132,15 +135,19 @@ struct Ensemble {
   int set_schedule(int ord, int width) {
     const std::vector<int2> rt = make_tiles(width, ord);
     const std::vector<int2> ft = make_tiles(32, ord);
+    const std::vector<int2> et = make_tiles(32, ord, true);
     if (!d_rtiles) {
       // capacity for the smallest width (the most tiles)
       d_rtiles = dalloc<int2>(make_tiles(64, 0).size());
       d_ftiles = dalloc<int2>(ft.size());
+      d_etiles = dalloc<int2>(et.size());
     }
     ENS_CUDA(cudaMemcpy(d_rtiles, rt.data(), rt.size() * sizeof(int2), cudaMemcpyHostToDevice));
     ENS_CUDA(cudaMemcpy(d_ftiles, ft.data(), ft.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    ENS_CUDA(cudaMemcpy(d_etiles, et.data(), et.size() * sizeof(int2), cudaMemcpyHostToDevice));
     n_rtiles = (int)rt.size();
     n_ftiles = (int)ft.size();
+    n_etiles = (int)et.size();
     order = ord;
     recon_width = width;
     return SPLASH_OK;
@@ -152,7 +159,8 @@ struct Ensemble {
   }
 
   cudaError_t launch_step(double dt0) {
-    return ensemble_step(d_inst, n, d_rtiles, n_rtiles, recon_width, d_ftiles, n_ftiles, max_slots, dt0,
+    return ensemble_step(d_inst, n, d_rtiles, n_rtiles, recon_width, d_ftiles, n_ftiles, d_etiles, n_etiles,
+                         max_slots, dt0,
                          stream);
   }
 
@@ -305,9 +313,15 @@ int splash_ensemble_create(const splash_member* members, int n, int device, int 
         L.G.arc_a = e->upload(mp.arc);
         L.G.ec = e->upload(mp.ec);
         L.G.en = e->upload(mp.en);
-        L.G.nxr = e->upload(mp.nxr);
         L.G.coef = e->upload(mp.coef);
-        L.G.rev = e->upload(L.sp.rev);
+        L.G.slot_edge = e->upload(mp.slot_edge);
+        L.G.n_edges = mp.n_edges;
+        L.G.epad = mp.epad;
+        L.G.e_own = e->upload(mp.e_own);
+        L.G.e_nbr = e->upload(mp.e_nbr);
+        L.G.e_ec = e->upload(mp.e_ec);
+        L.G.e_en = e->upload(mp.e_en);
+        L.G.e_nxr = e->upload(mp.e_nxr);
         it = level_of.emplace(key, (int)e->levels.size()).first;
         e->levels.push_back(std::move(L));
       }
@@ -315,13 +329,15 @@ int splash_ensemble_create(const splash_member* members, int n, int device, int 
       e->max_slots = std::max(e->max_slots, e->levels[it->second].sp.max_slots);
     }
     // pooled state
-    size_t faces = 0, slots = 0;
+    size_t faces = 0, slots = 0, edges = 0;
     for (int i = 0; i < n; ++i) {
       const splash::Level& L = e->levels[e->member_level[i]];
       e->off_face.push_back(faces);
       e->off_slot.push_back(slots);
+      e->off_edge.push_back(edges);
       faces += (size_t)L.sp.fpad;
       slots += L.sp.PS();
+      edges += (size_t)L.G.epad;
     }
     e->total_faces = faces;
     e->U = e->dalloc<double>(faces * kDim);
@@ -329,7 +345,7 @@ int splash_ensemble_create(const splash_member* members, int n, int device, int 
     e->acc = e->dalloc<double>(faces);
     e->W32 = e->dalloc<float>(faces * kDim);
     e->uplus = e->dalloc<float>(slots * kDim);
-    e->inc32 = e->dalloc<float>(faces * kDim);
+    e->fe32 = e->dalloc<float>(edges * kDim);
     e->scal = e->dalloc<double>((size_t)n * kScCount);
     e->scal_snap = e->dalloc<double>((size_t)n * kScCount);
     e->err = e->dalloc<unsigned int>((size_t)n * 4);
@@ -362,7 +378,7 @@ int splash_ensemble_create(const splash_member* members, int n, int device, int 
       I.S.U = e->U + e->off_face[i] * kDim;
       I.S.W32 = e->W32 + e->off_face[i] * kDim;
       I.S.uplus32 = e->uplus + e->off_slot[i] * kDim;
-      I.S.inc32 = e->inc32 + e->off_face[i] * kDim;
+      I.S.fe32 = e->fe32 + e->off_edge[i] * kDim;
       I.S.scal = e->scal + (size_t)i * kScCount;
       I.S.err = e->err + (size_t)i * 4;
       I.S.keys = e->keys + (size_t)i * 2;

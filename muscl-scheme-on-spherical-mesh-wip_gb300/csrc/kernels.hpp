@@ -40,13 +40,14 @@ const void* mixed_finalize_kernel_ptr();
 int mixed_partial_blocks(int n_faces);
 
 // ---- ensemble (step_mixed.cu): batched launches over instances ----
-// ftiles: (instance, first face) of 32-face tiles; rtiles: tiles of
-// `recon_width` faces for the reconstruction (blockDim.x = recon_width).
+// ftiles: (instance, first face) of 32-face tiles; etiles: (instance,
+// first edge) of 32-edge tiles; rtiles: tiles of `recon_width` faces for the
+// reconstruction (blockDim.x = recon_width).
 cudaError_t ensemble_prepare(const EnsInstance* inst, int n_inst, const int2* ftiles, int n_ftiles,
                              cudaStream_t st);
 cudaError_t ensemble_step(const EnsInstance* inst, int n_inst, const int2* rtiles, int n_rtiles,
-                          int recon_width, const int2* ftiles, int n_ftiles, int max_slots, double dt0,
-                          cudaStream_t st);
+                          int recon_width, const int2* ftiles, int n_ftiles, const int2* etiles, int n_etiles,
+                          int max_slots, double dt0, cudaStream_t st);
 const void* ensemble_finalize_kernel_ptr();
 
 }  // namespace splash

@@ -110,9 +110,16 @@ struct DevGeomMixed {
   const float* arc_a;
   const float* ec;        // 3 planes, unit edge centre
   const float* en;        // 3 planes
-  const float* nxr;       // 3 planes
   const float* coef;      // round_diff * chord / area
-  const int* rev;
+  const int* slot_edge;   // edge of the slot, bit 31 set on the edge's reverse side
+  // interior edges, each once, in the orientation of the owner slot
+  int n_edges;
+  int epad;               // n_edges rounded up to 32
+  const int* e_own;       // [epad] owner slot (slot-plane index)
+  const int* e_nbr;       // [epad] reverse slot
+  const float* e_ec;      // 3 planes of epad, the owner's unit edge centre
+  const float* e_en;      // 3 planes of epad
+  const float* e_nxr;     // 3 planes of epad, cross(en, ec)
 };
 
 // Solver state on the device.
@@ -123,7 +130,7 @@ struct DevState {
   double* uplus;  // reconstructed edge states, kDim * max_slots planes of fpad
   float* W32;     // mixed path: (Sigma, l, Pi) in FP32: [fpad] float4 (Sigma, l), then a Pi plane
   float* uplus32; // mixed path: edge states, same packing over max_slots * fpad slots
-  float* inc32;   // mixed path: per-face FP32 flux increment of a stage, kDim planes of fpad
+  float* fe32;    // mixed path: FP32 Riemann flux of every edge, packed like W32 over epad edges
   double* partial;  // per-block partial records (kPartialStride doubles)
   double* scal;   // device scalars, see ScalarSlot
   unsigned int* err;  // stop bits

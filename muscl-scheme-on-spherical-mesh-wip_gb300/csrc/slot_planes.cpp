@@ -200,7 +200,6 @@ MixedPlanes make_mixed_planes(const SlotPlanes& sp) {
   mp.arc = tof(sp.arc);
   mp.ec = tof(sp.ec);
   mp.en = tof(sp.en);
-  mp.nxr = tof(sp.nxr);
   mp.inv_h.assign(2 * PS, 1.0f);
   for (size_t q = 0; q < 2 * PS; ++q) mp.inv_h[q] = (float)(1.0 / sp.hpm[q]);
   mp.coef.assign(PS, 0.0f);
@@ -209,6 +208,38 @@ MixedPlanes make_mixed_planes(const SlotPlanes& sp) {
       const size_t q = (size_t)j * sp.fpad + i;
       mp.coef[q] = (float)(sp.round_diff * sp.chord[q] / sp.area[i]);
     }
+  // edges in ascending owner order (plane-major, faces ascending within a
+  // plane): the reverse side of every edge is met either as an owner's
+  // neighbour before it, or as an owner itself
+  mp.slot_edge.assign(PS, 0);
+  for (int j = 0; j < sp.max_slots; ++j)
+    for (int i = 0; i < sp.n_faces; ++i) {
+      if (j >= (int)sp.nslots[i]) continue;
+      const int s = j * sp.fpad + i, r = sp.rev[s];
+      if (r == s) throw std::runtime_error("slot without a neighbour");
+      if (s < r) {
+        const int e = (int)mp.e_own.size();
+        mp.e_own.push_back(s);
+        mp.e_nbr.push_back(r);
+        mp.slot_edge[s] = e;
+        mp.slot_edge[r] = (int)((unsigned)e | 0x80000000u);
+      }
+    }
+  mp.n_edges = (int)mp.e_own.size();
+  mp.epad = (mp.n_edges + 31) / 32 * 32;
+  mp.e_own.resize(mp.epad, mp.n_edges ? mp.e_own[0] : 0);
+  mp.e_nbr.resize(mp.epad, mp.n_edges ? mp.e_nbr[0] : 0);
+  mp.e_ec.assign(3 * (size_t)mp.epad, 0.f);
+  mp.e_en.assign(3 * (size_t)mp.epad, 0.f);
+  mp.e_nxr.assign(3 * (size_t)mp.epad, 0.f);
+  for (int e = 0; e < mp.n_edges; ++e) {
+    const size_t s = (size_t)mp.e_own[e];
+    for (int c = 0; c < 3; ++c) {
+      mp.e_ec[c * (size_t)mp.epad + e] = mp.ec[c * PS + s];
+      mp.e_en[c * (size_t)mp.epad + e] = mp.en[c * PS + s];
+      mp.e_nxr[c * (size_t)mp.epad + e] = (float)sp.nxr[c * PS + s];
+    }
+  }
   return mp;
 }
 

@@ -47,9 +47,18 @@ std::vector<double> accretion_source_fcn(const std::vector<double>& fcn, int n_f
                                          std::vector<double>* d_rate = nullptr,
                                          std::vector<double>* d_tilt = nullptr);
 
-// FP32 planes of the mixed path.
+// FP32 planes of the mixed path.  The Riemann flux of an interior edge is
+// evaluated once, in the orientation of its owner: of the edge's two slots
+// the one with the smaller slot-plane index.  Edges are numbered in owner
+// order; slot_edge maps every slot to its edge, with bit 31 set on the
+// reverse (non-owner) side, whose flux is the owner's with the sign flipped
+// (every Riemann solver here satisfies F(uR, uL, -n) = -F(uL, uR, n)).
 struct MixedPlanes {
-  std::vector<float> fcn32, beta, inv_h, bm, eta, arc, ec, en, nxr, coef;
+  std::vector<float> fcn32, beta, inv_h, bm, eta, arc, ec, en, coef;
+  int n_edges = 0, epad = 0;           // epad: n_edges rounded up to 32
+  std::vector<int> e_own, e_nbr;       // [epad] slot-plane indices of the two sides
+  std::vector<float> e_ec, e_en, e_nxr;  // 3 planes of epad: the owner slot's geometry
+  std::vector<int> slot_edge;          // [max_slots * fpad]
 };
 MixedPlanes make_mixed_planes(const SlotPlanes& sp);
 

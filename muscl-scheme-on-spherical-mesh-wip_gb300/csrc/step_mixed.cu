@@ -396,93 +396,59 @@ __global__ void __launch_bounds__(kBlock, 10) reconstruct_kernel(DevGeomMixed G,
   recon_body(G, S, P, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
 }
 
-constexpr int kFaceTile = 32;   // faces per flux block (x)
-constexpr int kMaxSlotLanes = 8;  // slot lanes per face (y), >= max_slots
+constexpr int kFaceTile = 32;  // faces (or edges) per tile of the batched launches
 
-// find_flux_var + res2d (MUSCL_base.hpp:345-359, 238-276).  Block = 32
-// faces x max_slots slot lanes: every (face, slot) thread evaluates one
-// Riemann flux and parks dt coef F in shared memory; then warp k sums field
-// k of each face over its slots in slot order (compensated) and stores the
-// FP32 flux increment.  The per-face FP64 work (source, RK combine, pressure
-// recovery, dt candidates) is the update launch, one thread per face, so
-// that it runs at full occupancy instead of on one warp per flux block.
-struct FluxShared {
-  float contrib[kMaxSlotLanes][kDim][kFaceTile];
-  unsigned bits;
-};
-
-template <int STAGE>
-__device__ __forceinline__ void flux_body(const DevGeomMixed& G, const DevState& S, const PhysParams& P,
-                                          int face_begin, FluxShared& sh) {
-  float (&contrib)[kMaxSlotLanes][kDim][kFaceTile] = sh.contrib;
-  unsigned& sbits = sh.bits;
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  const int f = face_begin + tx;
-  const int fp = G.fpad;
-  const int PS = G.max_slots * fp;
-  const float gam = P.gam_f;
-  if (tx == 0 && ty == 0) sbits = 0;
-  // the slot's geometry does not depend on the predecessor kernel
-  const bool active = f < G.n_faces && ty < G.nslots[f];
-  const int s = ty * fp + f;
-  int rv = 0;
+// find_flux_var (MUSCL_base.hpp:345-359) per interior edge: one thread per
+// edge evaluates the Riemann flux once, in the orientation of the edge's
+// owner slot (own edge state left, the reverse slot's right, the owner's
+// geometry), and stores it packed like W32.  The reference evaluates the
+// flux from both faces; every solver here satisfies
+// F(uR, uL, -n) = -F(uL, uR, n), so the reverse side takes the owner's flux
+// negated (the two evaluations differ only by FP32 rounding) and each edge
+// conserves exactly what it moves.  Stop bits are folded per warp.
+__device__ __forceinline__ void edge_flux_body(const DevGeomMixed& G, const DevState& S, const PhysParams& P,
+                                               int e) {
+  const bool live = e < G.n_edges;
+  const int PS = G.max_slots * G.fpad;
+  int so = 0, sr = 0;
   SlotGeomF g;
-  float coef = 0.f;
-  if (active) {
-    rv = G.rev[s];
-    g.ec = plane3f(G.ec, PS, s);
-    g.en = plane3f(G.en, PS, s);
-    g.nxr = plane3f(G.nxr, PS, s);
-    coef = G.coef[s];
+  if (live) {
+    so = G.e_own[e];
+    sr = G.e_nbr[e];
+    g.ec = plane3f(G.e_ec, G.epad, e);
+    g.en = plane3f(G.e_en, G.epad, e);
+    g.nxr = plane3f(G.e_nxr, G.epad, e);
   }
   griddep_wait();
-  const float2 dtf2 = *reinterpret_cast<const float2*>(S.scal + kScDtF);
-  const float dtf = (STAGE == 1) ? dtf2.y : dtf2.x;
-  __syncthreads();
-  {
-    float F[kDim] = {0.f, 0.f, 0.f, 0.f, 0.f};
-    float cf = 0.f;
-    if (active) {
-      float uL[kDim], uR[kDim];
-      ld5(S.uplus32, PS, s, uL);
-      ld5(S.uplus32, PS, rv, uR);
-      unsigned bits = (P.solver == kSolverIsoHLLE) ? iso_flux_star(uL, uR, g, F)
-                                                   : flux_star(uL, uR, g, gam, P.solver, F);
+  unsigned bits = 0;
+  if (live) {
+    float uL[kDim], uR[kDim], F[kDim] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    ld5(S.uplus32, PS, so, uL);
+    ld5(S.uplus32, PS, sr, uR);
+    bits = (P.solver == kSolverIsoHLLE) ? iso_flux_star(uL, uR, g, F) : flux_star(uL, uR, g, P.gam_f, P.solver, F);
 #pragma unroll
-      for (int k = 0; k < kDim; ++k)
-        if (isnan(F[k])) bits |= 1u;
-      if (bits) atomicOr(&sbits, bits);
-      cf = dtf * coef;
-    }
-#pragma unroll
-    for (int k = 0; k < kDim; ++k) contrib[ty][k][tx] = -cf * F[k];
+    for (int k = 0; k < kDim; ++k)
+      if (isnan(F[k])) bits |= 1u;
+    st5(S.fe32, G.epad, e, F);
   }
-  __syncthreads();
-  if (tx == 0 && ty == 0 && sbits) atomicOr(S.err, sbits);
-  if (f >= G.n_faces) return;
-  const int n = G.nslots[f];
-  for (int k = ty; k < kDim; k += blockDim.y) {
-    Acc acc{0.f, 0.f};
-    for (int j = 0; j < n; ++j) acc.add(contrib[j][k][tx]);
-    S.inc32[(size_t)k * fp + f] = acc.hi + acc.lo;
-  }
+  bits = __reduce_or_sync(0xffffffffu, bits);
+  if ((threadIdx.x & 31) == 0 && bits) atomicOr(S.err, bits);
 }
 
-// at most 51 registers (5 blocks of up to 256 threads per SM)
-template <int STAGE>
-__global__ void __launch_bounds__(kFaceTile * kMaxSlotLanes, 5) flux_kernel(DevGeomMixed G, DevState S,
-                                                                         PhysParams P) {
-  __shared__ FluxShared sh;
+__global__ void __launch_bounds__(kBlock) edge_flux_kernel(DevGeomMixed G, DevState S, PhysParams P) {
   griddep_launch_dependents();
-  flux_body<STAGE>(G, S, P, blockIdx.x * kFaceTile, sh);
+  edge_flux_body(G, S, P, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
-// RK combine (MUSCL_base.hpp:124-161) of face f: U_stage = U0 + (flux
-// increment + dt_here * source), the source in FP32 from the face state
-// (physics/adiabatic.hpp:396-541) except the accretion mass source, added in
-// FP64; the density floor, FP64 pressure recovery, the FP32 face state of
-// the next stage, and in stage 2 the new U and the dt candidates.  Every
-// lane of the calling warp must call it (the candidates fold per warp).
+// res2d + RK combine (MUSCL_base.hpp:238-276, 124-161) of face f: the
+// slot contributions -dt_here coef F (F the edge flux, negated on the
+// reverse side) summed in slot order (Neumaier-compensated FP32), plus
+// dt_here times the source in FP32 from the face state
+// (physics/adiabatic.hpp:396-541), rounded once and added to the FP64 U0;
+// the accretion mass source in FP64; the density floor, FP64 pressure
+// recovery, the FP32 face state of the next stage, and in stage 2 the new U
+// and the dt candidates.  Every lane of the calling warp must call it (the
+// candidates fold per warp).
 template <int STAGE>
 __device__ __forceinline__ void update_body(const DevGeomMixed& G, const DevState& S, const PhysParams& P,
                                             int f) {
@@ -491,16 +457,32 @@ __device__ __forceinline__ void update_body(const DevGeomMixed& G, const DevStat
   F3 fcn32 = f3(0.f, 0.f, 0.f);
   double acc0 = 0.0;
   f64::D3 r{0.0, 0.0, 0.0};
+  int n = 0;
   if (live) {
     fcn32 = plane3f(G.fcn32, fp, f);
     acc0 = G.acc_src[f];
     r = plane3d(G.fcn, fp, f);
+    n = G.nslots[f];
   }
   griddep_wait();
   double vmax = 0.0, dmin = kNoExtraSq;
   if (live) {
     const float2 dtf2 = *reinterpret_cast<const float2*>(S.scal + kScDtF);
     const float dtf = (STAGE == 1) ? dtf2.y : dtf2.x;
+    Acc acc[kDim];
+#pragma unroll
+    for (int k = 0; k < kDim; ++k) acc[k] = Acc{0.f, 0.f};
+    for (int j = 0; j < n; ++j) {
+      const int q = j * fp + f;
+      const int se = G.slot_edge[q];
+      const float cf = dtf * G.coef[q];
+      // -cf F with F = Fe on the owner side and -Fe on the reverse side
+      const float c = (se < 0) ? cf : -cf;
+      float fe[kDim];
+      ld5(S.fe32, G.epad, se & 0x7fffffff, fe);
+#pragma unroll
+      for (int k = 0; k < kDim; ++k) acc[k].add(c * fe[k]);
+    }
     float w[kDim], src[kDim];
     ld5(S.W32, fp, f, w);
     source_f32(w, fcn32, fpc::d2f(acc0), P, src);
@@ -508,7 +490,7 @@ __device__ __forceinline__ void update_body(const DevGeomMixed& G, const DevStat
     // the FP64 state; U0 stays in S.U until stage 2 overwrites it
     double u[kDim];
 #pragma unroll
-    for (int k = 0; k < kDim; ++k) u[k] = S.U[k * fp + f] + fpc::f2d(S.inc32[(size_t)k * fp + f] + dtf * src[k]);
+    for (int k = 0; k < kDim; ++k) u[k] = S.U[k * fp + f] + fpc::f2d((acc[k].hi + acc[k].lo) + dtf * src[k]);
     if (P.accretion_on) {  // accretion mass source in FP64
       const double dt_here = S.scal[(STAGE == 1) ? kScDtHalf : kScDt];
       u[0] += dt_here * acc0;
@@ -577,23 +559,24 @@ __global__ void __launch_bounds__(256, 5) ens_reconstruct_kernel(const EnsInstan
   recon_body(I.G, I.S, I.P, t.y + threadIdx.x, blockIdx.y);
 }
 
-template <int STAGE>
-__global__ void __launch_bounds__(kFaceTile * kMaxSlotLanes, 5) ens_flux_kernel(
-    const EnsInstance* __restrict__ inst, const int2* __restrict__ tiles) {
-  __shared__ FluxShared sh;
+// edge fluxes: one 32-edge tile per warp (tiles hold (instance, first edge))
+constexpr int kWarpTiles = kBlock / 32;
+__global__ void __launch_bounds__(kBlock) ens_edge_flux_kernel(const EnsInstance* __restrict__ inst,
+                                                               const int2* __restrict__ tiles, int n_tiles) {
   griddep_launch_dependents();
-  const int2 t = tiles[blockIdx.x];
+  const int tile = blockIdx.x * kWarpTiles + (threadIdx.x >> 5);
+  if (tile >= n_tiles) return;  // whole warps: stop bits fold per warp
+  const int2 t = tiles[tile];
   const EnsInstance& I = inst[t.x];
-  flux_body<STAGE>(I.G, I.S, I.P, t.y, sh);
+  edge_flux_body(I.G, I.S, I.P, t.y + (threadIdx.x & 31));
 }
 
-// update: one 32-face tile per warp, kUpdTiles tiles per block
-constexpr int kUpdTiles = kBlock / 32;
+// update: one 32-face tile per warp
 template <int STAGE>
 __global__ void __launch_bounds__(kBlock) ens_update_kernel(const EnsInstance* __restrict__ inst,
                                                             const int2* __restrict__ tiles, int n_tiles) {
   griddep_launch_dependents();
-  const int tile = blockIdx.x * kUpdTiles + (threadIdx.x >> 5);
+  const int tile = blockIdx.x * kWarpTiles + (threadIdx.x >> 5);
   if (tile >= n_tiles) return;  // whole warps: the candidates fold per warp
   const int2 t = tiles[tile];
   const EnsInstance& I = inst[t.x];
@@ -638,9 +621,8 @@ cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStre
 
 cudaError_t mixed_step(const DevGeomMixed& G, const DevState& S, const PhysParams& P, double dt0,
                        cudaStream_t st, cudaEvent_t* ev) {
-  const int ntile = (G.n_faces + mx::kFaceTile - 1) / mx::kFaceTile;
   const dim3 rgrid(mx::blocks_for(G.n_faces), G.max_slots);
-  const dim3 fblock(mx::kFaceTile, G.max_slots);
+  const dim3 egrid(mx::blocks_for(G.n_edges));
   const dim3 ugrid(mx::blocks_for(G.n_faces));
   cudaError_t e = cudaSuccess;
   auto chk = [&](cudaError_t r) {
@@ -651,12 +633,12 @@ cudaError_t mixed_step(const DevGeomMixed& G, const DevState& S, const PhysParam
   if (ev) cudaEventRecord(ev[1], st);
   chk(launch_pdl(mx::reconstruct_kernel, rgrid, dim3(mx::kBlock), st, G, S, P));
   if (ev) cudaEventRecord(ev[2], st);
-  chk(launch_pdl(mx::flux_kernel<1>, dim3(ntile), fblock, st, G, S, P));
+  chk(launch_pdl(mx::edge_flux_kernel, egrid, dim3(mx::kBlock), st, G, S, P));
   chk(launch_pdl(mx::update_kernel<1>, ugrid, dim3(mx::kBlock), st, G, S, P));
   if (ev) cudaEventRecord(ev[3], st);
   chk(launch_pdl(mx::reconstruct_kernel, rgrid, dim3(mx::kBlock), st, G, S, P));
   if (ev) cudaEventRecord(ev[4], st);
-  chk(launch_pdl(mx::flux_kernel<2>, dim3(ntile), fblock, st, G, S, P));
+  chk(launch_pdl(mx::edge_flux_kernel, egrid, dim3(mx::kBlock), st, G, S, P));
   chk(launch_pdl(mx::update_kernel<2>, ugrid, dim3(mx::kBlock), st, G, S, P));
   if (ev) cudaEventRecord(ev[5], st);
   return e != cudaSuccess ? e : cudaGetLastError();
@@ -670,21 +652,21 @@ cudaError_t ensemble_prepare(const EnsInstance* inst, int n_inst, const int2* ft
 }
 
 cudaError_t ensemble_step(const EnsInstance* inst, int n_inst, const int2* rtiles, int n_rtiles,
-                          int recon_width, const int2* ftiles, int n_ftiles, int max_slots, double dt0,
-                          cudaStream_t st) {
+                          int recon_width, const int2* ftiles, int n_ftiles, const int2* etiles, int n_etiles,
+                          int max_slots, double dt0, cudaStream_t st) {
   const dim3 rgrid(n_rtiles, max_slots);
-  const dim3 fblock(mx::kFaceTile, max_slots);
+  const dim3 egrid((n_etiles + mx::kWarpTiles - 1) / mx::kWarpTiles);
+  const dim3 ugrid((n_ftiles + mx::kWarpTiles - 1) / mx::kWarpTiles);
   cudaError_t e = cudaSuccess;
   auto chk = [&](cudaError_t r) {
     if (e == cudaSuccess) e = r;
   };
   chk(launch_pdl(mx::ens_finalize_kernel, dim3((n_inst + 127) / 128), dim3(128), st, inst, n_inst, dt0));
   chk(launch_pdl(mx::ens_reconstruct_kernel, rgrid, dim3(recon_width), st, inst, rtiles));
-  const dim3 ugrid((n_ftiles + mx::kUpdTiles - 1) / mx::kUpdTiles);
-  chk(launch_pdl(mx::ens_flux_kernel<1>, dim3(n_ftiles), fblock, st, inst, ftiles));
+  chk(launch_pdl(mx::ens_edge_flux_kernel, egrid, dim3(mx::kBlock), st, inst, etiles, n_etiles));
   chk(launch_pdl(mx::ens_update_kernel<1>, ugrid, dim3(mx::kBlock), st, inst, ftiles, n_ftiles));
   chk(launch_pdl(mx::ens_reconstruct_kernel, rgrid, dim3(recon_width), st, inst, rtiles));
-  chk(launch_pdl(mx::ens_flux_kernel<2>, dim3(n_ftiles), fblock, st, inst, ftiles));
+  chk(launch_pdl(mx::ens_edge_flux_kernel, egrid, dim3(mx::kBlock), st, inst, etiles, n_etiles));
   chk(launch_pdl(mx::ens_update_kernel<2>, ugrid, dim3(mx::kBlock), st, inst, ftiles, n_ftiles));
   return e != cudaSuccess ? e : cudaGetLastError();
 }
