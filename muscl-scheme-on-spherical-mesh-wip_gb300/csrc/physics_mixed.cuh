@@ -230,22 +230,22 @@ __device__ __forceinline__ float iso_limiter_field(float r, float eta, float sb_
 }
 
 // h(r) switch and the blended limiter (physics/adiabatic.hpp:685-828).
-// On (0, 1) the switch is 1 - tanh(y) = 2 / (1 + e^{2y}) (no cancellation);
-// for r >= 1 it is tanh(y)^6 = ((e^{2y} - 1) / (e^{2y} + 1))^6.
+// On (0, 1) the switch is 1 - tanh(y) = 2 / (1 + e^{2y}) (no cancellation)
+// with y = 4 r^2 (1 - r)^0.1; for r >= 1 it is tanh(z)^6 with
+// tanh(z) = (e^{2z} - 1) / (e^{2z} + 1), 2z = 20 (r - 1)^3 clamped at 80;
+// 0 elsewhere (and for NaN).  Written without branches so that a warp whose
+// lanes fall on both sides evaluates one exponential and one reciprocal per
+// lane, shared by the two forms, instead of both branches in turn.
 __device__ __forceinline__ float limiter_switch(float r) {
-  float o = 0.f;
-  if (r < 1.f && r > 0.f) {
-    const float y = 4.f * (r * r) * __expf(0.1f * __logf(1.f - r));
-    o = __fdividef(2.f, 1.f + __expf(2.f * y));
-  }
-  if (r >= 1.f) {
-    const float x = r - 1.f;
-    const float e = __expf(fminf(20.f * (x * x * x), 80.f));
-    const float t = __fdividef(e - 1.f, e + 1.f);
-    const float t2 = t * t;
-    o = t2 * t2 * t2;
-  }
-  return o;
+  const bool lo = r < 1.f && r > 0.f;
+  const bool hi = r >= 1.f;
+  const float y = 4.f * (r * r) * __expf(0.1f * __logf(lo ? 1.f - r : 1.f));
+  const float x = r - 1.f;
+  const float e = __expf(lo ? 2.f * y : fminf(20.f * (x * x * x), 80.f));
+  const float q = __fdividef(1.f, 1.f + e);
+  const float t = (e - 1.f) * q;
+  const float t2 = t * t;
+  return lo ? 2.f * q : (hi ? t2 * t2 * t2 : 0.f);
 }
 
 __device__ __forceinline__ float limiter_field(float r, float nu_plus, float eta_p, float sb_scale) {

@@ -397,6 +397,9 @@ __global__ void __launch_bounds__(kBlock, 10) reconstruct_kernel(DevGeomMixed G,
 }
 
 constexpr int kFaceTile = 32;  // faces (or edges) per tile of the batched launches
+// slot bound of the mixed path: solvers and ensembles reject meshes with
+// faces of more than 8 edges at creation
+constexpr int kMaxFaceSlots = 8;
 
 // find_flux_var (MUSCL_base.hpp:345-359) per interior edge: one thread per
 // edge evaluates the Riemann flux once, in the orientation of the edge's
@@ -458,11 +461,19 @@ __device__ __forceinline__ void update_body(const DevGeomMixed& G, const DevStat
   double acc0 = 0.0;
   f64::D3 r{0.0, 0.0, 0.0};
   int n = 0;
+  // the slots' edges and flux coefficients: geometry, loaded before the wait
+  int se[kMaxFaceSlots];
+  float co[kMaxFaceSlots];
   if (live) {
     fcn32 = plane3f(G.fcn32, fp, f);
     acc0 = G.acc_src[f];
     r = plane3d(G.fcn, fp, f);
     n = G.nslots[f];
+  }
+#pragma unroll
+  for (int j = 0; j < kMaxFaceSlots; ++j) {
+    se[j] = (j < n) ? G.slot_edge[j * fp + f] : 0;
+    co[j] = (j < n) ? G.coef[j * fp + f] : 0.f;
   }
   griddep_wait();
   double vmax = 0.0, dmin = kNoExtraSq;
@@ -472,16 +483,19 @@ __device__ __forceinline__ void update_body(const DevGeomMixed& G, const DevStat
     Acc acc[kDim];
 #pragma unroll
     for (int k = 0; k < kDim; ++k) acc[k] = Acc{0.f, 0.f};
-    for (int j = 0; j < n; ++j) {
-      const int q = j * fp + f;
-      const int se = G.slot_edge[q];
-      const float cf = dtf * G.coef[q];
-      // -cf F with F = Fe on the owner side and -Fe on the reverse side
-      const float c = (se < 0) ? cf : -cf;
-      float fe[kDim];
-      ld5(S.fe32, G.epad, se & 0x7fffffff, fe);
+    // unrolled over the slot bound so that every slot's gather is in flight
+    // before the first is summed; the sum stays in slot order
 #pragma unroll
-      for (int k = 0; k < kDim; ++k) acc[k].add(c * fe[k]);
+    for (int j = 0; j < kMaxFaceSlots; ++j) {
+      if (j < n) {
+        const float cf = dtf * co[j];
+        // -cf F with F = Fe on the owner side and -Fe on the reverse side
+        const float c = (se[j] < 0) ? cf : -cf;
+        float fe[kDim];
+        ld5(S.fe32, G.epad, se[j] & 0x7fffffff, fe);
+#pragma unroll
+        for (int k = 0; k < kDim; ++k) acc[k].add(c * fe[k]);
+      }
     }
     float w[kDim], src[kDim];
     ld5(S.W32, fp, f, w);
