@@ -170,14 +170,11 @@ void Solver::build_device_geometry(const RefGeometry& g) {
     GM.fcn32 = upload(mp.fcn32);
     GM.area = upload(sp.area);
     GM.acc_src = upload(acc);
-    GM.sten = upload(sp.sten);
-    GM.beta = upload(mp.beta);
-    GM.inv_h = upload(mp.inv_h);
-    GM.bm = upload(mp.bm);
-    GM.eta = upload(mp.eta);
-    GM.arc_a = upload(mp.arc);
-    GM.ec = upload(mp.ec);
-    GM.en = upload(mp.en);
+    GM.rc_sten = upload(mp.rc_sten);
+    GM.rc_beta = upload(mp.rc_beta);
+    GM.rc_h = upload(mp.rc_h);
+    GM.rc_ec = upload(mp.rc_ec);
+    GM.rc_en = upload(mp.rc_en);
     GM.coef = upload(mp.coef);
     GM.slot_edge = upload(mp.slot_edge);
     GM.n_edges = mp.n_edges;
@@ -188,10 +185,10 @@ void Solver::build_device_geometry(const RefGeometry& g) {
     GM.e_en = upload(mp.e_en);
     GM.e_nxr = upload(mp.e_nxr);
     geometry_bytes = sp.nslots.size() + 8 * (sp.fcn.size() + sp.area.size() + acc.size()) +
-                     4 * (sp.sten.size() + mp.fcn32.size() + mp.beta.size() + mp.inv_h.size() +
-                          mp.bm.size() + mp.eta.size() + mp.arc.size() + mp.ec.size() + mp.en.size() +
-                          mp.coef.size() + mp.slot_edge.size() + mp.e_own.size() + mp.e_nbr.size() +
-                          mp.e_ec.size() + mp.e_en.size() + mp.e_nxr.size());
+                     4 * (mp.fcn32.size() + mp.rc_sten.size() + mp.rc_beta.size() + mp.rc_h.size() +
+                          mp.rc_ec.size() + mp.rc_en.size() + mp.coef.size() + mp.slot_edge.size() +
+                          mp.e_own.size() + mp.e_nbr.size() + mp.e_ec.size() + mp.e_en.size() +
+                          mp.e_nxr.size());
   } else {
     G.n_faces = n_faces;
     G.fpad = fpad;

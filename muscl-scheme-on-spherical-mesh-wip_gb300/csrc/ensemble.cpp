@@ -305,14 +305,11 @@ int splash_ensemble_create(const splash_member* members, int n, int device, int 
         L.G.fcn = e->upload(L.sp.fcn);
         L.G.fcn32 = e->upload(mp.fcn32);
         L.G.area = e->upload(L.sp.area);
-        L.G.sten = e->upload(L.sp.sten);
-        L.G.beta = e->upload(mp.beta);
-        L.G.inv_h = e->upload(mp.inv_h);
-        L.G.bm = e->upload(mp.bm);
-        L.G.eta = e->upload(mp.eta);
-        L.G.arc_a = e->upload(mp.arc);
-        L.G.ec = e->upload(mp.ec);
-        L.G.en = e->upload(mp.en);
+        L.G.rc_sten = e->upload(mp.rc_sten);
+        L.G.rc_beta = e->upload(mp.rc_beta);
+        L.G.rc_h = e->upload(mp.rc_h);
+        L.G.rc_ec = e->upload(mp.rc_ec);
+        L.G.rc_en = e->upload(mp.rc_en);
         L.G.coef = e->upload(mp.coef);
         L.G.slot_edge = e->upload(mp.slot_edge);
         L.G.n_edges = mp.n_edges;

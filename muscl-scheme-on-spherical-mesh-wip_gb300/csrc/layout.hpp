@@ -102,14 +102,13 @@ struct DevGeomMixed {
   const float* fcn32;     // 3 planes, FP32 copy (source term)
   const double* area;
   const double* acc_src;  // accretion mass source, FP64
-  const int* sten;        // 4 planes
-  const float* beta;      // 4 planes
-  const float* inv_h;     // 2 planes: 1/H_plus, 1/H_minus
-  const float* bm;
-  const float* eta;       // 2 planes
-  const float* arc_a;
-  const float* ec;        // 3 planes, unit edge centre
-  const float* en;        // 3 planes
+  // reconstruction constants, four interleaved values per slot (read as
+  // one int4 / float4 each):
+  const int* rc_sten;     // stencil faces: plus pair, minus pair
+  const float* rc_beta;   // beta_plus 0, 1, beta_minus 0, 1
+  const float* rc_h;      // 1/H_plus, 1/H_minus, BM_dist, arc/area
+  const float* rc_ec;     // unit edge centre, H_plus/BM_dist
+  const float* rc_en;     // edge normal, H_minus/BM_dist
   const float* coef;      // round_diff * chord / area
   const int* slot_edge;   // edge of the slot, bit 31 set on the edge's reverse side
   // interior edges, each once, in the orientation of the owner slot

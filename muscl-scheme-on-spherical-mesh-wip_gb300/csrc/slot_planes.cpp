@@ -208,6 +208,27 @@ MixedPlanes make_mixed_planes(const SlotPlanes& sp) {
       const size_t q = (size_t)j * sp.fpad + i;
       mp.coef[q] = (float)(sp.round_diff * sp.chord[q] / sp.area[i]);
     }
+  mp.rc_sten.assign(4 * PS, 0);
+  mp.rc_beta.assign(4 * PS, 0.f);
+  mp.rc_h.assign(4 * PS, 0.f);
+  mp.rc_ec.assign(4 * PS, 0.f);
+  mp.rc_en.assign(4 * PS, 0.f);
+  for (size_t q = 0; q < PS; ++q) {
+    for (int c = 0; c < 4; ++c) {
+      mp.rc_sten[4 * q + c] = sp.sten[c * PS + q];
+      mp.rc_beta[4 * q + c] = mp.beta[c * PS + q];
+    }
+    mp.rc_h[4 * q + 0] = mp.inv_h[q];
+    mp.rc_h[4 * q + 1] = mp.inv_h[PS + q];
+    mp.rc_h[4 * q + 2] = mp.bm[q];
+    mp.rc_h[4 * q + 3] = mp.arc[q];
+    for (int c = 0; c < 3; ++c) {
+      mp.rc_ec[4 * q + c] = mp.ec[c * PS + q];
+      mp.rc_en[4 * q + c] = mp.en[c * PS + q];
+    }
+    mp.rc_ec[4 * q + 3] = mp.eta[q];
+    mp.rc_en[4 * q + 3] = mp.eta[PS + q];
+  }
   // edges in ascending owner order (plane-major, faces ascending within a
   // plane): the reverse side of every edge is met either as an owner's
   // neighbour before it, or as an owner itself

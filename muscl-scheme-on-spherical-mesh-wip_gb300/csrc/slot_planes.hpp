@@ -55,6 +55,12 @@ std::vector<double> accretion_source_fcn(const std::vector<double>& fcn, int n_f
 // (every Riemann solver here satisfies F(uR, uL, -n) = -F(uL, uR, n)).
 struct MixedPlanes {
   std::vector<float> fcn32, beta, inv_h, bm, eta, arc, ec, en, coef;
+  // the reconstruction's constants of slot s as four interleaved values
+  // (one 16-byte load each): stencil faces (a, b, c, d); (beta_plus 0, 1,
+  // beta_minus 0, 1); (1/H_plus, 1/H_minus, BM_dist, arc/area);
+  // (unit edge centre, H_plus/BM_dist); (edge normal, H_minus/BM_dist)
+  std::vector<int> rc_sten;
+  std::vector<float> rc_beta, rc_h, rc_ec, rc_en;
   int n_edges = 0, epad = 0;           // epad: n_edges rounded up to 32
   std::vector<int> e_own, e_nbr;       // [epad] slot-plane indices of the two sides
   std::vector<float> e_ec, e_en, e_nxr;  // 3 planes of epad: the owner slot's geometry

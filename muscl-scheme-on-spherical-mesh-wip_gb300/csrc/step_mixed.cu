@@ -332,12 +332,18 @@ __device__ __forceinline__ void recon_body(const DevGeomMixed& G, const DevState
   const int PS = G.max_slots * fp;
   const float* W = S.W32;
   const int s = j * fp + f;
-  const int ia = G.sten[s], ib = G.sten[PS + s], ic = G.sten[2 * PS + s], id = G.sten[3 * PS + s];
-  const float bp0 = G.beta[s], bp1 = G.beta[PS + s], bm0 = G.beta[2 * PS + s], bm1 = G.beta[3 * PS + s];
-  const float ihp = G.inv_h[s], ihm = G.inv_h[PS + s], bmd = G.bm[s];
-  const F3 ec = plane3f(G.ec, PS, s);
-  const F3 en = plane3f(G.en, PS, s);
-  const float arc_a = G.arc_a[s], eta_p = G.eta[s], eta_m = G.eta[PS + s];
+  // the slot's constants: five 16-byte loads
+  const int4 st = reinterpret_cast<const int4*>(G.rc_sten)[s];
+  const float4 bt = reinterpret_cast<const float4*>(G.rc_beta)[s];
+  const float4 hh = reinterpret_cast<const float4*>(G.rc_h)[s];
+  const float4 ce = reinterpret_cast<const float4*>(G.rc_ec)[s];
+  const float4 ne = reinterpret_cast<const float4*>(G.rc_en)[s];
+  const int ia = st.x, ib = st.y, ic = st.z, id = st.w;
+  const float bp0 = bt.x, bp1 = bt.y, bm0 = bt.z, bm1 = bt.w;
+  const float ihp = hh.x, ihm = hh.y, bmd = hh.z, arc_a = hh.w;
+  const F3 ec = f3(ce.x, ce.y, ce.z);
+  const F3 en = f3(ne.x, ne.y, ne.z);
+  const float eta_p = ce.w, eta_m = ne.w;
   griddep_wait();
   const float dt = reinterpret_cast<const float2*>(S.scal + kScDtF)->x;
   // the face and its four stencil faces: one 16-byte gather each for
