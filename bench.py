@@ -183,21 +183,28 @@ def cpu_baseline(geom, U0, gam, budget_s=15.0):
 
 
 def algorithmic_bytes_mixed(geom, kernel: str) -> float:
-    """Compulsory bytes per launch of one kernel of the mixed path.
+    """Compulsory bytes per launch of one kernel of the mixed path (F faces,
+    S slots, E = S / 2 interior edges).
 
-    reconstruct: read W32 (5 x 4 B per face); per slot 4 int32 stencil ids,
-      4 betas, 1/H+, 1/H-, BM, edge centre (3), normal (3), Courant factor,
-      2 eta (all FP32) ; write U+ (5 x 4 B per slot).
-    flux_update: read U+ (5 x 4 B per slot, once algorithmically); per slot
-      edge centre, normal, n x R (9 x 4 B), the FP64 flux coefficient and the
-      reverse index; per face W32, U0 (FP64), unit centre (FP32 + FP64), area,
-      accretion source ; write U (FP64) and W32.
+    reconstruct: read W32 (5 x 4 B per face, each face once); per slot the
+      packed constants (int4 stencil, float4 weights, float4 1/H+, 1/H-, BM,
+      arc/area, float4 edge centre + eta+, float4 normal + eta-: 80 B);
+      write U+ (5 x 4 B per slot).
+    edge_flux: per edge the two slot ids (8 B), edge centre, normal, n x R
+      (9 x 4 B), the two edge states (2 x 20 B), write the flux (20 B).
+    update (mean of the two stages): per face W32 (20 B), U0 (40 B), unit
+      centre FP64 + FP32 (24 + 12 B), accretion source (8 B), slot count
+      (1 B); per slot edge id and flux coefficient (8 B); every edge flux once
+      (20 B per edge); write W32 (20 B) and, in stage 2, U (40 B).
     """
     F = geom.n_faces
     S = geom.n_slots
+    E = S // 2
     if kernel == "reconstruct":
-        return F * 20 + S * (16 + 4 * (4 + 2 + 1 + 3 + 3 + 1 + 2)) + S * 20
-    return S * 20 + S * (9 * 4 + 8 + 4) + F * (20 + 40 + 12 + 24 + 8 + 8) + F * (40 + 20)
+        return F * 20 + S * 80 + S * 20
+    if kernel == "edge_flux":
+        return E * (8 + 36 + 40 + 20)
+    return F * (20 + 40 + 24 + 12 + 8 + 1) + S * 8 + E * 20 + F * (20 + 40 / 2)
 
 
 def algorithmic_bytes(geom, kernel: str) -> float:
@@ -427,12 +434,15 @@ def run_ours(args):
            "reference": "GPU FP64 path (1e-10 of the reference on the golden states)"}
     # per-kernel device times (un-captured launches, CUDA events on the solver stream)
     reps = max(3, min(20, args.steps))
-    ms = mixed.kernel_times(reps, DT0)
+    lt = mixed.launch_times(reps, DT0)
     ms64 = fp64.kernel_times(reps, DT0)
-    kern = {"dt_reduce": ms[0], "reconstruct": (ms[1] + ms[3]) / 2, "flux_update": (ms[2] + ms[4]) / 2}
+    # mean ms per launch of each kernel, and each kernel's ms per step
+    kern = {"finalize": lt[0], "reconstruct": (lt[1] + lt[4]) / 2, "edge_flux": (lt[2] + lt[5]) / 2,
+            "update": (lt[3] + lt[6]) / 2, "update_stage1": lt[3], "update_stage2": lt[6]}
+    per_step = {"reconstruct": lt[1] + lt[4], "edge_flux": lt[2] + lt[5], "update": lt[3] + lt[6]}
     kern64 = {"dt_reduce": ms64[0], "reconstruct": (ms64[1] + ms64[3]) / 2,
               "flux_update": (ms64[2] + ms64[4]) / 2}
-    dom = max(("reconstruct", "flux_update"), key=lambda k: kern[k])
+    dom = max(per_step, key=per_step.get)
     hbm, src = peaks()
     ach = algorithmic_bytes_mixed(geom, dom) / (kern[dom] * 1e-3) / 1e9
     geo_b, st_b = mixed.memory()
@@ -457,7 +467,7 @@ def run_ours(args):
                      "unit": "GB/s", "frac": ach / hbm, "traffic": measured_traffic(dom),
                      "algorithmic_bytes": algorithmic_bytes_mixed(geom, dom),
                      "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)",
-                     "kernel_ms": kern},
+                     "kernel_ms": kern, "kernel_ms_per_step": per_step},
         "clocks": clk,
     }
     mixed.close()

@@ -148,12 +148,22 @@ SPLASH_API int splash_synchronize(splash_solver* s);
 /* The cudaStream_t the solver launches on (as void*), so a caller can
  * order its own work or record CUDA events against the step. */
 SPLASH_API int splash_stream(splash_solver* s, void** stream);
-/* Runs `reps` un-captured steps with CUDA events around every launch and
- * returns the mean device time per launch in milliseconds:
- * ms[0] dt reduction, ms[1] reconstruct (stage 1), ms[2] flux+update
- * (stage 1), ms[3] reconstruct (stage 2), ms[4] flux+update (stage 2).
+/* Runs `reps` un-captured steps with CUDA events between the step's phases
+ * and returns the mean device time per phase in milliseconds:
+ * ms[0] dt reduction (finalize), ms[1] reconstruct (stage 1), ms[2] flux and
+ * update (stage 1; on the mixed path the edge-flux and update launches),
+ * ms[3] reconstruct (stage 2), ms[4] flux and update (stage 2).
  * The steps advance the state like do_step(dt0). */
 SPLASH_API int splash_kernel_times(splash_solver* s, int reps, double dt0, double ms[5]);
+/* Mean device ms of every launch of one step over `reps` un-captured steps,
+ * with a CUDA event between consecutive launches (which serialises the
+ * step's programmatic overlap, so the sum exceeds the captured step's time).
+ * Mixed path, 7 launches: finalize, reconstruct, edge flux, update (stage 1),
+ * reconstruct, edge flux, update (stage 2); FP64 path, 5 launches: dt
+ * reduction, reconstruct, flux+update, reconstruct, flux+update.  Writes
+ * min(cap, *count) values; *count = launches per step.  The steps advance
+ * the state like do_step(dt0). */
+SPLASH_API int splash_launch_times(splash_solver* s, int reps, double dt0, double* ms, int cap, int* count);
 /* Device bytes held by the solver: out[0] geometry, out[1] state + scratch. */
 SPLASH_API int splash_memory(splash_solver* s, int64_t out[2]);
 

@@ -269,8 +269,8 @@ cudaError_t Solver::launch_prepare() {
   return precision == SPLASH_PREC_MIXED ? mixed_prepare(GM, S, P, stream) : fp64_prepare(G, S, P, stream);
 }
 
-cudaError_t Solver::launch_step(cudaEvent_t* ev, double dt0) {
-  if (precision == SPLASH_PREC_MIXED) return mixed_step(GM, S, P, dt0, stream, ev);
+cudaError_t Solver::launch_step(cudaEvent_t* ev, double dt0, bool per_launch) {
+  if (precision == SPLASH_PREC_MIXED) return mixed_step(GM, S, P, dt0, stream, ev, per_launch);
   cudaError_t e = fp64_set_dt0(S, dt0, stream);
   if (e != cudaSuccess) return e;
   return fp64_step(G, S, P, stream, ev);
@@ -559,6 +559,35 @@ int splash_kernel_times(splash_solver* h, int reps, double dt0, double ms[5]) {
   for (auto& e : ev) cudaEventDestroy(e);
   if (rc) return rc;
   for (int k = 0; k < 5; ++k) ms[k] = acc[k] / reps;
+  return SPLASH_OK;
+}
+
+int splash_launch_times(splash_solver* h, int reps, double dt0, double* ms, int cap, int* count) {
+  GET_SOLVER(h);
+  if (reps <= 0 || !ms || !count || cap < 0) return fail(SPLASH_E_INVALID, "reps must be > 0, ms and count non-NULL");
+  const int nl = s->launches_per_step();
+  cudaEvent_t ev[8];
+  for (int k = 0; k <= nl; ++k) SPLASH_CUDA(cudaEventCreate(&ev[k]));
+  double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+  int rc = SPLASH_OK;
+  for (int r = 0; r < reps && rc == SPLASH_OK; ++r) {
+    cudaError_t e = s->launch_step(ev, dt0, true);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ev[nl]);
+    if (e != cudaSuccess) {
+      rc = fail(SPLASH_E_CUDA, "launch timing: %s", cudaGetErrorString(e));
+      break;
+    }
+    for (int k = 0; k < nl; ++k) {
+      float t = 0;
+      cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+      acc[k] += t;
+    }
+    ++s->steps;
+  }
+  for (int k = 0; k <= nl; ++k) cudaEventDestroy(ev[k]);
+  if (rc) return rc;
+  for (int k = 0; k < nl && k < cap; ++k) ms[k] = acc[k] / reps;
+  *count = nl;
   return SPLASH_OK;
 }
 

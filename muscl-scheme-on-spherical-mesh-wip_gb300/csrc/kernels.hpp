@@ -34,8 +34,12 @@ cudaError_t mixed_prepare(const DevGeomMixed& G, const DevState& S, const PhysPa
 // One do_step: the dt finalize (1 thread, argument dt0) then the four
 // stage launches.  Capturable; the finalize node's dt0 can be updated in an
 // instantiated graph (mixed_finalize_kernel_ptr identifies the node).
+// ev (optional): events recorded on st at the step's boundaries; six
+// (before the step, after finalize, after reconstruction 1, after stage 1,
+// after reconstruction 2, after stage 2), or with per_launch eight, one
+// before the step and one after each of its seven launches.
 cudaError_t mixed_step(const DevGeomMixed& G, const DevState& S, const PhysParams& P, double dt0,
-                       cudaStream_t st, cudaEvent_t* ev = nullptr);
+                       cudaStream_t st, cudaEvent_t* ev = nullptr, bool per_launch = false);
 const void* mixed_finalize_kernel_ptr();
 int mixed_partial_blocks(int n_faces);
 

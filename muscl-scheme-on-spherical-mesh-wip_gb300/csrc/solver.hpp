@@ -82,7 +82,10 @@ struct Solver {
   int read_scalars(double* out);
   int capture_graph();
   int step(double dt0);
-  cudaError_t launch_step(cudaEvent_t* ev, double dt0);  // one un-captured step
+  // one un-captured step; ev as for mixed_step (the FP64 step has five
+  // launches, so its two layouts coincide)
+  cudaError_t launch_step(cudaEvent_t* ev, double dt0, bool per_launch = false);
+  int launches_per_step() const { return precision == SPLASH_PREC_MIXED ? 7 : 5; }
   cudaError_t launch_prepare();
   static int check_cuda(cudaError_t e, const char* what);
 };

@@ -640,7 +640,7 @@ cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStre
 }  // namespace
 
 cudaError_t mixed_step(const DevGeomMixed& G, const DevState& S, const PhysParams& P, double dt0,
-                       cudaStream_t st, cudaEvent_t* ev) {
+                       cudaStream_t st, cudaEvent_t* ev, bool per_launch) {
   const dim3 rgrid(mx::blocks_for(G.n_faces), G.max_slots);
   const dim3 egrid(mx::blocks_for(G.n_edges));
   const dim3 ugrid(mx::blocks_for(G.n_faces));
@@ -654,13 +654,15 @@ cudaError_t mixed_step(const DevGeomMixed& G, const DevState& S, const PhysParam
   chk(launch_pdl(mx::reconstruct_kernel, rgrid, dim3(mx::kBlock), st, G, S, P));
   if (ev) cudaEventRecord(ev[2], st);
   chk(launch_pdl(mx::edge_flux_kernel, egrid, dim3(mx::kBlock), st, G, S, P));
+  if (ev && per_launch) cudaEventRecord(ev[3], st);
   chk(launch_pdl(mx::update_kernel<1>, ugrid, dim3(mx::kBlock), st, G, S, P));
-  if (ev) cudaEventRecord(ev[3], st);
+  if (ev) cudaEventRecord(ev[per_launch ? 4 : 3], st);
   chk(launch_pdl(mx::reconstruct_kernel, rgrid, dim3(mx::kBlock), st, G, S, P));
-  if (ev) cudaEventRecord(ev[4], st);
+  if (ev) cudaEventRecord(ev[per_launch ? 5 : 4], st);
   chk(launch_pdl(mx::edge_flux_kernel, egrid, dim3(mx::kBlock), st, G, S, P));
+  if (ev && per_launch) cudaEventRecord(ev[6], st);
   chk(launch_pdl(mx::update_kernel<2>, ugrid, dim3(mx::kBlock), st, G, S, P));
-  if (ev) cudaEventRecord(ev[5], st);
+  if (ev) cudaEventRecord(ev[per_launch ? 7 : 5], st);
   return e != cudaSuccess ? e : cudaGetLastError();
 }
 

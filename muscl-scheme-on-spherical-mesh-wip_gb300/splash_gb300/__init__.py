@@ -51,7 +51,7 @@ EXPORTED = (
     "splash_write_t_p", "splash_write_t_curl", "splash_write_t_omega_z",
     "splash_write_t_L", "splash_get_light_curves", "splash_write_final_state",
     "splash_geometry_build", "splash_geometry_free", "splash_geometry_info",
-    "splash_geometry_get", "splash_stream", "splash_kernel_times", "splash_memory",
+    "splash_geometry_get", "splash_stream", "splash_kernel_times", "splash_launch_times", "splash_memory",
     "splash_ensemble_create", "splash_ensemble_destroy", "splash_ensemble_do_steps",
     "splash_ensemble_synchronize", "splash_ensemble_stream", "splash_ensemble_get_state",
     "splash_ensemble_member_info", "splash_ensemble_schedule", "splash_ensemble_size",
@@ -130,6 +130,7 @@ def library(path: str | os.PathLike | None = None) -> C.CDLL:
         "splash_geometry_get": [vp, C.c_char_p, vp, C.c_size_t, C.POINTER(C.c_size_t)],
         "splash_stream": [vp, C.POINTER(vp)],
         "splash_kernel_times": [vp, C.c_int, C.c_double, dp],
+        "splash_launch_times": [vp, C.c_int, C.c_double, dp, C.c_int, ip],
         "splash_memory": [vp, C.POINTER(C.c_int64)],
         "splash_ensemble_create": [C.POINTER(Member), C.c_int, C.c_int, C.c_int, C.POINTER(vp)],
         "splash_ensemble_destroy": [vp], "splash_ensemble_do_steps": [vp, C.c_int, C.c_double],
@@ -364,6 +365,15 @@ class Solver:
         out = np.zeros(5)
         _check(self._lib.splash_kernel_times(self.handle, reps, dt0, _dptr(out)))
         return out
+
+    def launch_times(self, reps: int, dt0: float) -> np.ndarray:
+        """Mean device ms of every launch of one step (mixed: finalize,
+        reconstruct, edge flux, update, reconstruct, edge flux, update; FP64:
+        dt, recon1, flux1, recon2, flux2), with events between launches."""
+        out = np.zeros(8)
+        n = C.c_int(0)
+        _check(self._lib.splash_launch_times(self.handle, reps, dt0, _dptr(out), 8, C.byref(n)))
+        return out[: n.value].copy()
 
     def memory(self) -> tuple[int, int]:
         out = (C.c_int64 * 2)()
