@@ -186,12 +186,12 @@ def algorithmic_bytes_mixed(geom, kernel: str) -> float:
     """Compulsory bytes per launch of one kernel of the mixed path (F faces,
     S slots, E = S / 2 interior edges).
 
-    reconstruct: read W32 (5 x 4 B per face, each face once); per slot the
-      packed constants (int4 stencil, float4 weights, float4 1/H+, 1/H-, BM,
-      arc/area, float4 edge centre + eta+, float4 normal + eta-: 80 B);
-      write U+ (5 x 4 B per slot).
-    edge_flux: per edge the two slot ids (8 B), edge centre, normal, n x R
-      (9 x 4 B), the two edge states (2 x 20 B), write the flux (20 B).
+    edge (reconstruction + Riemann flux, one thread per edge): the edge
+      record (face ids, edge centre, normal, n x R, both slots' eta: 64 B)
+      and per side the stencil, weights and distances (2 x 48 B); every face
+      state W32 read once (20 B per face); write the edge flux (20 B per
+      edge) and, in stage 2, both edge states (2 x 20 B per edge; mean of the
+      two stages).
     update (mean of the two stages): per face W32 (20 B), U0 (40 B), unit
       centre FP64 + FP32 (24 + 12 B), accretion source (8 B), slot count
       (1 B); per slot edge id and flux coefficient (8 B); every edge flux once
@@ -200,10 +200,8 @@ def algorithmic_bytes_mixed(geom, kernel: str) -> float:
     F = geom.n_faces
     S = geom.n_slots
     E = S // 2
-    if kernel == "reconstruct":
-        return F * 20 + S * 80 + S * 20
-    if kernel == "edge_flux":
-        return E * (8 + 36 + 40 + 20)
+    if kernel == "edge":
+        return E * (64 + 96 + 20 + 40 / 2) + F * 20
     return F * (20 + 40 + 24 + 12 + 8 + 1) + S * 8 + E * 20 + F * (20 + 40 / 2)
 
 
@@ -437,9 +435,10 @@ def run_ours(args):
     lt = mixed.launch_times(reps, DT0)
     ms64 = fp64.kernel_times(reps, DT0)
     # mean ms per launch of each kernel, and each kernel's ms per step
-    kern = {"finalize": lt[0], "reconstruct": (lt[1] + lt[4]) / 2, "edge_flux": (lt[2] + lt[5]) / 2,
-            "update": (lt[3] + lt[6]) / 2, "update_stage1": lt[3], "update_stage2": lt[6]}
-    per_step = {"reconstruct": lt[1] + lt[4], "edge_flux": lt[2] + lt[5], "update": lt[3] + lt[6]}
+    # (launches: finalize, edge 1, update 1, edge 2, update 2)
+    kern = {"finalize": lt[0], "edge": (lt[1] + lt[3]) / 2, "update": (lt[2] + lt[4]) / 2,
+            "edge_stage1": lt[1], "edge_stage2": lt[3], "update_stage1": lt[2], "update_stage2": lt[4]}
+    per_step = {"edge": lt[1] + lt[3], "update": lt[2] + lt[4]}
     kern64 = {"dt_reduce": ms64[0], "reconstruct": (ms64[1] + ms64[3]) / 2,
               "flux_update": (ms64[2] + ms64[4]) / 2}
     dom = max(per_step, key=per_step.get)
@@ -457,7 +456,7 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
         "config": {**workload_config(F, "mixed FP32/FP64"), "parallelism": f"replicas{world}",
                    "working_set_mb": round((geo_b + st_b) / 2**20, 1)},
-        "gpu_launches": 7 * args.steps,
+        "gpu_launches": 5 * args.steps,
         "e2e": {"value": F * e2e_steps / e2e_secs, "unit": METRIC, "h2d_bytes_per_step": bytes_io,
                 "d2h_bytes_per_step": bytes_io},
         "fp64": {"value": value64, "ms_per_step": secs64 / args.steps * 1e3, "kernel_ms": kern64},

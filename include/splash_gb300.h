@@ -265,8 +265,10 @@ SPLASH_API int splash_ensemble_stream(splash_ensemble* e, void** stream);
 SPLASH_API int splash_ensemble_get_state(splash_ensemble* e, int member, double* U);
 /* out = {t, dt of the last step, max_vel, extra_dt}; err = stop bits */
 SPLASH_API int splash_ensemble_member_info(splash_ensemble* e, int member, double out[4], uint32_t* err);
-/* The chosen schedule and the autotuner's per-candidate ms per step
- * (index order*3 + {64,128,256}-wide tiles). */
+/* The chosen schedule: tile order (0 member order, 1 largest first, 2
+ * round-robin) and the threads per block of the reconstruction + edge-flux
+ * launch; and the autotuner's per-candidate ms per step (index
+ * order*3 + {64,128,256}-thread blocks). */
 SPLASH_API int splash_ensemble_schedule(splash_ensemble* e, int* order, int* recon_width, double trial_ms[9]);
 SPLASH_API int splash_ensemble_size(splash_ensemble* e, int* n_members, int64_t* total_faces);
 

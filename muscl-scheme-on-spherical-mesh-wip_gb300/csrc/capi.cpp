@@ -170,25 +170,22 @@ void Solver::build_device_geometry(const RefGeometry& g) {
     GM.fcn32 = upload(mp.fcn32);
     GM.area = upload(sp.area);
     GM.acc_src = upload(acc);
-    GM.rc_sten = upload(mp.rc_sten);
-    GM.rc_beta = upload(mp.rc_beta);
-    GM.rc_h = upload(mp.rc_h);
-    GM.rc_ec = upload(mp.rc_ec);
-    GM.rc_en = upload(mp.rc_en);
     GM.coef = upload(mp.coef);
     GM.slot_edge = upload(mp.slot_edge);
+    h_slot_edge = mp.slot_edge;
     GM.n_edges = mp.n_edges;
     GM.epad = mp.epad;
-    GM.e_own = upload(mp.e_own);
-    GM.e_nbr = upload(mp.e_nbr);
+    GM.e_ids = upload(mp.e_ids);
     GM.e_ec = upload(mp.e_ec);
     GM.e_en = upload(mp.e_en);
-    GM.e_nxr = upload(mp.e_nxr);
+    GM.e_eta = upload(mp.e_eta);
+    GM.e_sten = upload(mp.e_sten);
+    GM.e_beta = upload(mp.e_beta);
+    GM.e_h = upload(mp.e_h);
     geometry_bytes = sp.nslots.size() + 8 * (sp.fcn.size() + sp.area.size() + acc.size()) +
-                     4 * (mp.fcn32.size() + mp.rc_sten.size() + mp.rc_beta.size() + mp.rc_h.size() +
-                          mp.rc_ec.size() + mp.rc_en.size() + mp.coef.size() + mp.slot_edge.size() +
-                          mp.e_own.size() + mp.e_nbr.size() + mp.e_ec.size() + mp.e_en.size() +
-                          mp.e_nxr.size());
+                     4 * (mp.fcn32.size() + mp.coef.size() + mp.slot_edge.size() + mp.e_ids.size() +
+                          mp.e_ec.size() + mp.e_en.size() + mp.e_eta.size() + mp.e_sten.size() +
+                          mp.e_beta.size() + mp.e_h.size());
   } else {
     G.n_faces = n_faces;
     G.fpad = fpad;
@@ -453,11 +450,11 @@ int splash_create(const splash_mesh_desc* mesh, const double* U_in, int dim, dou
     S.W1 = s->dalloc<double>(splash::kDim * fp);
     if (precision == SPLASH_PREC_MIXED) {
       S.W32 = s->dalloc<float>(splash::kDim * fp);
-      S.uplus32 = s->dalloc<float>(splash::kDim * PS);
+      S.uplus32 = s->dalloc<float>(splash::kDim * 2 * (size_t)s->GM.epad);
       S.fe32 = s->dalloc<float>(splash::kDim * (size_t)s->GM.epad);
       S.uplus = nullptr;
       SPLASH_CUDA(cudaMemset(S.W32, 0, splash::kDim * fp * sizeof(float)));
-      SPLASH_CUDA(cudaMemset(S.uplus32, 0, splash::kDim * PS * sizeof(float)));
+      SPLASH_CUDA(cudaMemset(S.uplus32, 0, splash::kDim * 2 * (size_t)s->GM.epad * sizeof(float)));
       s->n_partials = splash::mixed_partial_blocks(s->n_faces);
     } else {
       S.uplus = s->dalloc<double>(splash::kDim * PS);
@@ -781,12 +778,20 @@ int splash_write_t_curl(splash_solver* h, const char* path) {
   if (s->S.uplus) {
     SPLASH_CUDA(cudaMemcpy(up.data(), s->S.uplus, up.size() * sizeof(double), cudaMemcpyDeviceToHost));
   } else {
-    // packed FP32 edge states: [PS][4] (Sigma, l) then the Pi plane
-    std::vector<float> up32(splash::kDim * PS);
+    // packed FP32 edge states of the last stage, edge-major (owner side of
+    // edge e at e, reverse side at epad + e): [2 epad][4] (Sigma, l), then Pi
+    const size_t ne = 2 * (size_t)s->GM.epad;
+    std::vector<float> up32(splash::kDim * ne);
     SPLASH_CUDA(cudaMemcpy(up32.data(), s->S.uplus32, up32.size() * sizeof(float), cudaMemcpyDeviceToHost));
-    for (size_t q = 0; q < PS; ++q) {
-      for (int k = 0; k < 4; ++k) up[k * PS + q] = up32[4 * q + k];
-      up[4 * PS + q] = up32[4 * PS + q];
+    for (int i = 0; i < s->n_faces; ++i) {
+      const int n = s->wr_face_off[s->perm[i] + 1] - s->wr_face_off[s->perm[i]];
+      for (int j = 0; j < n; ++j) {
+        const size_t q = (size_t)j * s->fpad + i;
+        const unsigned se = (unsigned)s->h_slot_edge[q];
+        const size_t x = (se & 0x7fffffffu) + ((se >> 31) ? (size_t)s->GM.epad : 0);
+        for (int k = 0; k < 4; ++k) up[k * PS + q] = up32[4 * x + k];
+        up[4 * PS + q] = up32[4 * ne + x];
+      }
     }
   }
   double t;

@@ -62,12 +62,12 @@ struct Ensemble {
   std::vector<EnsInstance> inst;
   EnsInstance* d_inst = nullptr;
   double *U = nullptr, *acc = nullptr, *scal = nullptr, *U_snap = nullptr, *scal_snap = nullptr;
-  float *W32 = nullptr, *uplus = nullptr, *fe32 = nullptr;
+  float *W32 = nullptr, *fe32 = nullptr;
   unsigned int *err = nullptr, *err_snap = nullptr;
   unsigned long long* keys = nullptr;
-  int2 *d_rtiles = nullptr, *d_ftiles = nullptr, *d_etiles = nullptr;
-  int n_rtiles = 0, n_ftiles = 0, n_etiles = 0;
-  int order = 0, recon_width = 128;
+  int2 *d_ftiles = nullptr, *d_etiles = nullptr;
+  int n_ftiles = 0, n_etiles = 0;
+  int order = 0, recon_width = 128;  // tile order; threads per block of the edge launch
   double tuned_ms[9] = {0};
   std::vector<void*> allocs;
   cudaGraph_t graph = nullptr;
@@ -133,19 +133,14 @@ struct Ensemble {
   }
 
   int set_schedule(int ord, int width) {
-    const std::vector<int2> rt = make_tiles(width, ord);
     const std::vector<int2> ft = make_tiles(32, ord);
     const std::vector<int2> et = make_tiles(32, ord, true);
-    if (!d_rtiles) {
-      // capacity for the smallest width (the most tiles)
-      d_rtiles = dalloc<int2>(make_tiles(64, 0).size());
+    if (!d_ftiles) {
       d_ftiles = dalloc<int2>(ft.size());
       d_etiles = dalloc<int2>(et.size());
     }
-    ENS_CUDA(cudaMemcpy(d_rtiles, rt.data(), rt.size() * sizeof(int2), cudaMemcpyHostToDevice));
     ENS_CUDA(cudaMemcpy(d_ftiles, ft.data(), ft.size() * sizeof(int2), cudaMemcpyHostToDevice));
     ENS_CUDA(cudaMemcpy(d_etiles, et.data(), et.size() * sizeof(int2), cudaMemcpyHostToDevice));
-    n_rtiles = (int)rt.size();
     n_ftiles = (int)ft.size();
     n_etiles = (int)et.size();
     order = ord;
@@ -159,9 +154,7 @@ struct Ensemble {
   }
 
   cudaError_t launch_step(double dt0) {
-    return ensemble_step(d_inst, n, d_rtiles, n_rtiles, recon_width, d_ftiles, n_ftiles, d_etiles, n_etiles,
-                         max_slots, dt0,
-                         stream);
+    return ensemble_step(d_inst, n, d_ftiles, n_ftiles, d_etiles, n_etiles, recon_width, dt0, stream);
   }
 
   // Times every (order, width) candidate over a few steps, keeps the
@@ -305,20 +298,17 @@ int splash_ensemble_create(const splash_member* members, int n, int device, int 
         L.G.fcn = e->upload(L.sp.fcn);
         L.G.fcn32 = e->upload(mp.fcn32);
         L.G.area = e->upload(L.sp.area);
-        L.G.rc_sten = e->upload(mp.rc_sten);
-        L.G.rc_beta = e->upload(mp.rc_beta);
-        L.G.rc_h = e->upload(mp.rc_h);
-        L.G.rc_ec = e->upload(mp.rc_ec);
-        L.G.rc_en = e->upload(mp.rc_en);
         L.G.coef = e->upload(mp.coef);
         L.G.slot_edge = e->upload(mp.slot_edge);
         L.G.n_edges = mp.n_edges;
         L.G.epad = mp.epad;
-        L.G.e_own = e->upload(mp.e_own);
-        L.G.e_nbr = e->upload(mp.e_nbr);
+        L.G.e_ids = e->upload(mp.e_ids);
         L.G.e_ec = e->upload(mp.e_ec);
         L.G.e_en = e->upload(mp.e_en);
-        L.G.e_nxr = e->upload(mp.e_nxr);
+        L.G.e_eta = e->upload(mp.e_eta);
+        L.G.e_sten = e->upload(mp.e_sten);
+        L.G.e_beta = e->upload(mp.e_beta);
+        L.G.e_h = e->upload(mp.e_h);
         it = level_of.emplace(key, (int)e->levels.size()).first;
         e->levels.push_back(std::move(L));
       }
@@ -341,7 +331,6 @@ int splash_ensemble_create(const splash_member* members, int n, int device, int 
     e->U_snap = e->dalloc<double>(faces * kDim);
     e->acc = e->dalloc<double>(faces);
     e->W32 = e->dalloc<float>(faces * kDim);
-    e->uplus = e->dalloc<float>(slots * kDim);
     e->fe32 = e->dalloc<float>(edges * kDim);
     e->scal = e->dalloc<double>((size_t)n * kScCount);
     e->scal_snap = e->dalloc<double>((size_t)n * kScCount);
@@ -350,7 +339,6 @@ int splash_ensemble_create(const splash_member* members, int n, int device, int 
     e->keys = e->dalloc<unsigned long long>((size_t)n * 2);
     ENS_CUDA(cudaMemset(e->U, 0, faces * kDim * sizeof(double)));
     ENS_CUDA(cudaMemset(e->W32, 0, faces * kDim * sizeof(float)));
-    ENS_CUDA(cudaMemset(e->uplus, 0, slots * kDim * sizeof(float)));
     ENS_CUDA(cudaMemset(e->scal, 0, (size_t)n * kScCount * sizeof(double)));
     ENS_CUDA(cudaMemset(e->err, 0, (size_t)n * 4 * sizeof(unsigned)));
     size_t max_fpad = 0;
@@ -374,7 +362,7 @@ int splash_ensemble_create(const splash_member* members, int n, int device, int 
       I.G.acc_src = e->acc + e->off_face[i];
       I.S.U = e->U + e->off_face[i] * kDim;
       I.S.W32 = e->W32 + e->off_face[i] * kDim;
-      I.S.uplus32 = e->uplus + e->off_slot[i] * kDim;
+      I.S.uplus32 = nullptr;  // no writer reads a member's edge states
       I.S.fe32 = e->fe32 + e->off_edge[i] * kDim;
       I.S.scal = e->scal + (size_t)i * kScCount;
       I.S.err = e->err + (size_t)i * 4;

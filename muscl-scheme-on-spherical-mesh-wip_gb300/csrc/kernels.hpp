@@ -34,10 +34,9 @@ cudaError_t mixed_prepare(const DevGeomMixed& G, const DevState& S, const PhysPa
 // One do_step: the dt finalize (1 thread, argument dt0) then the four
 // stage launches.  Capturable; the finalize node's dt0 can be updated in an
 // instantiated graph (mixed_finalize_kernel_ptr identifies the node).
-// ev (optional): events recorded on st at the step's boundaries; six
-// (before the step, after finalize, after reconstruction 1, after stage 1,
-// after reconstruction 2, after stage 2), or with per_launch eight, one
-// before the step and one after each of its seven launches.
+// ev (optional): six events recorded on st around the step's five launches
+// (before the step, after finalize, after each stage's edge launch and
+// update launch); per_launch gives the same layout.
 cudaError_t mixed_step(const DevGeomMixed& G, const DevState& S, const PhysParams& P, double dt0,
                        cudaStream_t st, cudaEvent_t* ev = nullptr, bool per_launch = false);
 const void* mixed_finalize_kernel_ptr();
@@ -45,13 +44,12 @@ int mixed_partial_blocks(int n_faces);
 
 // ---- ensemble (step_mixed.cu): batched launches over instances ----
 // ftiles: (instance, first face) of 32-face tiles; etiles: (instance,
-// first edge) of 32-edge tiles; rtiles: tiles of `recon_width` faces for the
-// reconstruction (blockDim.x = recon_width).
+// first edge) of 32-edge tiles; edge_block: threads per block of the
+// reconstruction + edge-flux launch (a multiple of 32; one tile per warp).
 cudaError_t ensemble_prepare(const EnsInstance* inst, int n_inst, const int2* ftiles, int n_ftiles,
                              cudaStream_t st);
-cudaError_t ensemble_step(const EnsInstance* inst, int n_inst, const int2* rtiles, int n_rtiles,
-                          int recon_width, const int2* ftiles, int n_ftiles, const int2* etiles, int n_etiles,
-                          int max_slots, double dt0, cudaStream_t st);
+cudaError_t ensemble_step(const EnsInstance* inst, int n_inst, const int2* ftiles, int n_ftiles,
+                          const int2* etiles, int n_etiles, int edge_block, double dt0, cudaStream_t st);
 const void* ensemble_finalize_kernel_ptr();
 
 }  // namespace splash

@@ -102,23 +102,19 @@ struct DevGeomMixed {
   const float* fcn32;     // 3 planes, FP32 copy (source term)
   const double* area;
   const double* acc_src;  // accretion mass source, FP64
-  // reconstruction constants, four interleaved values per slot (read as
-  // one int4 / float4 each):
-  const int* rc_sten;     // stencil faces: plus pair, minus pair
-  const float* rc_beta;   // beta_plus 0, 1, beta_minus 0, 1
-  const float* rc_h;      // 1/H_plus, 1/H_minus, BM_dist, arc/area
-  const float* rc_ec;     // unit edge centre, H_plus/BM_dist
-  const float* rc_en;     // edge normal, H_minus/BM_dist
-  const float* coef;      // round_diff * chord / area
-  const int* slot_edge;   // edge of the slot, bit 31 set on the edge's reverse side
-  // interior edges, each once, in the orientation of the owner slot
+  const float* coef;      // per slot: round_diff * chord / area
+  const int* slot_edge;   // per slot: its edge, bit 31 set on the edge's reverse side
+  // interior edges, each once, in owner order; records of four interleaved
+  // values (read as one int4 / float4 each), see MixedPlanes
   int n_edges;
   int epad;               // n_edges rounded up to 32
-  const int* e_own;       // [epad] owner slot (slot-plane index)
-  const int* e_nbr;       // [epad] reverse slot
-  const float* e_ec;      // 3 planes of epad, the owner's unit edge centre
-  const float* e_en;      // 3 planes of epad
-  const float* e_nxr;     // 3 planes of epad, cross(en, ec)
+  const int* e_ids;       // f | n_f << 28, g | n_g << 28, bits of (n x R).z, 0
+  const float* e_ec;      // owner's unit edge centre, (n x R).x
+  const float* e_en;      // owner's edge normal, (n x R).y
+  const float* e_eta;     // H+/BM, H-/BM: owner, then reverse slot
+  const int* e_sten;      // [2][epad]: stencil faces, owner then reverse slot
+  const float* e_beta;    // [2][epad]: beta_plus 0, 1, beta_minus 0, 1
+  const float* e_h;       // [2][epad]: 1/H_plus, 1/H_minus, BM_dist, arc/area
 };
 
 // Solver state on the device.
@@ -128,7 +124,8 @@ struct DevState {
   double* W1;     // (Sigma, l, Pi) after stage 1, kDim planes
   double* uplus;  // reconstructed edge states, kDim * max_slots planes of fpad
   float* W32;     // mixed path: (Sigma, l, Pi) in FP32: [fpad] float4 (Sigma, l), then a Pi plane
-  float* uplus32; // mixed path: edge states, same packing over max_slots * fpad slots
+  float* uplus32; // mixed path: stage-2 edge states, packed like W32 over 2 * epad entries
+                  // (owner side of edge e at e, reverse side at epad + e); may be null
   float* fe32;    // mixed path: FP32 Riemann flux of every edge, packed like W32 over epad edges
   double* partial;  // per-block partial records (kPartialStride doubles)
   double* scal;   // device scalars, see ScalarSlot

@@ -2,6 +2,7 @@
 #include "slot_planes.hpp"
 
 #include <cmath>
+#include <cstring>
 #include <stdexcept>
 
 #include "hilbert.hpp"
@@ -190,48 +191,20 @@ std::vector<double> accretion_source_fcn(const std::vector<double>& fcn, int n_f
 }
 
 MixedPlanes make_mixed_planes(const SlotPlanes& sp) {
-  auto tof = [](const std::vector<double>& v) { return std::vector<float>(v.begin(), v.end()); };
   MixedPlanes mp;
   const size_t PS = sp.PS();
-  mp.fcn32 = tof(sp.fcn);
-  mp.beta = tof(sp.beta);
-  mp.bm = tof(sp.bm);
-  mp.eta = tof(sp.eta);
-  mp.arc = tof(sp.arc);
-  mp.ec = tof(sp.ec);
-  mp.en = tof(sp.en);
-  mp.inv_h.assign(2 * PS, 1.0f);
-  for (size_t q = 0; q < 2 * PS; ++q) mp.inv_h[q] = (float)(1.0 / sp.hpm[q]);
+  mp.fcn32.assign(sp.fcn.begin(), sp.fcn.end());
   mp.coef.assign(PS, 0.0f);
   for (int i = 0; i < sp.n_faces; ++i)
     for (int j = 0; j < (int)sp.nslots[i]; ++j) {
       const size_t q = (size_t)j * sp.fpad + i;
       mp.coef[q] = (float)(sp.round_diff * sp.chord[q] / sp.area[i]);
     }
-  mp.rc_sten.assign(4 * PS, 0);
-  mp.rc_beta.assign(4 * PS, 0.f);
-  mp.rc_h.assign(4 * PS, 0.f);
-  mp.rc_ec.assign(4 * PS, 0.f);
-  mp.rc_en.assign(4 * PS, 0.f);
-  for (size_t q = 0; q < PS; ++q) {
-    for (int c = 0; c < 4; ++c) {
-      mp.rc_sten[4 * q + c] = sp.sten[c * PS + q];
-      mp.rc_beta[4 * q + c] = mp.beta[c * PS + q];
-    }
-    mp.rc_h[4 * q + 0] = mp.inv_h[q];
-    mp.rc_h[4 * q + 1] = mp.inv_h[PS + q];
-    mp.rc_h[4 * q + 2] = mp.bm[q];
-    mp.rc_h[4 * q + 3] = mp.arc[q];
-    for (int c = 0; c < 3; ++c) {
-      mp.rc_ec[4 * q + c] = mp.ec[c * PS + q];
-      mp.rc_en[4 * q + c] = mp.en[c * PS + q];
-    }
-    mp.rc_ec[4 * q + 3] = mp.eta[q];
-    mp.rc_en[4 * q + 3] = mp.eta[PS + q];
-  }
+  if (sp.n_faces >= (1 << 28)) throw std::runtime_error("too many faces for the edge records");
   // edges in ascending owner order (plane-major, faces ascending within a
   // plane): the reverse side of every edge is met either as an owner's
   // neighbour before it, or as an owner itself
+  std::vector<int> own, nbr;
   mp.slot_edge.assign(PS, 0);
   for (int j = 0; j < sp.max_slots; ++j)
     for (int i = 0; i < sp.n_faces; ++i) {
@@ -239,26 +212,56 @@ MixedPlanes make_mixed_planes(const SlotPlanes& sp) {
       const int s = j * sp.fpad + i, r = sp.rev[s];
       if (r == s) throw std::runtime_error("slot without a neighbour");
       if (s < r) {
-        const int e = (int)mp.e_own.size();
-        mp.e_own.push_back(s);
-        mp.e_nbr.push_back(r);
+        const int e = (int)own.size();
+        own.push_back(s);
+        nbr.push_back(r);
         mp.slot_edge[s] = e;
         mp.slot_edge[r] = (int)((unsigned)e | 0x80000000u);
       }
     }
-  mp.n_edges = (int)mp.e_own.size();
-  mp.epad = (mp.n_edges + 31) / 32 * 32;
-  mp.e_own.resize(mp.epad, mp.n_edges ? mp.e_own[0] : 0);
-  mp.e_nbr.resize(mp.epad, mp.n_edges ? mp.e_nbr[0] : 0);
-  mp.e_ec.assign(3 * (size_t)mp.epad, 0.f);
-  mp.e_en.assign(3 * (size_t)mp.epad, 0.f);
-  mp.e_nxr.assign(3 * (size_t)mp.epad, 0.f);
+  mp.n_edges = (int)own.size();
+  const int ep = mp.epad = (mp.n_edges + 31) / 32 * 32;
+  mp.e_ids.assign(4 * (size_t)ep, 0);
+  mp.e_ec.assign(4 * (size_t)ep, 0.f);
+  mp.e_en.assign(4 * (size_t)ep, 0.f);
+  mp.e_eta.assign(4 * (size_t)ep, 1.f);
+  mp.e_sten.assign(8 * (size_t)ep, 0);
+  mp.e_beta.assign(8 * (size_t)ep, 0.f);
+  mp.e_h.assign(8 * (size_t)ep, 0.f);
   for (int e = 0; e < mp.n_edges; ++e) {
-    const size_t s = (size_t)mp.e_own[e];
+    const size_t side_slot[2] = {(size_t)own[e], (size_t)nbr[e]};
+    int face[2], n[2];
+    for (int k = 0; k < 2; ++k) {
+      face[k] = (int)(side_slot[k] % sp.fpad);
+      n[k] = sp.nslots[face[k]];
+    }
+    int* id = &mp.e_ids[4 * (size_t)e];
+    id[0] = face[0] | (n[0] << 28);
+    id[1] = face[1] | (n[1] << 28);
+    const size_t so = side_slot[0];
     for (int c = 0; c < 3; ++c) {
-      mp.e_ec[c * (size_t)mp.epad + e] = mp.ec[c * PS + s];
-      mp.e_en[c * (size_t)mp.epad + e] = mp.en[c * PS + s];
-      mp.e_nxr[c * (size_t)mp.epad + e] = (float)sp.nxr[c * PS + s];
+      mp.e_ec[4 * (size_t)e + c] = (float)sp.ec[c * PS + so];
+      mp.e_en[4 * (size_t)e + c] = (float)sp.en[c * PS + so];
+    }
+    // the owner's n x R (FP64, rounded once) rides in the spare lanes
+    mp.e_ec[4 * (size_t)e + 3] = (float)sp.nxr[so];
+    mp.e_en[4 * (size_t)e + 3] = (float)sp.nxr[PS + so];
+    const float nz = (float)sp.nxr[2 * PS + so];
+    std::memcpy(&id[2], &nz, 4);
+    id[3] = 0;
+    for (int k = 0; k < 2; ++k) {
+      const size_t q = side_slot[k];
+      const size_t o = 4 * ((size_t)k * ep + e);
+      mp.e_eta[4 * (size_t)e + 2 * k] = (float)sp.eta[q];
+      mp.e_eta[4 * (size_t)e + 2 * k + 1] = (float)sp.eta[PS + q];
+      for (int c = 0; c < 4; ++c) {
+        mp.e_sten[o + c] = sp.sten[c * PS + q];
+        mp.e_beta[o + c] = (float)sp.beta[c * PS + q];
+      }
+      mp.e_h[o + 0] = (float)(1.0 / sp.hpm[q]);
+      mp.e_h[o + 1] = (float)(1.0 / sp.hpm[PS + q]);
+      mp.e_h[o + 2] = (float)sp.bm[q];
+      mp.e_h[o + 3] = (float)sp.arc[q];
     }
   }
   return mp;

@@ -47,24 +47,27 @@ std::vector<double> accretion_source_fcn(const std::vector<double>& fcn, int n_f
                                          std::vector<double>* d_rate = nullptr,
                                          std::vector<double>* d_tilt = nullptr);
 
-// FP32 planes of the mixed path.  The Riemann flux of an interior edge is
-// evaluated once, in the orientation of its owner: of the edge's two slots
-// the one with the smaller slot-plane index.  Edges are numbered in owner
-// order; slot_edge maps every slot to its edge, with bit 31 set on the
-// reverse (non-owner) side, whose flux is the owner's with the sign flipped
-// (every Riemann solver here satisfies F(uR, uL, -n) = -F(uL, uR, n)).
+// FP32 planes of the mixed path.  The mixed step works per interior edge:
+// one thread reconstructs the edge states of the edge's two slots (owner:
+// the slot with the smaller slot-plane index; reverse: the other) and
+// evaluates the Riemann flux once, in the owner's orientation.  Edges are
+// numbered in owner order; slot_edge maps every slot to its edge, with bit
+// 31 set on the reverse side, whose flux is the owner's with the sign
+// flipped (every Riemann solver here satisfies F(uR, uL, -n) = -F(uL, uR, n)).
+// The two sides share the edge centre (the same two vertices) and have
+// opposite normals (exactly, in the reference geometry), so the reverse
+// slot is reconstructed with the owner's centre and the negated normal.
+// Per-edge records hold four interleaved values (one 16-byte load each).
 struct MixedPlanes {
-  std::vector<float> fcn32, beta, inv_h, bm, eta, arc, ec, en, coef;
-  // the reconstruction's constants of slot s as four interleaved values
-  // (one 16-byte load each): stencil faces (a, b, c, d); (beta_plus 0, 1,
-  // beta_minus 0, 1); (1/H_plus, 1/H_minus, BM_dist, arc/area);
-  // (unit edge centre, H_plus/BM_dist); (edge normal, H_minus/BM_dist)
-  std::vector<int> rc_sten;
-  std::vector<float> rc_beta, rc_h, rc_ec, rc_en;
+  std::vector<float> fcn32, coef;      // per face; per slot (slot planes)
   int n_edges = 0, epad = 0;           // epad: n_edges rounded up to 32
-  std::vector<int> e_own, e_nbr;       // [epad] slot-plane indices of the two sides
-  std::vector<float> e_ec, e_en, e_nxr;  // 3 planes of epad: the owner slot's geometry
   std::vector<int> slot_edge;          // [max_slots * fpad]
+  std::vector<int> e_ids;              // [epad][4]: f | n_f << 28, g | n_g << 28, bits of (n x R).z, 0
+  std::vector<float> e_ec, e_en;       // [epad][4]: owner's unit edge centre | (n x R).x, normal | (n x R).y
+  std::vector<float> e_eta;            // [epad][4]: H+/BM, H-/BM of the owner, then of the reverse slot
+  std::vector<int> e_sten;             // [2][epad][4]: stencil faces (plus pair, minus pair), owner then reverse
+  std::vector<float> e_beta;           // [2][epad][4]: beta_plus 0, 1, beta_minus 0, 1
+  std::vector<float> e_h;              // [2][epad][4]: 1/H_plus, 1/H_minus, BM_dist, arc/area
 };
 MixedPlanes make_mixed_planes(const SlotPlanes& sp);
 

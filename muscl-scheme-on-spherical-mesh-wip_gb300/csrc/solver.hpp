@@ -40,6 +40,7 @@ struct Solver {
 
   // numbering: perm[internal] = reference face id, iperm = inverse
   std::vector<int> perm, iperm;
+  std::vector<int> h_slot_edge;  // mixed path: slot -> edge map (the writers' edge-state lookup)
 
   // reference-order host copies used by the writers
   std::vector<double> wr_vertices, wr_face_centers, wr_area;
@@ -85,7 +86,7 @@ struct Solver {
   // one un-captured step; ev as for mixed_step (the FP64 step has five
   // launches, so its two layouts coincide)
   cudaError_t launch_step(cudaEvent_t* ev, double dt0, bool per_launch = false);
-  int launches_per_step() const { return precision == SPLASH_PREC_MIXED ? 7 : 5; }
+  int launches_per_step() const { return 5; }
   cudaError_t launch_prepare();
   static int check_cuda(cudaError_t e, const char* what);
 };

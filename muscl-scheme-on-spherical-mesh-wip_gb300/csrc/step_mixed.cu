@@ -30,6 +30,10 @@ namespace mx {
 namespace {
 
 constexpr int kBlock = 128;
+constexpr int kFaceTile = 32;  // faces (or edges) per tile of the batched launches
+// slot bound of the mixed path: solvers and ensembles reject meshes with
+// faces of more than 8 edges at creation
+constexpr int kMaxFaceSlots = 8;
 
 __device__ __forceinline__ F3 plane3f(const float* p, int stride, int i) {
   return F3{p[i], p[stride + i], p[2 * stride + i]};
@@ -319,47 +323,34 @@ __global__ void finalize_kernel(DevState S, PhysParams P, double dt0) {
   finalize_body(S, P, dt0);
 }
 
-// find_U_edges (MUSCL_base.hpp:361-434) in FP32; edge field 4 stays Pi.
-// One thread per (face, slot): blockIdx.y is the slot plane, so a warp reads
-// consecutive faces of one plane and the 4-face gathers of six slots are in
-// flight at once instead of one after the other.
-__device__ __forceinline__ void recon_body(const DevGeomMixed& G, const DevState& S, const PhysParams& P,
-                                           int f, int j) {
-  if (f >= G.n_faces) return;
-  const int n = G.nslots[f];
-  if (j >= n) return;
-  const int fp = G.fpad;
-  const int PS = G.max_slots * fp;
-  const float* W = S.W32;
-  const int s = j * fp + f;
-  // the slot's constants: five 16-byte loads
-  const int4 st = reinterpret_cast<const int4*>(G.rc_sten)[s];
-  const float4 bt = reinterpret_cast<const float4*>(G.rc_beta)[s];
-  const float4 hh = reinterpret_cast<const float4*>(G.rc_h)[s];
-  const float4 ce = reinterpret_cast<const float4*>(G.rc_ec)[s];
-  const float4 ne = reinterpret_cast<const float4*>(G.rc_en)[s];
-  const int ia = st.x, ib = st.y, ic = st.z, id = st.w;
-  const float bp0 = bt.x, bp1 = bt.y, bm0 = bt.z, bm1 = bt.w;
-  const float ihp = hh.x, ihm = hh.y, bmd = hh.z, arc_a = hh.w;
-  const F3 ec = f3(ce.x, ce.y, ce.z);
-  const F3 en = f3(ne.x, ne.y, ne.z);
-  const float eta_p = ce.w, eta_m = ne.w;
-  griddep_wait();
-  const float dt = reinterpret_cast<const float2*>(S.scal + kScDtF)->x;
+// find_U_edges (MUSCL_base.hpp:361-434) in FP32 for one slot: the edge
+// state (Sigma, l, Pi) of face f (n edges) across the slot's edge, from the
+// face, its four stencil faces and the slot's constants.  Edge field 4 stays
+// Pi; the isothermal solver leaves it 0.
+struct SlotConsts {
+  int4 st;    // stencil faces: plus pair, minus pair
+  float4 bt;  // beta_plus 0, 1, beta_minus 0, 1
+  float4 hh;  // 1/H_plus, 1/H_minus, BM_dist, arc/area
+  float eta_p, eta_m;
+};
+
+__device__ __forceinline__ void recon_slot(const float* W, int fp, int f, int n, const SlotConsts& sc, F3 ec,
+                                           F3 en, float dt, const PhysParams& P, float* up) {
+  const int ia = sc.st.x, ib = sc.st.y, ic = sc.st.z, id = sc.st.w;
+  const float bp0 = sc.bt.x, bp1 = sc.bt.y, bm0 = sc.bt.z, bm1 = sc.bt.w;
+  const float ihp = sc.hh.x, ihm = sc.hh.y, bmd = sc.hh.z, arc_a = sc.hh.w;
   // the face and its four stencil faces: one 16-byte gather each for
   // (Sigma, l), one more each for Pi (adiabatic only)
   const float4 w4 = ld4(W, f), a4 = ld4(W, ia), b4 = ld4(W, ib), c4 = ld4(W, ic), d4 = ld4(W, id);
   const float w[4] = {w4.x, w4.y, w4.z, w4.w};
   const float wa[4] = {a4.x, a4.y, a4.z, a4.w}, wb[4] = {b4.x, b4.y, b4.z, b4.w};
   const float wc[4] = {c4.x, c4.y, c4.z, c4.w}, wd[4] = {d4.x, d4.y, d4.z, d4.w};
-  float4 o;
-  float* up = reinterpret_cast<float*>(&o);
   if (P.solver == kSolverIsoHLLE) {
     // isothermal: 4 fields, superbee limiter with the Courant factor
     // (a + v.n) dt arc / area (physics/isothermal.hpp:269-320)
     const F3 vel = scal(cross3(ec, f3(w[1], w[2], w[3])), -1.0f / w[0]);
     const float nu_plus = (1.f + dot3(vel, en)) * dt * arc_a;
-    const float eta = eta_m;
+    const float eta = sc.eta_m;
     const float sb_scale = eta * 2.f / ((float)(2 * n) * nu_plus);
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
@@ -368,7 +359,7 @@ __device__ __forceinline__ void recon_body(const DevGeomMixed& G, const DevState
       const float lim = iso_limiter_field(pm / pp, eta, sb_scale);
       up[k] = w[k] + pp * lim * bmd;
     }
-    reinterpret_cast<float4*>(S.uplus32)[s] = o;
+    up[4] = 0.f;
     return;
   }
   const float* Wp = W + 4 * (size_t)fp;
@@ -378,62 +369,71 @@ __device__ __forceinline__ void recon_body(const DevGeomMixed& G, const DevState
   const float c = sqrtf(gam * wp / w[0]);
   const F3 vel = scal(cross3(ec, f3(w[1], w[2], w[3])), inv_rho);
   const float nu_plus = (c + dot3(vel, en)) * dt * arc_a;
-  const float sb_scale = eta_m / ((float)(2 * n) * nu_plus);
+  const float sb_scale = sc.eta_m / ((float)(2 * n) * nu_plus);
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     const float pp = (bp0 * wa[k] + bp1 * wb[k] - w[k]) * ihp;
     const float pm = (w[k] - (bm0 * wc[k] + bm1 * wd[k])) * ihm;
-    const float lim = limiter_field(pm / pp, nu_plus, eta_p, sb_scale);
+    const float lim = limiter_field(pm / pp, nu_plus, sc.eta_p, sb_scale);
     up[k] = w[k] + pp * lim * bmd;
   }
-  reinterpret_cast<float4*>(S.uplus32)[s] = o;
   {
     const float pp = (bp0 * Wp[ia] + bp1 * Wp[ib] - wp) * ihp;
     const float pm = (wp - (bm0 * Wp[ic] + bm1 * Wp[id])) * ihm;
-    const float lim = limiter_field(pm / pp, nu_plus, eta_p, sb_scale);
-    S.uplus32[4 * (size_t)PS + s] = wp + pp * lim * bmd;
+    const float lim = limiter_field(pm / pp, nu_plus, sc.eta_p, sb_scale);
+    up[4] = wp + pp * lim * bmd;
   }
 }
 
-// at most 51 registers (10 blocks of 128 per SM): the gathers need warps in
-// flight more than registers
-__global__ void __launch_bounds__(kBlock, 10) reconstruct_kernel(DevGeomMixed G, DevState S, PhysParams P) {
-  griddep_launch_dependents();
-  recon_body(G, S, P, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
-}
-
-constexpr int kFaceTile = 32;  // faces (or edges) per tile of the batched launches
-// slot bound of the mixed path: solvers and ensembles reject meshes with
-// faces of more than 8 edges at creation
-constexpr int kMaxFaceSlots = 8;
-
-// find_flux_var (MUSCL_base.hpp:345-359) per interior edge: one thread per
-// edge evaluates the Riemann flux once, in the orientation of the edge's
-// owner slot (own edge state left, the reverse slot's right, the owner's
-// geometry), and stores it packed like W32.  The reference evaluates the
-// flux from both faces; every solver here satisfies
-// F(uR, uL, -n) = -F(uL, uR, n), so the reverse side takes the owner's flux
-// negated (the two evaluations differ only by FP32 rounding) and each edge
-// conserves exactly what it moves.  Stop bits are folded per warp.
-__device__ __forceinline__ void edge_flux_body(const DevGeomMixed& G, const DevState& S, const PhysParams& P,
-                                               int e) {
+// One stage's reconstruction and Riemann fluxes, one thread per interior
+// edge (find_U_edges + find_flux_var, MUSCL_base.hpp:361-434, 345-359): the
+// edge states of the owner slot (face f) and of the reverse slot (face g,
+// same edge centre, negated normal), then the flux once in the owner's
+// orientation (the reverse side takes it negated in the update).  The
+// reference evaluates the flux from both faces; every solver here satisfies
+// F(uR, uL, -n) = -F(uL, uR, n), so each edge moves exactly what it removes
+// from its neighbour.  The edge states never go to memory, except in stage 2
+// when the state has an edge-state buffer (edge-major, for the writers that
+// read the last stage's edge states; batched instances have none).
+// Stop bits are folded per warp.
+template <int STAGE>
+__device__ __forceinline__ void edge_body(const DevGeomMixed& G, const DevState& S, const PhysParams& P, int e) {
   const bool live = e < G.n_edges;
-  const int PS = G.max_slots * G.fpad;
-  int so = 0, sr = 0;
-  SlotGeomF g;
+  int4 ids = make_int4(0, 0, 0, 0);
+  float4 ce = make_float4(0.f, 0.f, 0.f, 0.f), ne = ce, et = ce;
+  SlotConsts so{}, sr{};
   if (live) {
-    so = G.e_own[e];
-    sr = G.e_nbr[e];
-    g.ec = plane3f(G.e_ec, G.epad, e);
-    g.en = plane3f(G.e_en, G.epad, e);
-    g.nxr = plane3f(G.e_nxr, G.epad, e);
+    ids = reinterpret_cast<const int4*>(G.e_ids)[e];
+    ce = reinterpret_cast<const float4*>(G.e_ec)[e];
+    ne = reinterpret_cast<const float4*>(G.e_en)[e];
+    et = reinterpret_cast<const float4*>(G.e_eta)[e];
+    so.st = reinterpret_cast<const int4*>(G.e_sten)[e];
+    sr.st = reinterpret_cast<const int4*>(G.e_sten)[G.epad + e];
+    so.bt = reinterpret_cast<const float4*>(G.e_beta)[e];
+    sr.bt = reinterpret_cast<const float4*>(G.e_beta)[G.epad + e];
+    so.hh = reinterpret_cast<const float4*>(G.e_h)[e];
+    sr.hh = reinterpret_cast<const float4*>(G.e_h)[G.epad + e];
   }
+  so.eta_p = et.x;
+  so.eta_m = et.y;
+  sr.eta_p = et.z;
+  sr.eta_m = et.w;
   griddep_wait();
   unsigned bits = 0;
   if (live) {
+    const float dt = reinterpret_cast<const float2*>(S.scal + kScDtF)->x;
+    SlotGeomF g;
+    g.ec = f3(ce.x, ce.y, ce.z);
+    g.en = f3(ne.x, ne.y, ne.z);
+    g.nxr = f3(ce.w, ne.w, __int_as_float(ids.z));
     float uL[kDim], uR[kDim], F[kDim] = {0.f, 0.f, 0.f, 0.f, 0.f};
-    ld5(S.uplus32, PS, so, uL);
-    ld5(S.uplus32, PS, sr, uR);
+    recon_slot(S.W32, G.fpad, ids.x & 0x0fffffff, ids.x >> 28, so, g.ec, g.en, dt, P, uL);
+    recon_slot(S.W32, G.fpad, ids.y & 0x0fffffff, ids.y >> 28, sr, g.ec, f3(-g.en.x, -g.en.y, -g.en.z), dt,
+               P, uR);
+    if (STAGE == 2 && S.uplus32 != nullptr) {
+      st5(S.uplus32, 2 * G.epad, e, uL);
+      st5(S.uplus32, 2 * G.epad, G.epad + e, uR);
+    }
     bits = (P.solver == kSolverIsoHLLE) ? iso_flux_star(uL, uR, g, F) : flux_star(uL, uR, g, P.gam_f, P.solver, F);
 #pragma unroll
     for (int k = 0; k < kDim; ++k)
@@ -444,9 +444,11 @@ __device__ __forceinline__ void edge_flux_body(const DevGeomMixed& G, const DevS
   if ((threadIdx.x & 31) == 0 && bits) atomicOr(S.err, bits);
 }
 
-__global__ void __launch_bounds__(kBlock) edge_flux_kernel(DevGeomMixed G, DevState S, PhysParams P) {
+// at most 85 registers (6 blocks of 128 per SM; measured best of 5, 6, 8)
+template <int STAGE>
+__global__ void __launch_bounds__(kBlock, 6) edge_kernel(DevGeomMixed G, DevState S, PhysParams P) {
   griddep_launch_dependents();
-  edge_flux_body(G, S, P, blockIdx.x * blockDim.x + threadIdx.x);
+  edge_body<STAGE>(G, S, P, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // res2d + RK combine (MUSCL_base.hpp:238-276, 124-161) of face f: the
@@ -571,24 +573,18 @@ __global__ void ens_finalize_kernel(const EnsInstance* __restrict__ inst, int n,
   if (i < n) finalize_body(inst[i].S, inst[i].P, dt0);
 }
 
-__global__ void __launch_bounds__(256, 5) ens_reconstruct_kernel(const EnsInstance* __restrict__ inst,
-                                                              const int2* __restrict__ tiles) {
-  griddep_launch_dependents();
-  const int2 t = tiles[blockIdx.x];
-  const EnsInstance& I = inst[t.x];
-  recon_body(I.G, I.S, I.P, t.y + threadIdx.x, blockIdx.y);
-}
-
-// edge fluxes: one 32-edge tile per warp (tiles hold (instance, first edge))
+// reconstruction + edge fluxes: one 32-edge tile per warp (tiles hold
+// (instance, first edge))
 constexpr int kWarpTiles = kBlock / 32;
-__global__ void __launch_bounds__(kBlock) ens_edge_flux_kernel(const EnsInstance* __restrict__ inst,
-                                                               const int2* __restrict__ tiles, int n_tiles) {
+template <int STAGE>
+__global__ void __launch_bounds__(256) ens_edge_kernel(const EnsInstance* __restrict__ inst,
+                                                       const int2* __restrict__ tiles, int n_tiles) {
   griddep_launch_dependents();
-  const int tile = blockIdx.x * kWarpTiles + (threadIdx.x >> 5);
+  const int tile = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (tile >= n_tiles) return;  // whole warps: stop bits fold per warp
   const int2 t = tiles[tile];
   const EnsInstance& I = inst[t.x];
-  edge_flux_body(I.G, I.S, I.P, t.y + (threadIdx.x & 31));
+  edge_body<STAGE>(I.G, I.S, I.P, t.y + (threadIdx.x & 31));
 }
 
 // update: one 32-face tile per warp
@@ -640,8 +636,7 @@ cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStre
 }  // namespace
 
 cudaError_t mixed_step(const DevGeomMixed& G, const DevState& S, const PhysParams& P, double dt0,
-                       cudaStream_t st, cudaEvent_t* ev, bool per_launch) {
-  const dim3 rgrid(mx::blocks_for(G.n_faces), G.max_slots);
+                       cudaStream_t st, cudaEvent_t* ev, bool /*per_launch: five launches, same layout*/) {
   const dim3 egrid(mx::blocks_for(G.n_edges));
   const dim3 ugrid(mx::blocks_for(G.n_faces));
   cudaError_t e = cudaSuccess;
@@ -651,18 +646,14 @@ cudaError_t mixed_step(const DevGeomMixed& G, const DevState& S, const PhysParam
   if (ev) cudaEventRecord(ev[0], st);
   chk(launch_pdl(mx::finalize_kernel, dim3(1), dim3(1), st, S, P, dt0));
   if (ev) cudaEventRecord(ev[1], st);
-  chk(launch_pdl(mx::reconstruct_kernel, rgrid, dim3(mx::kBlock), st, G, S, P));
+  chk(launch_pdl(mx::edge_kernel<1>, egrid, dim3(mx::kBlock), st, G, S, P));
   if (ev) cudaEventRecord(ev[2], st);
-  chk(launch_pdl(mx::edge_flux_kernel, egrid, dim3(mx::kBlock), st, G, S, P));
-  if (ev && per_launch) cudaEventRecord(ev[3], st);
   chk(launch_pdl(mx::update_kernel<1>, ugrid, dim3(mx::kBlock), st, G, S, P));
-  if (ev) cudaEventRecord(ev[per_launch ? 4 : 3], st);
-  chk(launch_pdl(mx::reconstruct_kernel, rgrid, dim3(mx::kBlock), st, G, S, P));
-  if (ev) cudaEventRecord(ev[per_launch ? 5 : 4], st);
-  chk(launch_pdl(mx::edge_flux_kernel, egrid, dim3(mx::kBlock), st, G, S, P));
-  if (ev && per_launch) cudaEventRecord(ev[6], st);
+  if (ev) cudaEventRecord(ev[3], st);
+  chk(launch_pdl(mx::edge_kernel<2>, egrid, dim3(mx::kBlock), st, G, S, P));
+  if (ev) cudaEventRecord(ev[4], st);
   chk(launch_pdl(mx::update_kernel<2>, ugrid, dim3(mx::kBlock), st, G, S, P));
-  if (ev) cudaEventRecord(ev[per_launch ? 7 : 5], st);
+  if (ev) cudaEventRecord(ev[5], st);
   return e != cudaSuccess ? e : cudaGetLastError();
 }
 
@@ -673,22 +664,19 @@ cudaError_t ensemble_prepare(const EnsInstance* inst, int n_inst, const int2* ft
   return cudaGetLastError();
 }
 
-cudaError_t ensemble_step(const EnsInstance* inst, int n_inst, const int2* rtiles, int n_rtiles,
-                          int recon_width, const int2* ftiles, int n_ftiles, const int2* etiles, int n_etiles,
-                          int max_slots, double dt0, cudaStream_t st) {
-  const dim3 rgrid(n_rtiles, max_slots);
-  const dim3 egrid((n_etiles + mx::kWarpTiles - 1) / mx::kWarpTiles);
+cudaError_t ensemble_step(const EnsInstance* inst, int n_inst, const int2* ftiles, int n_ftiles,
+                          const int2* etiles, int n_etiles, int edge_block, double dt0, cudaStream_t st) {
+  const int wpb = edge_block / 32;
+  const dim3 egrid((n_etiles + wpb - 1) / wpb);
   const dim3 ugrid((n_ftiles + mx::kWarpTiles - 1) / mx::kWarpTiles);
   cudaError_t e = cudaSuccess;
   auto chk = [&](cudaError_t r) {
     if (e == cudaSuccess) e = r;
   };
   chk(launch_pdl(mx::ens_finalize_kernel, dim3((n_inst + 127) / 128), dim3(128), st, inst, n_inst, dt0));
-  chk(launch_pdl(mx::ens_reconstruct_kernel, rgrid, dim3(recon_width), st, inst, rtiles));
-  chk(launch_pdl(mx::ens_edge_flux_kernel, egrid, dim3(mx::kBlock), st, inst, etiles, n_etiles));
+  chk(launch_pdl(mx::ens_edge_kernel<1>, egrid, dim3(edge_block), st, inst, etiles, n_etiles));
   chk(launch_pdl(mx::ens_update_kernel<1>, ugrid, dim3(mx::kBlock), st, inst, ftiles, n_ftiles));
-  chk(launch_pdl(mx::ens_reconstruct_kernel, rgrid, dim3(recon_width), st, inst, rtiles));
-  chk(launch_pdl(mx::ens_edge_flux_kernel, egrid, dim3(mx::kBlock), st, inst, etiles, n_etiles));
+  chk(launch_pdl(mx::ens_edge_kernel<2>, egrid, dim3(edge_block), st, inst, etiles, n_etiles));
   chk(launch_pdl(mx::ens_update_kernel<2>, ugrid, dim3(mx::kBlock), st, inst, ftiles, n_ftiles));
   return e != cudaSuccess ? e : cudaGetLastError();
 }

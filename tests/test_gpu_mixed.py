@@ -120,3 +120,33 @@ def test_mixed_dt0_changes_between_steps():
     for dt0 in (1e-3, 5e-4, 5e-4, 2e-4, 1e-3):
         f.do_step(dt0)
     assert abs(f.time() - s.time()) < 1e-15
+
+
+@pytest.mark.parametrize("solver", [2, 4])
+def test_mixed_edge_state_writer_matches_fp64(tmp_path, solver):
+    """write_t_curl reads the last stage's edge states; the mixed path keeps
+    them edge-major (two sides per edge) and the writer maps every slot to
+    its edge and side.  After the same steps the mixed and FP64 writers must
+    agree to mixed-precision tolerance (a wrong slot mapping scrambles the
+    per-face vorticity by O(1))."""
+    import splash_gb300 as sg
+
+    mesh = mesh_of("hex", 4)
+    g = sg.Geometry(mesh)
+    gam = sg.initial_conditions.gam2d(4 / 3)
+    U0 = sg.initial_conditions.rotating_blob(g.unit_face_centers(), gam, seed=4)
+    dim = 4 if solver == 4 else 5
+    U0 = np.ascontiguousarray(U0[:, :dim])
+    out = {}
+    for prec in (sg.PREC_FP64, sg.PREC_MIXED):
+        s = sg.Solver(mesh, U0, dim, gam, 0.0, False, params=sg.SolverParams(), solver=solver, precision=prec)
+        s.do_steps(20, 1e-3)
+        path = tmp_path / f"curl_{prec}.dat"
+        s.write_t_curl(path)
+        out[prec] = np.array(path.read_text().split(), dtype=float)
+        s.close()
+    a, b = out[sg.PREC_FP64], out[sg.PREC_MIXED]
+    assert a.shape == b.shape == (g.n_faces + 1,)
+    scale = np.max(np.abs(a[1:]))
+    assert scale > 0
+    assert np.max(np.abs(a[1:] - b[1:])) < 1e-4 * scale
