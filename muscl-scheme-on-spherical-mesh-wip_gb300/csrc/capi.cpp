@@ -274,16 +274,18 @@ cudaError_t Solver::launch_step(cudaEvent_t* ev, double dt0, bool per_launch) {
 }
 
 int Solver::upload_state(const double* U_ref) {
-  if (host_direct) {
-    // the scatter kernel reads the caller's array over the coherent link
-    SPLASH_CUDA(fp64_scatter_state(U_ref, d_iperm, S.U, n_faces, fpad, stream, dim));
-    SPLASH_CUDA(launch_prepare());
+  const double* src = U_ref;  // with host_direct the kernels read the caller's array over the coherent link
+  if (!host_direct) {
+    std::memcpy(h_stage, U_ref, (size_t)n_faces * dim * sizeof(double));
+    SPLASH_CUDA(cudaMemcpyAsync(d_stage, h_stage, (size_t)n_faces * dim * sizeof(double),
+                                cudaMemcpyHostToDevice, stream));
+    src = d_stage;
+  }
+  if (precision == SPLASH_PREC_MIXED) {
+    SPLASH_CUDA(mixed_scatter_prepare(src, d_iperm, GM, S, P, dim, stream));
     return SPLASH_OK;
   }
-  std::memcpy(h_stage, U_ref, (size_t)n_faces * dim * sizeof(double));
-  SPLASH_CUDA(cudaMemcpyAsync(d_stage, h_stage, (size_t)n_faces * dim * sizeof(double),
-                              cudaMemcpyHostToDevice, stream));
-  SPLASH_CUDA(fp64_scatter_state(d_stage, d_iperm, S.U, n_faces, fpad, stream, dim));
+  SPLASH_CUDA(fp64_scatter_state(src, d_iperm, S.U, n_faces, fpad, stream, dim));
   SPLASH_CUDA(launch_prepare());
   return SPLASH_OK;
 }

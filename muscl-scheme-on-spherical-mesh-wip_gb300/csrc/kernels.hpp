@@ -40,6 +40,11 @@ cudaError_t mixed_prepare(const DevGeomMixed& G, const DevState& S, const PhysPa
 cudaError_t mixed_step(const DevGeomMixed& G, const DevState& S, const PhysParams& P, double dt0,
                        cudaStream_t st, cudaEvent_t* ev = nullptr, bool per_launch = false);
 const void* mixed_finalize_kernel_ptr();
+// set_state + prepare in one pass: aos is the caller's [n_faces][dim] array
+// in reference order (host memory the device can access, or device memory),
+// iperm maps reference to internal face indices.
+cudaError_t mixed_scatter_prepare(const double* aos, const int* iperm, const DevGeomMixed& G, const DevState& S,
+                                  const PhysParams& P, int dim, cudaStream_t st);
 int mixed_partial_blocks(int n_faces);
 
 // ---- ensemble (step_mixed.cu): batched launches over instances ----

@@ -271,6 +271,28 @@ __global__ void gather_state_kernel(const double* __restrict__ U, const int* __r
   const int r = (int)(e / dim), k = (int)(e % dim);
   aos[e] = U[(size_t)k * fpad + iperm[r]];
 }
+// Two consecutive elements per thread with one 16-byte access on the
+// caller's side (used when the caller's array is 16-byte aligned): half the
+// warp instructions on the host link, 512 contiguous bytes per warp access.
+__global__ void gather_state2_kernel(const double* __restrict__ U, const int* __restrict__ iperm,
+                                     double* __restrict__ aos, int n_faces, int fpad, int dim) {
+  const unsigned ne = (unsigned)n_faces * (unsigned)dim;
+  const unsigned e0 = 2u * (blockIdx.x * blockDim.x + threadIdx.x);
+  if (e0 >= ne) return;
+  double v[2] = {0.0, 0.0};
+#pragma unroll
+  for (unsigned q = 0; q < 2; ++q) {
+    const unsigned e = e0 + q;
+    if (e < ne) {
+      const unsigned r = e / (unsigned)dim, k = e - r * (unsigned)dim;
+      v[q] = U[(size_t)k * fpad + iperm[r]];
+    }
+  }
+  if (e0 + 1 < ne)
+    *reinterpret_cast<double2*>(aos + e0) = make_double2(v[0], v[1]);
+  else
+    aos[e0] = v[0];
+}
 constexpr int kMoveBlock = 256;
 
 inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
@@ -339,6 +361,12 @@ cudaError_t fp64_scatter_state(const double* aos, const int* iperm, double* U, i
 cudaError_t fp64_gather_state(const double* U, const int* iperm, double* aos, int n_faces,
                               int fpad, cudaStream_t st, int dim) {
   const size_t ne = (size_t)n_faces * dim;
+  if (((uintptr_t)aos & 15) == 0) {
+    const size_t nt = (ne + 1) / 2;
+    f64::gather_state2_kernel<<<(unsigned)((nt + f64::kMoveBlock - 1) / f64::kMoveBlock), f64::kMoveBlock, 0, st>>>(
+        U, iperm, aos, n_faces, fpad, dim);
+    return cudaGetLastError();
+  }
   f64::gather_state_kernel<<<(unsigned)((ne + f64::kMoveBlock - 1) / f64::kMoveBlock), f64::kMoveBlock, 0, st>>>(
       U, iperm, aos, n_faces, fpad, dim);
   return cudaGetLastError();

@@ -259,6 +259,20 @@ __device__ __forceinline__ void iso_w32_candidates(const double* u, f64::D3 r, f
   dmin = kNoExtraSq;
 }
 
+// W32 and the dt candidates of the state u of internal face f
+__device__ __forceinline__ void prepare_face(const DevGeomMixed& G, const DevState& S, const PhysParams& P, int f,
+                                             const double* u, double& vmax, double& dmin) {
+  const f64::D3 r = plane3d(G.fcn, G.fpad, f);
+  if (P.solver == kSolverIsoHLLE) {
+    iso_w32_candidates(u, r, S.W32, G.fpad, f, vmax, dmin);
+  } else {
+    double v2, inv_rho;
+    const double p = pressure_recover(u, r, P.gam_m1, v2, inv_rho);
+    store_w32(S.W32, G.fpad, f, u, p);
+    dt_candidates_sq(u, r, p, v2, inv_rho, P, vmax, dmin);
+  }
+}
+
 // W32 and the dt candidates of the current U for face f (all 32 lanes of a
 // warp call it; lanes past the last face contribute neutral values).
 __device__ __forceinline__ void prepare_body(const DevGeomMixed& G, const DevState& S,
@@ -268,21 +282,54 @@ __device__ __forceinline__ void prepare_body(const DevGeomMixed& G, const DevSta
     double u[kDim];
 #pragma unroll
     for (int k = 0; k < kDim; ++k) u[k] = S.U[k * G.fpad + f];
-    const f64::D3 r = plane3d(G.fcn, G.fpad, f);
-    if (P.solver == kSolverIsoHLLE) {
-      iso_w32_candidates(u, r, S.W32, G.fpad, f, vmax, dmin);
-    } else {
-      double v2, inv_rho;
-      const double p = pressure_recover(u, r, P.gam_m1, v2, inv_rho);
-      store_w32(S.W32, G.fpad, f, u, p);
-      dt_candidates_sq(u, r, p, v2, inv_rho, P, vmax, dmin);
-    }
+    prepare_face(G, S, P, f, u, vmax, dmin);
   }
   fold_candidates(vmax, dmin, S.keys);
 }
 
 __global__ void __launch_bounds__(128) prepare_kernel(DevGeomMixed G, DevState S, PhysParams P) {
   prepare_body(G, S, P, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// set_state of the mixed path in one pass: the block stages the caller's
+// rows of kBlock consecutive reference faces (contiguous in the caller's
+// [F][dim] array, possibly host memory read over the coherent link) through
+// shared memory with one element per thread and load, so every warp load
+// covers 256 contiguous bytes; then each thread stores its face's FP64
+// state at the face's internal index and computes its W32 and dt candidates
+// from registers (no second pass over U).
+template <bool VEC>
+__global__ void __launch_bounds__(kBlock) scatter_prepare_kernel(const double* __restrict__ aos,
+                                                                 const int* __restrict__ iperm, DevGeomMixed G,
+                                                                 DevState S, PhysParams P, int dim) {
+  __shared__ __align__(16) double rows[kBlock * kDim];
+  const int r0 = blockIdx.x * kBlock;
+  const int nr = min(kBlock, G.n_faces - r0);
+  const int ne = nr * dim;
+  const double* src = aos + (size_t)r0 * dim;
+  if (VEC) {
+    // 16-byte accesses (the array and every block's first row are 16-byte
+    // aligned: r0 * dim * 8 is a multiple of 16)
+    for (int k = 2 * threadIdx.x; k + 1 < ne; k += 2 * kBlock)
+      *reinterpret_cast<double2*>(rows + k) = *reinterpret_cast<const double2*>(src + k);
+    if ((ne & 1) && threadIdx.x == 0) rows[ne - 1] = src[ne - 1];
+  } else {
+    for (int k = threadIdx.x; k < ne; k += kBlock) rows[k] = src[k];
+  }
+  __syncthreads();
+  double vmax = 0.0, dmin = kNoExtraSq;
+  const int t = threadIdx.x;
+  if (t < nr) {
+    const int f = iperm[r0 + t];
+    double u[kDim];
+#pragma unroll
+    for (int k = 0; k < kDim; ++k) {
+      u[k] = (k < dim) ? rows[t * dim + k] : 0.0;
+      S.U[(size_t)k * G.fpad + f] = u[k];
+    }
+    prepare_face(G, S, P, f, u, vmax, dmin);
+  }
+  fold_candidates(vmax, dmin, S.keys);
 }
 
 // initial keys: max |v|^2 starts at (1e-8)^2 and min extra dt at 1e20 (as
@@ -614,6 +661,16 @@ cudaError_t mixed_prepare(const DevGeomMixed& G, const DevState& S, const PhysPa
                           cudaStream_t st) {
   mx::reset_keys_kernel<<<1, 1, 0, st>>>(S.keys);
   mx::prepare_kernel<<<(G.n_faces + 127) / 128, 128, 0, st>>>(G, S, P);
+  return cudaGetLastError();
+}
+
+cudaError_t mixed_scatter_prepare(const double* aos, const int* iperm, const DevGeomMixed& G, const DevState& S,
+                                  const PhysParams& P, int dim, cudaStream_t st) {
+  mx::reset_keys_kernel<<<1, 1, 0, st>>>(S.keys);
+  if (((uintptr_t)aos & 15) == 0)
+    mx::scatter_prepare_kernel<true><<<mx::blocks_for(G.n_faces), mx::kBlock, 0, st>>>(aos, iperm, G, S, P, dim);
+  else
+    mx::scatter_prepare_kernel<false><<<mx::blocks_for(G.n_faces), mx::kBlock, 0, st>>>(aos, iperm, G, S, P, dim);
   return cudaGetLastError();
 }
 
