@@ -177,9 +177,50 @@ def cpu_baseline(geom, U0, gam, budget_s=15.0):
         if time.perf_counter() - t0 > budget_s:
             break
     dt = time.perf_counter() - t0
+    # one thread, a shorter sample of the same state
+    o1 = Oracle(geom, U0, gam, 0.0, True, sg.SolverParams(**PARAMS).as_list(), 3, threads=1)
+    t1 = time.perf_counter()
+    n1 = 0
+    while n1 < 10:
+        o1.do_step(DT0)
+        n1 += 1
+        if time.perf_counter() - t1 > budget_s / 3:
+            break
+    dt1 = time.perf_counter() - t1
     return {"value": geom.n_faces * n / dt, "unit": METRIC, "cores": cores, "kind": "port",
             "sample": f"{n} do_step calls of the full workload after 1 warm-up "
-                      f"({dt:.1f} s, OpenMP {cores} threads, {platform.machine()})"}
+                      f"({dt:.1f} s, OpenMP {cores} threads, {platform.machine()})",
+            "value_1_thread": geom.n_faces * n1 / dt1, "sample_1_thread": f"{n1} do_step calls ({dt1:.1f} s)",
+            "cpu_model": cpu_model()}
+
+
+def cpu_model() -> str:
+    """The host CPU's model name (or its architecture when none is listed)."""
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            key = line.split(":")[0].strip().lower()
+            if key in ("model name", "cpu model", "hardware"):
+                return line.split(":", 1)[1].strip()
+        parts = [line.split(":", 1)[1].strip() for line in Path("/proc/cpuinfo").read_text().splitlines()
+                 if line.lower().startswith(("cpu implementer", "cpu part"))][:2]
+        if parts:
+            return f"{platform.machine()} implementer {parts[0]} part {parts[1] if len(parts) > 1 else '?'}"
+    except OSError:
+        pass
+    return platform.machine()
+
+
+def step_bytes_mixed(geom) -> float:
+    """Compulsory bytes of one mixed-precision step by the per-mesh formula
+    bytes/step = 2 (b_slot S + b_edge E + b_face F) + 5 dim 8 F with the
+    FP32-geometry sizes b_slot = 44 (4 stencil ids, 4 weights, H+, H-,
+    BM_dist), b_edge = 36 (normal, centre, length, 2 face ids), b_face = 20
+    (FP64 area, FP32 unit centre): the minimal data set, once per stage, and
+    the five FP64 state accesses of a step."""
+    F = geom.n_faces
+    S = geom.n_slots
+    E = S // 2
+    return 2 * (44 * S + 36 * E + 20 * F) + 5 * 5 * 8 * F
 
 
 def algorithmic_bytes_mixed(geom, kernel: str) -> float:
@@ -467,6 +508,10 @@ def run_ours(args):
                      "algorithmic_bytes": algorithmic_bytes_mixed(geom, dom),
                      "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)",
                      "kernel_ms": kern, "kernel_ms_per_step": per_step},
+        "roofline_step": {"bound": "hbm", "bytes_per_step": step_bytes_mixed(geom),
+                          "bytes_per_face_update": step_bytes_mixed(geom) / F,
+                          "achieved": step_bytes_mixed(geom) / (secs / args.steps) / 1e9, "peak": hbm,
+                          "unit": "GB/s", "frac": step_bytes_mixed(geom) / (secs / args.steps) / 1e9 / hbm},
         "clocks": clk,
     }
     mixed.close()

@@ -83,6 +83,8 @@ Solver::~Solver() {
   if (device >= 0) cudaSetDevice(device);
   if (graph_exec) cudaGraphExecDestroy(graph_exec);
   if (graph) cudaGraphDestroy(graph);
+  if (graph_k_exec) cudaGraphExecDestroy(graph_k_exec);
+  if (graph_k) cudaGraphDestroy(graph_k);
   for (void* p : dev_allocs) cudaFree(p);
   if (h_stage) cudaFreeHost(h_stage);
   if (h_diag) cudaFreeHost(h_diag);
@@ -340,28 +342,84 @@ int Solver::capture_graph() {
       if (kp.func == mixed_finalize_kernel_ptr()) dt0_node = nd;
     }
     if (!dt0_node) return fail(SPLASH_E_CUDA, "dt node not found in the captured step");
+    // the same step kGraphSteps times in one graph
+    SPLASH_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t lk = cudaSuccess;
+    for (int k = 0; k < kGraphSteps && lk == cudaSuccess; ++k)
+      lk = mixed_step(GM, S, P, graph_dt0, stream, nullptr);
+    cudaGraph_t gk = nullptr;
+    cudaError_t ck = cudaStreamEndCapture(stream, &gk);
+    if (lk != cudaSuccess) {
+      if (gk) cudaGraphDestroy(gk);
+      return fail(SPLASH_E_CUDA, "step launch during capture: %s", cudaGetErrorString(lk));
+    }
+    SPLASH_CUDA(ck);
+    graph_k = gk;
+    SPLASH_CUDA(cudaGraphInstantiate(&graph_k_exec, graph_k, 0));
+    SPLASH_CUDA(cudaGraphGetNodes(graph_k, nullptr, &n));
+    nodes.resize(n);
+    SPLASH_CUDA(cudaGraphGetNodes(graph_k, nodes.data(), &n));
+    dt0_nodes_k.clear();
+    for (cudaGraphNode_t nd : nodes) {
+      cudaGraphNodeType t;
+      SPLASH_CUDA(cudaGraphNodeGetType(nd, &t));
+      if (t != cudaGraphNodeTypeKernel) continue;
+      cudaKernelNodeParams kp{};
+      SPLASH_CUDA(cudaGraphKernelNodeGetParams(nd, &kp));
+      if (kp.func == mixed_finalize_kernel_ptr()) dt0_nodes_k.push_back(nd);
+    }
+    if ((int)dt0_nodes_k.size() != kGraphSteps)
+      return fail(SPLASH_E_CUDA, "dt nodes not found in the captured steps");
   }
+  return SPLASH_OK;
+}
+
+int Solver::set_graph_dt0(double dt0) {
+  if (dt0 == graph_dt0) return SPLASH_OK;
+  // new dt0: rewrite the finalize nodes' arguments in the instantiated
+  // graphs (takes effect from the next launch; launches in flight keep theirs)
+  cudaKernelNodeParams kp{};
+  SPLASH_CUDA(cudaGraphKernelNodeGetParams(dt0_node, &kp));
+  void* args[] = {&S, &P, &dt0};
+  kp.kernelParams = args;
+  kp.extra = nullptr;
+  SPLASH_CUDA(cudaGraphExecKernelNodeSetParams(graph_exec, dt0_node, &kp));
+  for (cudaGraphNode_t nd : dt0_nodes_k) SPLASH_CUDA(cudaGraphExecKernelNodeSetParams(graph_k_exec, nd, &kp));
+  graph_dt0 = dt0;
   return SPLASH_OK;
 }
 
 int Solver::step(double dt0) {
   if (precision == SPLASH_PREC_MIXED) {
-    if (dt0 != graph_dt0) {
-      // new dt0: rewrite the finalize node's arguments in the instantiated
-      // graph (takes effect from the next launch; launches in flight keep theirs)
-      cudaKernelNodeParams kp{};
-      SPLASH_CUDA(cudaGraphKernelNodeGetParams(dt0_node, &kp));
-      void* args[] = {&S, &P, &dt0};
-      kp.kernelParams = args;
-      kp.extra = nullptr;
-      SPLASH_CUDA(cudaGraphExecKernelNodeSetParams(graph_exec, dt0_node, &kp));
-      graph_dt0 = dt0;
-    }
+    const int rc = set_graph_dt0(dt0);
+    if (rc) return rc;
   } else {
     SPLASH_CUDA(fp64_set_dt0(S, dt0, stream));
   }
   SPLASH_CUDA(cudaGraphLaunch(graph_exec, stream));
   ++steps;
+  return SPLASH_OK;
+}
+
+int Solver::steps_n(int n, double dt0) {
+  if (precision != SPLASH_PREC_MIXED || !graph_k_exec) {
+    for (int i = 0; i < n; ++i) {
+      const int rc = step(dt0);
+      if (rc) return rc;
+    }
+    return SPLASH_OK;
+  }
+  const int rc = set_graph_dt0(dt0);
+  if (rc) return rc;
+  int left = n;
+  for (; left >= kGraphSteps; left -= kGraphSteps) {
+    SPLASH_CUDA(cudaGraphLaunch(graph_k_exec, stream));
+    steps += kGraphSteps;
+  }
+  for (; left > 0; --left) {
+    SPLASH_CUDA(cudaGraphLaunch(graph_exec, stream));
+    ++steps;
+  }
   return SPLASH_OK;
 }
 
@@ -520,11 +578,7 @@ int splash_do_step(splash_solver* h, double dt0) {
 int splash_do_steps(splash_solver* h, int n, double dt0) {
   GET_SOLVER(h);
   if (n < 0) return fail(SPLASH_E_INVALID, "n < 0");
-  for (int i = 0; i < n; ++i) {
-    const int rc = s->step(dt0);
-    if (rc) return rc;
-  }
-  return SPLASH_OK;
+  return s->steps_n(n, dt0);
 }
 
 int splash_stream(splash_solver* h, void** stream) {

@@ -67,7 +67,14 @@ struct Solver {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   cudaGraphNode_t dt0_node = nullptr;  // mixed path: the finalize node taking dt0
-  double graph_dt0 = 0.0;              // dt0 the instantiated graph currently uses
+  double graph_dt0 = 0.0;              // dt0 the instantiated graphs currently use
+  // mixed path: kGraphSteps consecutive steps in one graph, so that each
+  // step's first launch overlaps the previous step's last one (programmatic
+  // dependent launch works within a graph, not across graph launches)
+  static constexpr int kGraphSteps = 4;
+  cudaGraph_t graph_k = nullptr;
+  cudaGraphExec_t graph_k_exec = nullptr;
+  std::vector<cudaGraphNode_t> dt0_nodes_k;
   int64_t steps = 0;
 
   ~Solver();
@@ -82,6 +89,8 @@ struct Solver {
   int download_state(double* U_ref);
   int read_scalars(double* out);
   int capture_graph();
+  int set_graph_dt0(double dt0);  // mixed path: rewrite dt0 in the instantiated graphs
+  int steps_n(int n, double dt0);  // n steps (K-step graphs where they fit)
   int step(double dt0);
   // one un-captured step; ev as for mixed_step (the FP64 step has five
   // launches, so its two layouts coincide)

@@ -150,3 +150,29 @@ def test_mixed_edge_state_writer_matches_fp64(tmp_path, solver):
     scale = np.max(np.abs(a[1:]))
     assert scale > 0
     assert np.max(np.abs(a[1:] - b[1:])) < 1e-4 * scale
+
+
+def test_multi_step_graphs_equal_single_steps():
+    """do_steps(n) replays graphs of several steps (each step's first launch
+    overlapping the previous step's last); the result must equal n single
+    do_step calls bit for bit, across a change of dt0 between calls."""
+    import splash_gb300 as sg
+
+    mesh = mesh_of("hex", 4)
+    g = sg.Geometry(mesh)
+    gam = sg.initial_conditions.gam2d(4 / 3)
+    U0 = sg.initial_conditions.rotating_blob(g.unit_face_centers(), gam, seed=8)
+    params = sg.SolverParams(accretion_rate=1e-2, e_acc=0.5, omega_acc_abs=0.5, tilt_angle=0.2,
+                             acc_width=0.1, alpha=1e-6, friction_on=True)
+    a = sg.Solver(mesh, U0, 5, gam, 0.0, True, params=params, solver=3, precision=sg.PREC_MIXED)
+    b = sg.Solver(mesh, U0, 5, gam, 0.0, True, params=params, solver=3, precision=sg.PREC_MIXED)
+    a.do_steps(11, 1e-3)
+    a.do_steps(6, 5e-4)
+    for _ in range(11):
+        b.do_step(1e-3)
+    for _ in range(6):
+        b.do_step(5e-4)
+    assert np.array_equal(a.get_state(), b.get_state())
+    assert a.time() == b.time() and a.last_dt() == b.last_dt()
+    a.close()
+    b.close()
