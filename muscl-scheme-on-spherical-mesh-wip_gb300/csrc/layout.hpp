@@ -42,7 +42,7 @@ struct PhysParams {
   // (physics/adiabatic.hpp:563-566), and FP32 copies for the mixed path
   double fric_k;
   double gam_m1, fric_ak;  // gam - 1 and alpha * fric_k (mixed-path update)
-  float gam_f, e_acc_f, alpha_f, omega_ns_f;
+  float gam_f, e_acc_f, alpha_f, omega_ns_f, fric_ak_f;
   float omega_acc_f[3];
   float depletion_f;     // -(acc_rate 4 pi) / total_mass (adiabatic.hpp:430-436)
 };
@@ -53,6 +53,7 @@ inline void derive_params(PhysParams& P) {
   P.fric_k = gam3d / (2 * gam3d - 1);
   P.gam_m1 = P.gam - 1.0;
   P.fric_ak = P.alpha * P.fric_k;
+  P.fric_ak_f = (float)P.fric_ak;
   P.gam_f = (float)P.gam;
   P.e_acc_f = (float)P.e_acc;
   P.alpha_f = (float)P.alpha;

@@ -144,36 +144,45 @@ __device__ __forceinline__ double pressure_recover(const double* u, f64::D3 r, d
   return (1e-16 < p) ? p : 1e-16;
 }
 
-__device__ __forceinline__ void store_w32(float* W32, int fp, int f, const double* u, double p) {
-  const float v[kDim] = {fpc::d2f(u[0]), fpc::d2f(u[1]), fpc::d2f(u[2]), fpc::d2f(u[3]), fpc::d2f(p)};
+// stores the FP32 face state (Sigma, l, Pi) of u and pressure p, returned in v
+__device__ __forceinline__ void store_w32(float* W32, int fp, int f, const double* u, double p, float* v) {
+  v[0] = fpc::d2f(u[0]);
+  v[1] = fpc::d2f(u[1]);
+  v[2] = fpc::d2f(u[2]);
+  v[3] = fpc::d2f(u[3]);
+  v[4] = fpc::d2f(p);
   st5(W32, fp, f, v);
 }
 
-// dt candidates in FP64 without a square root or a division per face.
-// The CFL maximum is reduced over squared speeds max(|v|^2, gam p / Sigma).
-// extra_dt_constr (physics/adiabatic.hpp:543-580) simplifies to
-// d = A / (B |v - v0|) with A = 0.01 p, B = alpha k g_eff Sigma and
-// k = gam3d / (2 gam3d - 1); it is reduced as the signed square
-// sgn(d) d^2 = sgn(B) A^2 / (B^2 |v - v0|^2), which orders like d (x |x| is
-// increasing), so the finalize takes one square root of the minimum.  The
-// sign comes from B's sign bit, so the zero-denominator cases give the
-// infinities of the direct quotient with their signs.  Both square roots are
-// exact up to rounding; the candidates are compared, not accumulated.
-__device__ __forceinline__ void dt_candidates_sq(const double* u, f64::D3 r, double p, double v2,
-                                                 double inv_rho, const PhysParams& P, double& vmax2,
-                                                 double& dmin_sq) {
-  vmax2 = fmax(v2, P.gam * p * inv_rho);
-  const f64::D3 c = f64::cross3(r, f64::d3(u[1], u[2], u[3]));
+// dt candidates in FP32 from the FP32 face state w = (Sigma, l, Pi) (the
+// FP64 state and pressure rounded once) and the FP32 unit centre r: the CFL
+// maximum over squared speeds max(|v|^2, gam Pi / Sigma), and
+// extra_dt_constr (physics/adiabatic.hpp:543-580), d = A / (B |v - v0|) with
+// A = 0.01 Pi, B = alpha k g_eff Sigma, k = gam3d / (2 gam3d - 1), reduced as
+// the signed square sgn(B) A^2 / (B^2 |v - v0|^2) (x |x| is increasing, so
+// the minimum is the same; the finalize takes one square root).  The sign
+// comes from B's sign bit, so zero denominators give the direct quotient's
+// signed infinities; a bound past the FP32 range (d above ~1.8e19) reads as
+// no bound, like the initial 1e20.  Both candidates carry FP32 rounding
+// (~1e-7 relative), so the mixed path's dt follows the FP64 path's to that
+// level when the clip is active.  Returned as doubles for the keys.
+__device__ __forceinline__ void dt_candidates_f32(const float* w, F3 r, const PhysParams& P, double& vmax2,
+                                                  double& dmin_sq) {
+  const float ir = 1.0f / w[0];
+  const F3 c = cross3(r, f3(w[1], w[2], w[3]));
+  const float v2 = dot3(c, c) * (ir * ir);
+  const float vm = fmaxf(v2, P.gam_f * w[4] * ir);
   // v = (r x l) / (-Sigma) ; v0 = omega_ns z x r
-  const double vx = -c.x * inv_rho + P.omega_ns * r.y;
-  const double vy = -c.y * inv_rho - P.omega_ns * r.x;
-  const double vz = -c.z * inv_rho;
-  const double d2 = vx * vx + vy * vy + vz * vz;
-  const double g_eff = 0.217909 - v2;
-  const double A = 0.01 * p;
-  const double B = P.fric_ak * g_eff * u[0];
-  const double q = (A * A) * recip_nr((B * B) * d2);
-  dmin_sq = signbit(B) ? -q : q;
+  const float vx = -c.x * ir + P.omega_ns_f * r.y;
+  const float vy = -c.y * ir - P.omega_ns_f * r.x;
+  const float vz = -c.z * ir;
+  const float d2 = vx * vx + vy * vy + vz * vz;
+  const float g_eff = 0.217909f - v2;
+  const float A = 0.01f * w[4];
+  const float B = P.fric_ak_f * g_eff * w[0];
+  const float q = (A * A) / ((B * B) * d2);
+  vmax2 = fpc::f2d(vm);
+  dmin_sq = fpc::f2d(signbit(B) ? -q : q);
 }
 
 // physics/adiabatic.hpp:396-541 in FP32, except the accretion mass source
@@ -248,28 +257,29 @@ __device__ __forceinline__ void source_f32(const float* w, F3 fcn, float acc0, c
 // Isothermal state (4 fields): W32 is the state itself (field 4 unused) and
 // the CFL candidate is max(|v|^2, a^2) with a = 1 (find_v_max with the
 // isothermal sound speed); no extra constraint (isothermal.hpp:262-267).
-__device__ __forceinline__ void iso_w32_candidates(const double* u, f64::D3 r, float* W32, int fp, int f,
+__device__ __forceinline__ void iso_w32_candidates(const double* u, F3 r, float* W32, int fp, int f,
                                                    double& vmax2, double& dmin) {
   const float v[kDim] = {fpc::d2f(u[0]), fpc::d2f(u[1]), fpc::d2f(u[2]), fpc::d2f(u[3]), 0.f};
   st5(W32, fp, f, v);
-  const f64::D3 c = f64::cross3(r, f64::d3(u[1], u[2], u[3]));
-  const double inv_rho = recip_nr(u[0]);
-  const double v2 = (c.x * c.x + c.y * c.y + c.z * c.z) * inv_rho * inv_rho;
-  vmax2 = fmax(v2, 1.0);
+  const float ir = 1.0f / v[0];
+  const F3 c = cross3(r, f3(v[1], v[2], v[3]));
+  vmax2 = fpc::f2d(fmaxf(dot3(c, c) * (ir * ir), 1.f));
   dmin = kNoExtraSq;
 }
 
 // W32 and the dt candidates of the state u of internal face f
 __device__ __forceinline__ void prepare_face(const DevGeomMixed& G, const DevState& S, const PhysParams& P, int f,
                                              const double* u, double& vmax, double& dmin) {
-  const f64::D3 r = plane3d(G.fcn, G.fpad, f);
+  const F3 r32 = plane3f(G.fcn32, G.fpad, f);
   if (P.solver == kSolverIsoHLLE) {
-    iso_w32_candidates(u, r, S.W32, G.fpad, f, vmax, dmin);
+    iso_w32_candidates(u, r32, S.W32, G.fpad, f, vmax, dmin);
   } else {
+    const f64::D3 r = plane3d(G.fcn, G.fpad, f);
     double v2, inv_rho;
     const double p = pressure_recover(u, r, P.gam_m1, v2, inv_rho);
-    store_w32(S.W32, G.fpad, f, u, p);
-    dt_candidates_sq(u, r, p, v2, inv_rho, P, vmax, dmin);
+    float w[kDim];
+    store_w32(S.W32, G.fpad, f, u, p, w);
+    dt_candidates_f32(w, r32, P, vmax, dmin);
   }
 }
 
@@ -568,7 +578,7 @@ __device__ __forceinline__ void update_body(const DevGeomMixed& G, const DevStat
     if (P.solver == kSolverIsoHLLE) {
       u[4] = 0.0;
       double vm, dm;
-      iso_w32_candidates(u, r, S.W32, fp, f, vm, dm);
+      iso_w32_candidates(u, fcn32, S.W32, fp, f, vm, dm);
       if (STAGE == 2) {
 #pragma unroll
         for (int k = 0; k < kDim; ++k) S.U[k * fp + f] = u[k];
@@ -578,11 +588,12 @@ __device__ __forceinline__ void update_body(const DevGeomMixed& G, const DevStat
     } else {
       double v2, inv_rho;
       const double p = pressure_recover(u, r, P.gam_m1, v2, inv_rho);
-      store_w32(S.W32, fp, f, u, p);
+      float w32[kDim];
+      store_w32(S.W32, fp, f, u, p, w32);
       if (STAGE == 2) {
 #pragma unroll
         for (int k = 0; k < kDim; ++k) S.U[k * fp + f] = u[k];
-        dt_candidates_sq(u, r, p, v2, inv_rho, P, vmax, dmin);
+        dt_candidates_f32(w32, fcn32, P, vmax, dmin);
       }
     }
   }
