@@ -224,9 +224,13 @@ __device__ __forceinline__ unsigned iso_flux_star(const float* uL, const float* 
 
 // isothermal limiter (physics/isothermal.hpp:269-320, etha_minus taken as
 // H_minus / BM_dist) for one field; sb_scale = 2 eta / (2 N nu_plus)
+// After the NaN test no operand of the min/max below is NaN except
+// r * sb_scale (0 * inf, inf * 0), where smin(1, NaN) and fminf(1, NaN) both
+// give 1; so the hardware min/max (one instruction) equals the reference's
+// compare-and-select form.
 __device__ __forceinline__ float iso_limiter_field(float r, float eta, float sb_scale) {
   if (isnan(r)) return 0.f;
-  return smax(0.f, smax(smin(1.f, r * sb_scale), smin(r, eta)));
+  return fmaxf(0.f, fmaxf(fminf(1.f, r * sb_scale), fminf(r, eta)));
 }
 
 // h(r) switch and the blended limiter (physics/adiabatic.hpp:685-828).
@@ -248,10 +252,12 @@ __device__ __forceinline__ float limiter_switch(float r) {
   return lo ? 2.f * q : (hi ? t2 * t2 * t2 : 0.f);
 }
 
+// min/max as in iso_limiter_field: after the NaN test, smin(1, NaN) and
+// fminf(1, NaN) agree, and smin(sb, NaN) = fminf(sb, NaN) = sb.
 __device__ __forceinline__ float limiter_field(float r, float nu_plus, float eta_p, float sb_scale) {
   if (isnan(r)) return 0.f;
-  const float sb = smax(0.f, smax(smin(1.f, r * sb_scale), smin(r, eta_p)));
-  const float to = smax(0.f, smin(sb, 1.f + (1.f + nu_plus) * (1.f / 3.f) * (r - 1.f)));
+  const float sb = fmaxf(0.f, fmaxf(fminf(1.f, r * sb_scale), fminf(r, eta_p)));
+  const float to = fmaxf(0.f, fminf(sb, 1.f + (1.f + nu_plus) * (1.f / 3.f) * (r - 1.f)));
   const float hv = limiter_switch(r);
   return (1.f - hv) * to + hv * sb;
 }
