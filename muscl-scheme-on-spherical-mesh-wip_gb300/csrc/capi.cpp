@@ -264,9 +264,9 @@ int Solver::run_diagnostics(double* out9) {
   return SPLASH_OK;
 }
 
-cudaError_t Solver::launch_prepare() {
-  return precision == SPLASH_PREC_MIXED ? mixed_prepare(GM, S, P, stream) : fp64_prepare(G, S, P, stream);
-}
+// FP64 path: W and the dt partial records of the current U (the mixed path
+// computes its face states and dt keys in the set_state pass)
+cudaError_t Solver::launch_prepare() { return fp64_prepare(G, S, P, stream); }
 
 cudaError_t Solver::launch_step(cudaEvent_t* ev, double dt0, bool per_launch) {
   if (precision == SPLASH_PREC_MIXED) return mixed_step(GM, S, P, dt0, stream, ev, per_launch);
@@ -506,8 +506,6 @@ int splash_create(const splash_mesh_desc* mesh, const double* U_in, int dim, dou
     const size_t PS = (size_t)s->max_slots * fp;
     splash::DevState& S = s->S;
     S.U = s->dalloc<double>(splash::kDim * fp);
-    S.W0 = s->dalloc<double>(splash::kDim * fp);
-    S.W1 = s->dalloc<double>(splash::kDim * fp);
     if (precision == SPLASH_PREC_MIXED) {
       S.W32 = s->dalloc<float>(splash::kDim * fp);
       S.uplus32 = s->dalloc<float>(splash::kDim * 2 * (size_t)s->GM.epad);
@@ -515,13 +513,17 @@ int splash_create(const splash_mesh_desc* mesh, const double* U_in, int dim, dou
       S.uplus = nullptr;
       SPLASH_CUDA(cudaMemset(S.W32, 0, splash::kDim * fp * sizeof(float)));
       SPLASH_CUDA(cudaMemset(S.uplus32, 0, splash::kDim * 2 * (size_t)s->GM.epad * sizeof(float)));
-      s->n_partials = splash::mixed_partial_blocks(s->n_faces);
+      s->n_partials = 0;  // the mixed path reduces the dt candidates as keys
     } else {
+      S.W0 = s->dalloc<double>(splash::kDim * fp);
+      S.W1 = s->dalloc<double>(splash::kDim * fp);
+      SPLASH_CUDA(cudaMemset(S.W0, 0, splash::kDim * fp * sizeof(double)));
+      SPLASH_CUDA(cudaMemset(S.W1, 0, splash::kDim * fp * sizeof(double)));
       S.uplus = s->dalloc<double>(splash::kDim * PS);
       SPLASH_CUDA(cudaMemset(S.uplus, 0, splash::kDim * PS * sizeof(double)));
       s->n_partials = splash::fp64_partial_blocks(s->n_faces);
+      S.partial = s->dalloc<double>((size_t)s->n_partials * splash::kPartialStride);
     }
-    S.partial = s->dalloc<double>((size_t)s->n_partials * splash::kPartialStride);
     S.scal = s->dalloc<double>(splash::kScCount);
     S.err = s->dalloc<unsigned int>(4);
     S.keys = s->dalloc<unsigned long long>(2);
@@ -540,8 +542,6 @@ int splash_create(const splash_mesh_desc* mesh, const double* U_in, int dim, dou
         s->host_direct = pma != 0 && std::getenv("SPLASH_STAGED_TRANSFERS") == nullptr;
     }
     SPLASH_CUDA(cudaMemset(S.U, 0, splash::kDim * fp * sizeof(double)));
-    SPLASH_CUDA(cudaMemset(S.W0, 0, splash::kDim * fp * sizeof(double)));
-    SPLASH_CUDA(cudaMemset(S.W1, 0, splash::kDim * fp * sizeof(double)));
     SPLASH_CUDA(cudaMemset(S.scal, 0, splash::kScCount * sizeof(double)));
     SPLASH_CUDA(cudaMemset(S.err, 0, 4 * sizeof(unsigned int)));
     SPLASH_CUDA(cudaMallocHost(&s->h_stage, (size_t)s->n_faces * dim * sizeof(double)));
@@ -649,9 +649,8 @@ int splash_memory(splash_solver* h, int64_t out[2]) {
   if (!s || !out) return fail(SPLASH_E_INVALID, "NULL argument");
   const size_t fp = (size_t)s->fpad, PS = (size_t)s->max_slots * fp;
   out[0] = (int64_t)s->geometry_bytes;
-  if (s->precision == SPLASH_PREC_MIXED)
-    out[1] = (int64_t)(8 * splash::kDim * fp + 4 * (splash::kDim * fp + splash::kDim * PS) +
-                       8 * (size_t)s->n_partials * splash::kPartialStride);
+  if (s->precision == SPLASH_PREC_MIXED)  // U; W32; edge states (2 per edge); edge fluxes
+    out[1] = (int64_t)(8 * splash::kDim * fp + 4 * splash::kDim * (fp + 3 * (size_t)s->GM.epad));
   else
     out[1] = (int64_t)(8 * (3 * splash::kDim * fp + splash::kDim * PS) +
                        8 * (size_t)s->n_partials * splash::kPartialStride);

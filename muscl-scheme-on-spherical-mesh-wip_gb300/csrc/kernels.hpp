@@ -29,8 +29,6 @@ cudaError_t fp64_gather_state(const double* U, const int* iperm, double* aos, in
                               cudaStream_t st, int dim = kDim);
 
 // ---- FP32/FP64 mixed path (step_mixed.cu) ----
-cudaError_t mixed_prepare(const DevGeomMixed& G, const DevState& S, const PhysParams& P,
-                          cudaStream_t st);
 // One do_step: the dt finalize (1 thread, argument dt0) then the four
 // stage launches.  Capturable; the finalize node's dt0 can be updated in an
 // instantiated graph (mixed_finalize_kernel_ptr identifies the node).
@@ -45,7 +43,6 @@ const void* mixed_finalize_kernel_ptr();
 // iperm maps reference to internal face indices.
 cudaError_t mixed_scatter_prepare(const double* aos, const int* iperm, const DevGeomMixed& G, const DevState& S,
                                   const PhysParams& P, int dim, cudaStream_t st);
-int mixed_partial_blocks(int n_faces);
 
 // ---- ensemble (step_mixed.cu): batched launches over instances ----
 // ftiles: (instance, first face) of 32-face tiles; etiles: (instance,

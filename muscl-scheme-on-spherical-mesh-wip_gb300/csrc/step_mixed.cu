@@ -297,10 +297,6 @@ __device__ __forceinline__ void prepare_body(const DevGeomMixed& G, const DevSta
   fold_candidates(vmax, dmin, S.keys);
 }
 
-__global__ void __launch_bounds__(128) prepare_kernel(DevGeomMixed G, DevState S, PhysParams P) {
-  prepare_body(G, S, P, blockIdx.x * blockDim.x + threadIdx.x);
-}
-
 // set_state of the mixed path in one pass: the block stages the caller's
 // rows of kBlock consecutive reference faces (contiguous in the caller's
 // [F][dim] array, possibly host memory read over the coherent link) through
@@ -662,18 +658,7 @@ inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
 }  // namespace
 }  // namespace mx
 
-// the stage-2 flux launch writes one partial record per 32-face tile; the
-// prepare launch (128 faces per block) writes fewer, all within that count
-int mixed_partial_blocks(int n_faces) { return (n_faces + mx::kFaceTile - 1) / mx::kFaceTile; }
-
 const void* mixed_finalize_kernel_ptr() { return (const void*)mx::finalize_kernel; }
-
-cudaError_t mixed_prepare(const DevGeomMixed& G, const DevState& S, const PhysParams& P,
-                          cudaStream_t st) {
-  mx::reset_keys_kernel<<<1, 1, 0, st>>>(S.keys);
-  mx::prepare_kernel<<<(G.n_faces + 127) / 128, 128, 0, st>>>(G, S, P);
-  return cudaGetLastError();
-}
 
 cudaError_t mixed_scatter_prepare(const double* aos, const int* iperm, const DevGeomMixed& G, const DevState& S,
                                   const PhysParams& P, int dim, cudaStream_t st) {

@@ -176,3 +176,26 @@ def test_multi_step_graphs_equal_single_steps():
     assert a.time() == b.time() and a.last_dt() == b.last_dt()
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("field", [0, 4])
+def test_nan_input_stop_flag_mixed_like_fp64(field):
+    """A NaN planted in the host input state: in the density it reaches the
+    fluxes and latches the stop flag (MUSCL_base.hpp:264-268); in the energy
+    the pressure floor swallows it (MUSCL_base.hpp:538) and the step does not
+    stop.  The mixed path must stop exactly when the FP64 path (and the
+    reference) does, and carry the same NaN pattern in its state."""
+    from test_gpu_parity import gpu_solver
+
+    c = dict(load("state_hex3_hllc_acc.npz"))
+    U = c["U0"].copy()
+    U[5, field] = np.nan
+    out = {}
+    for prec in (0, 1):
+        s = gpu_solver(c, precision=prec)
+        s.set_state(U)
+        s.do_step(1e-3)
+        out[prec] = (s.get_stop_check(), np.isnan(s.get_state()))
+    assert out[0][0] == out[1][0] == (field == 0)
+    if field == 4:
+        assert np.array_equal(out[0][1], out[1][1])
