@@ -64,7 +64,9 @@ def peaks():
 def workload_config(n_faces, precision_name):
     return {"workload": f"icosphere_hex({LEVEL}) MUSCL_HLLCplus dim5 accretion_on quiet-noise seed1",
             "n_faces": n_faces, "solver": "HLLCplus", "dt0": DT0, "precision": precision_name,
-            "l2": "per-step working set larger than the 129 MB L2 (see working_set_mb)"}
+            "l2": "inputs larger than L2: the per-step working set (working_set_mb, decimal MB) exceeds the "
+                  "129 MB L2 and is swept cyclically, so each launch re-reads its geometry from DRAM "
+                  "(ncu: 82 MB DRAM reads per edge launch, profiles/traffic_hex7_mixed.txt); no flush"}
 
 
 # ------------------------------------------------------------------ clocks
@@ -496,7 +498,7 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
         "config": {**workload_config(F, "mixed FP32/FP64"), "parallelism": f"replicas{world}",
-                   "working_set_mb": round((geo_b + st_b) / 2**20, 1)},
+                   "working_set_mb": round((geo_b + st_b) / 1e6, 1)},
         "gpu_launches": 5 * args.steps,
         "e2e": {"value": F * e2e_steps / e2e_secs, "unit": METRIC, "h2d_bytes_per_step": bytes_io,
                 "d2h_bytes_per_step": bytes_io},
