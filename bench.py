@@ -453,7 +453,7 @@ def run_ours(args):
                               device=local)
     fp64 = sg.MUSCL_HLLCplus(mesh, U0, 5, gam, 0.0, True, params=params, precision=sg.PREC_FP64,
                              device=local)
-    # one replica per GPU (the step does not shard)
+    # one full replica per GPU: the step does not shard
     with ClockSampler(local) as clocks:
         if world > 1:
             torch.distributed.barrier()
