@@ -497,9 +497,10 @@ __device__ __forceinline__ void edge_body(const DevGeomMixed& G, const DevState&
   if ((threadIdx.x & 31) == 0 && bits) atomicOr(S.err, bits);
 }
 
-// at most 85 registers (6 blocks of 128 per SM; measured best of 5, 6, 8)
+// at most 73 registers (7 blocks of 128 per SM; a small spill, measured best
+// of 5 to 8 blocks)
 template <int STAGE>
-__global__ void __launch_bounds__(kBlock, 6) edge_kernel(DevGeomMixed G, DevState S, PhysParams P) {
+__global__ void __launch_bounds__(kBlock, 7) edge_kernel(DevGeomMixed G, DevState S, PhysParams P) {
   griddep_launch_dependents();
   edge_body<STAGE>(G, S, P, blockIdx.x * blockDim.x + threadIdx.x);
 }
