@@ -268,7 +268,7 @@ SPLASH_API int splash_ensemble_member_info(splash_ensemble* e, int member, doubl
 /* The chosen schedule: tile order (0 member order, 1 largest first, 2
  * round-robin) and the threads per block of the reconstruction + edge-flux
  * launch; and the autotuner's per-candidate ms per step (index
- * order*3 + {64,128,256}-thread blocks). */
+ * order*3 + {32,64,128}-thread blocks). */
 SPLASH_API int splash_ensemble_schedule(splash_ensemble* e, int* order, int* recon_width, double trial_ms[9]);
 SPLASH_API int splash_ensemble_size(splash_ensemble* e, int* n_members, int64_t* total_faces);
 

@@ -169,7 +169,7 @@ struct Ensemble {
     cudaEvent_t a, b;
     ENS_CUDA(cudaEventCreate(&a));
     ENS_CUDA(cudaEventCreate(&b));
-    const int widths[3] = {64, 128, 256};
+    const int widths[3] = {32, 64, 128};  // threads per edge block (at most 128, the kernel's bound)
     double best = 1e30;
     int best_o = 0, best_w = 128;
     for (int o = 0; o < 3; ++o)

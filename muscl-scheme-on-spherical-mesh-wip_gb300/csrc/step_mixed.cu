@@ -631,8 +631,10 @@ __global__ void ens_finalize_kernel(const EnsInstance* __restrict__ inst, int n,
 // reconstruction + edge fluxes: one 32-edge tile per warp (tiles hold
 // (instance, first edge))
 constexpr int kWarpTiles = kBlock / 32;
+// at most 73 registers like the single-solver edge launch (blocks of at
+// most 128 threads)
 template <int STAGE>
-__global__ void __launch_bounds__(256) ens_edge_kernel(const EnsInstance* __restrict__ inst,
+__global__ void __launch_bounds__(kBlock, 7) ens_edge_kernel(const EnsInstance* __restrict__ inst,
                                                        const int2* __restrict__ tiles, int n_tiles) {
   griddep_launch_dependents();
   const int tile = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);

@@ -43,7 +43,7 @@ def test_ensemble_members_equal_standalone_solvers():
     n, total = ens.size()
     assert n == len(ms) and total == sum(m["U_in"].shape[0] for m in ms)
     sched = ens.schedule()
-    assert sched["recon_width"] in (64, 128, 256)
+    assert sched["recon_width"] in (32, 64, 128)
     assert all(t > 0 for row in sched["trial_ms"] for t in row)
     ens.do_steps(25, 1e-2)  # dt0 large: every member takes its own CFL dt
     dts = set()
