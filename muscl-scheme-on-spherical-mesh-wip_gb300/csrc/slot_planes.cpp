@@ -1,6 +1,7 @@
 // Host preparation of the device layout; see slot_planes.hpp.
 #include "slot_planes.hpp"
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <stdexcept>
@@ -195,31 +196,53 @@ MixedPlanes make_mixed_planes(const SlotPlanes& sp) {
   const size_t PS = sp.PS();
   mp.fcn32.assign(sp.fcn.begin(), sp.fcn.end());
   mp.coef.assign(PS, 0.0f);
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < sp.n_faces; ++i)
     for (int j = 0; j < (int)sp.nslots[i]; ++j) {
       const size_t q = (size_t)j * sp.fpad + i;
       mp.coef[q] = (float)(sp.round_diff * sp.chord[q] / sp.area[i]);
     }
   if (sp.n_faces >= (1 << 28)) throw std::runtime_error("too many faces for the edge records");
-  // edges in ascending owner order (plane-major, faces ascending within a
-  // plane): the reverse side of every edge is met either as an owner's
-  // neighbour before it, or as an owner itself
-  std::vector<int> own, nbr;
+  // Edges in ascending owner order (plane-major, faces ascending within a
+  // plane, i.e. ascending slot-plane index): edge e is the e-th owner slot,
+  // its index an exclusive prefix sum of the owner flags.
+  std::vector<unsigned char> is_own(PS, 0);
+  bool lonely = false;
+#pragma omp parallel for schedule(static) reduction(|| : lonely)
+  for (long long q = 0; q < (long long)PS; ++q) {
+    const int i = (int)(q % sp.fpad), j = (int)(q / sp.fpad);
+    if (i >= sp.n_faces || j >= (int)sp.nslots[i]) continue;
+    const int r = sp.rev[q];
+    if (r == (int)q) lonely = true;
+    is_own[q] = (int)q < r;
+  }
+  if (lonely) throw std::runtime_error("slot without a neighbour");
+  // prefix sum over fixed chunks: counts per chunk, then offsets
+  const long long nchunk = 256, clen = ((long long)PS + nchunk - 1) / nchunk;
+  std::vector<long long> base(nchunk + 1, 0);
+#pragma omp parallel for schedule(static)
+  for (long long c = 0; c < nchunk; ++c) {
+    long long cnt = 0;
+    for (long long q = c * clen; q < std::min((long long)PS, (c + 1) * clen); ++q) cnt += is_own[q];
+    base[c + 1] = cnt;
+  }
+  for (long long c = 0; c < nchunk; ++c) base[c + 1] += base[c];
+  mp.n_edges = (int)base[nchunk];
+  std::vector<int> own(mp.n_edges), nbr(mp.n_edges);
   mp.slot_edge.assign(PS, 0);
-  for (int j = 0; j < sp.max_slots; ++j)
-    for (int i = 0; i < sp.n_faces; ++i) {
-      if (j >= (int)sp.nslots[i]) continue;
-      const int s = j * sp.fpad + i, r = sp.rev[s];
-      if (r == s) throw std::runtime_error("slot without a neighbour");
-      if (s < r) {
-        const int e = (int)own.size();
-        own.push_back(s);
-        nbr.push_back(r);
-        mp.slot_edge[s] = e;
-        mp.slot_edge[r] = (int)((unsigned)e | 0x80000000u);
-      }
+#pragma omp parallel for schedule(static)
+  for (long long c = 0; c < nchunk; ++c) {
+    long long e = base[c];
+    for (long long q = c * clen; q < std::min((long long)PS, (c + 1) * clen); ++q) {
+      if (!is_own[q]) continue;
+      const int r = sp.rev[q];
+      own[e] = (int)q;
+      nbr[e] = r;
+      mp.slot_edge[q] = (int)e;
+      mp.slot_edge[r] = (int)((unsigned)e | 0x80000000u);
+      ++e;
     }
-  mp.n_edges = (int)own.size();
+  }
   const int ep = mp.epad = (mp.n_edges + 31) / 32 * 32;
   mp.e_ids.assign(4 * (size_t)ep, 0);
   mp.e_ec.assign(4 * (size_t)ep, 0.f);
@@ -228,6 +251,7 @@ MixedPlanes make_mixed_planes(const SlotPlanes& sp) {
   mp.e_sten.assign(8 * (size_t)ep, 0);
   mp.e_beta.assign(8 * (size_t)ep, 0.f);
   mp.e_h.assign(8 * (size_t)ep, 0.f);
+#pragma omp parallel for schedule(static)
   for (int e = 0; e < mp.n_edges; ++e) {
     const size_t side_slot[2] = {(size_t)own[e], (size_t)nbr[e]};
     int face[2], n[2];
