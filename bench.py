@@ -433,6 +433,23 @@ def l1_rel(a, b, area):
     return num / np.where(den > 0, den, 1)
 
 
+def max_over_ranks(torch, secs: float, world: int, device: str) -> float:
+    """The largest timed-region length over all ranks (every rank runs one
+    full replica; the whole job ends when the slowest does).  device: where
+    the reduction tensor lives ("cuda" for NCCL, "cpu" for gloo)."""
+    if world <= 1:
+        return secs
+    t = torch.tensor([secs], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(units_per_rank: int, steps: int, world: int, secs_max: float) -> float:
+    """Whole-job throughput: the units every rank processed, over the
+    slowest rank's time (weak scaling: each rank's work is fixed)."""
+    return units_per_rank * steps * world / secs_max
+
+
 def run_ours(args):
     import torch
 
@@ -459,12 +476,9 @@ def run_ours(args):
             torch.distributed.barrier()
         torch.cuda.synchronize()
         secs = time_device(sg, torch, mixed, F, args.steps, args.warmup)
-        if world > 1:
-            t = torch.tensor([secs], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            secs = float(t.item())
+        secs = max_over_ranks(torch, secs, world, "cuda")
     clk = clocks.summary()
-    value = F * args.steps * world / secs
+    value = job_value(F, args.steps, world, secs)
     secs64 = time_device(sg, torch, fp64, F, args.steps, args.warmup)
     value64 = F * args.steps / secs64
     # accuracy of the timed runs: both advanced warmup + steps from the same state
