@@ -158,11 +158,11 @@ SPLASH_API int splash_kernel_times(splash_solver* s, int reps, double dt0, doubl
 /* Mean device ms of every launch of one step over `reps` un-captured steps,
  * with a CUDA event between consecutive launches (which serialises the
  * step's programmatic overlap, so the sum exceeds the captured step's time).
- * Mixed path, 7 launches: finalize, reconstruct, edge flux, update (stage 1),
- * reconstruct, edge flux, update (stage 2); FP64 path, 5 launches: dt
- * reduction, reconstruct, flux+update, reconstruct, flux+update.  Writes
- * min(cap, *count) values; *count = launches per step.  The steps advance
- * the state like do_step(dt0). */
+ * Five launches on either path: mixed, finalize, edge (reconstruction +
+ * Riemann flux, stage 1), update (stage 1), edge (stage 2), update
+ * (stage 2); FP64, dt reduction, reconstruct, flux+update, reconstruct,
+ * flux+update.  Writes min(cap, *count) values; *count = launches per step.
+ * The steps advance the state like do_step(dt0). */
 SPLASH_API int splash_launch_times(splash_solver* s, int reps, double dt0, double* ms, int cap, int* count);
 /* Device bytes held by the solver: out[0] geometry, out[1] state + scratch. */
 SPLASH_API int splash_memory(splash_solver* s, int64_t out[2]);
