@@ -150,10 +150,11 @@ SPLASH_API int splash_synchronize(splash_solver* s);
 SPLASH_API int splash_stream(splash_solver* s, void** stream);
 /* Runs `reps` un-captured steps with CUDA events between the step's phases
  * and returns the mean device time per phase in milliseconds:
- * ms[0] dt reduction (finalize), ms[1] reconstruct (stage 1), ms[2] flux and
- * update (stage 1; on the mixed path the edge-flux and update launches),
- * ms[3] reconstruct (stage 2), ms[4] flux and update (stage 2).
- * The steps advance the state like do_step(dt0). */
+ * ms[0] dt reduction (finalize); FP64 path: ms[1] reconstruct (stage 1),
+ * ms[2] flux+update (stage 1), ms[3] reconstruct (stage 2), ms[4]
+ * flux+update (stage 2); mixed path: ms[1] edge (reconstruction + Riemann
+ * flux, stage 1), ms[2] update (stage 1), ms[3] edge (stage 2), ms[4] update
+ * (stage 2).  The steps advance the state like do_step(dt0). */
 SPLASH_API int splash_kernel_times(splash_solver* s, int reps, double dt0, double ms[5]);
 /* Mean device ms of every launch of one step over `reps` un-captured steps,
  * with a CUDA event between consecutive launches (which serialises the
