@@ -350,15 +350,23 @@ __global__ void reset_keys_kernel(unsigned long long* keys) {
 // and a fresh start for the keys the step's stage-2 launch will fold into.
 __device__ __forceinline__ void finalize_body(const DevState& S, const PhysParams& P, double dt0) {
   griddep_wait();
-  const double max_vel = sqrt(key_value(S.keys[0]));
+  // the candidates are FP32 values (see dt_candidates_f32), so the clip is
+  // evaluated in FP32 and only the chosen bound is widened to FP64
+  const float max_vel_f = sqrtf(fpc::d2f(key_value(S.keys[0])));
+  const double max_vel = fpc::f2d(max_vel_f);
   const double xs = key_value(S.keys[1]);
-  double extra = (xs >= kNoExtraSq) ? 1e20 : (xs < 0 ? -sqrt(-xs) : sqrt(xs));
+  double extra = 1e20;
+  if (xs < kNoExtraSq) {
+    const float xf = fpc::d2f(xs);
+    extra = fpc::f2d(xf < 0.f ? -sqrtf(-xf) : sqrtf(xf));
+  }
   if (extra < 0) {
     atomicOr(S.err, 8u);  // SPLASH_STOP_NEG_EXTRA_DT
     extra = 1e20;
   }
+  const double cfl = fpc::f2d(fpc::d2f(P.h0 * 0.1) / max_vel_f);
   double dt = dt0;
-  if (dt > P.h0 * 0.1 / max_vel) dt = P.h0 * 0.1 / max_vel;
+  if (dt > cfl) dt = cfl;
   if (dt > extra) dt = extra;
   S.scal[kScDt] = dt;
   S.scal[kScDtHalf] = dt / 2;
