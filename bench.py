@@ -230,8 +230,8 @@ def algorithmic_bytes_mixed(geom, kernel: str) -> float:
     S slots, E = S / 2 interior edges).
 
     edge (reconstruction + Riemann flux, one thread per edge): the edge
-      record (face ids, edge centre, normal, n x R, both slots' eta: 64 B)
-      and per side the stencil, weights and distances (2 x 48 B); every face
+      record (face ids, edge centre, normal, n x R: 48 B) and per side the
+      stencil, weights and distances (2 x 48 B); every face
       state W32 read once (20 B per face); write the edge flux (20 B per
       edge) and, in stage 2, both edge states (2 x 20 B per edge; mean of the
       two stages).
@@ -244,7 +244,7 @@ def algorithmic_bytes_mixed(geom, kernel: str) -> float:
     S = geom.n_slots
     E = S // 2
     if kernel == "edge":
-        return E * (64 + 96 + 20 + 40 / 2) + F * 20
+        return E * (48 + 96 + 20 + 40 / 2) + F * 20
     return F * (20 + 40 + 24 + 12 + 8 + 1) + S * 8 + E * 20 + F * (20 + 40 / 2)
 
 

@@ -180,13 +180,12 @@ void Solver::build_device_geometry(const RefGeometry& g) {
     GM.e_ids = upload(mp.e_ids);
     GM.e_ec = upload(mp.e_ec);
     GM.e_en = upload(mp.e_en);
-    GM.e_eta = upload(mp.e_eta);
     GM.e_sten = upload(mp.e_sten);
     GM.e_beta = upload(mp.e_beta);
     GM.e_h = upload(mp.e_h);
     geometry_bytes = sp.nslots.size() + 8 * (sp.fcn.size() + sp.area.size() + acc.size()) +
                      4 * (mp.fcn32.size() + mp.coef.size() + mp.slot_edge.size() + mp.e_ids.size() +
-                          mp.e_ec.size() + mp.e_en.size() + mp.e_eta.size() + mp.e_sten.size() +
+                          mp.e_ec.size() + mp.e_en.size() + mp.e_sten.size() +
                           mp.e_beta.size() + mp.e_h.size());
   } else {
     G.n_faces = n_faces;

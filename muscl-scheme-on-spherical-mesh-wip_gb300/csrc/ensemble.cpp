@@ -305,7 +305,6 @@ int splash_ensemble_create(const splash_member* members, int n, int device, int 
         L.G.e_ids = e->upload(mp.e_ids);
         L.G.e_ec = e->upload(mp.e_ec);
         L.G.e_en = e->upload(mp.e_en);
-        L.G.e_eta = e->upload(mp.e_eta);
         L.G.e_sten = e->upload(mp.e_sten);
         L.G.e_beta = e->upload(mp.e_beta);
         L.G.e_h = e->upload(mp.e_h);

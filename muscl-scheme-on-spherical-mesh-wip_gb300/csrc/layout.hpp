@@ -112,7 +112,6 @@ struct DevGeomMixed {
   const int* e_ids;       // f | n_f << 28, g | n_g << 28, bits of (n x R).z, 0
   const float* e_ec;      // owner's unit edge centre, (n x R).x
   const float* e_en;      // owner's edge normal, (n x R).y
-  const float* e_eta;     // H+/BM, H-/BM: owner, then reverse slot
   const int* e_sten;      // [2][epad]: stencil faces, owner then reverse slot
   const float* e_beta;    // [2][epad]: beta_plus 0, 1, beta_minus 0, 1
   const float* e_h;       // [2][epad]: 1/H_plus, 1/H_minus, BM_dist, arc/area

@@ -247,7 +247,6 @@ MixedPlanes make_mixed_planes(const SlotPlanes& sp) {
   mp.e_ids.assign(4 * (size_t)ep, 0);
   mp.e_ec.assign(4 * (size_t)ep, 0.f);
   mp.e_en.assign(4 * (size_t)ep, 0.f);
-  mp.e_eta.assign(4 * (size_t)ep, 1.f);
   mp.e_sten.assign(8 * (size_t)ep, 0);
   mp.e_beta.assign(8 * (size_t)ep, 0.f);
   mp.e_h.assign(8 * (size_t)ep, 0.f);
@@ -276,8 +275,6 @@ MixedPlanes make_mixed_planes(const SlotPlanes& sp) {
     for (int k = 0; k < 2; ++k) {
       const size_t q = side_slot[k];
       const size_t o = 4 * ((size_t)k * ep + e);
-      mp.e_eta[4 * (size_t)e + 2 * k] = (float)sp.eta[q];
-      mp.e_eta[4 * (size_t)e + 2 * k + 1] = (float)sp.eta[PS + q];
       for (int c = 0; c < 4; ++c) {
         mp.e_sten[o + c] = sp.sten[c * PS + q];
         mp.e_beta[o + c] = (float)sp.beta[c * PS + q];

@@ -64,7 +64,6 @@ struct MixedPlanes {
   std::vector<int> slot_edge;          // [max_slots * fpad]
   std::vector<int> e_ids;              // [epad][4]: f | n_f << 28, g | n_g << 28, bits of (n x R).z, 0
   std::vector<float> e_ec, e_en;       // [epad][4]: owner's unit edge centre | (n x R).x, normal | (n x R).y
-  std::vector<float> e_eta;            // [epad][4]: H+/BM, H-/BM of the owner, then of the reverse slot
   std::vector<int> e_sten;             // [2][epad][4]: stencil faces (plus pair, minus pair), owner then reverse
   std::vector<float> e_beta;           // [2][epad][4]: beta_plus 0, 1, beta_minus 0, 1
   std::vector<float> e_h;              // [2][epad][4]: 1/H_plus, 1/H_minus, BM_dist, arc/area

@@ -461,13 +461,12 @@ template <int STAGE>
 __device__ __forceinline__ void edge_body(const DevGeomMixed& G, const DevState& S, const PhysParams& P, int e) {
   const bool live = e < G.n_edges;
   int4 ids = make_int4(0, 0, 0, 0);
-  float4 ce = make_float4(0.f, 0.f, 0.f, 0.f), ne = ce, et = ce;
+  float4 ce = make_float4(0.f, 0.f, 0.f, 0.f), ne = ce;
   SlotConsts so{}, sr{};
   if (live) {
     ids = reinterpret_cast<const int4*>(G.e_ids)[e];
     ce = reinterpret_cast<const float4*>(G.e_ec)[e];
     ne = reinterpret_cast<const float4*>(G.e_en)[e];
-    et = reinterpret_cast<const float4*>(G.e_eta)[e];
     so.st = reinterpret_cast<const int4*>(G.e_sten)[e];
     sr.st = reinterpret_cast<const int4*>(G.e_sten)[G.epad + e];
     so.bt = reinterpret_cast<const float4*>(G.e_beta)[e];
@@ -475,10 +474,11 @@ __device__ __forceinline__ void edge_body(const DevGeomMixed& G, const DevState&
     so.hh = reinterpret_cast<const float4*>(G.e_h)[e];
     sr.hh = reinterpret_cast<const float4*>(G.e_h)[G.epad + e];
   }
-  so.eta_p = et.x;
-  so.eta_m = et.y;
-  sr.eta_p = et.z;
-  sr.eta_m = et.w;
+  // H+/BM and H-/BM from the distances: 1 / ((1/H) BM)
+  so.eta_p = 1.0f / (so.hh.x * so.hh.z);
+  so.eta_m = 1.0f / (so.hh.y * so.hh.z);
+  sr.eta_p = 1.0f / (sr.hh.x * sr.hh.z);
+  sr.eta_m = 1.0f / (sr.hh.y * sr.hh.z);
   griddep_wait();
   unsigned bits = 0;
   if (live) {
