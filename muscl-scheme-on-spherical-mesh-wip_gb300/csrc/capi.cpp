@@ -170,6 +170,7 @@ void Solver::build_device_geometry(const RefGeometry& g) {
     GM.nslots = upload(sp.nslots);
     GM.fcn = upload(sp.fcn);
     GM.fcn32 = upload(mp.fcn32);
+    GM.fcn_lo = upload(mp.fcn_lo);
     GM.area = upload(sp.area);
     GM.acc_src = upload(acc);
     GM.coef = upload(mp.coef);
@@ -184,7 +185,7 @@ void Solver::build_device_geometry(const RefGeometry& g) {
     GM.e_beta = upload(mp.e_beta);
     GM.e_h = upload(mp.e_h);
     geometry_bytes = sp.nslots.size() + 8 * (sp.fcn.size() + sp.area.size() + acc.size()) +
-                     4 * (mp.fcn32.size() + mp.coef.size() + mp.slot_edge.size() + mp.e_ids.size() +
+                     4 * (mp.fcn32.size() + mp.fcn_lo.size() + mp.coef.size() + mp.slot_edge.size() + mp.e_ids.size() +
                           mp.e_ec.size() + mp.e_en.size() + mp.e_sten.size() +
                           mp.e_beta.size() + mp.e_h.size());
   } else {

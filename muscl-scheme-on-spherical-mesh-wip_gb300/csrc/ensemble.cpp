@@ -297,6 +297,7 @@ int splash_ensemble_create(const splash_member* members, int n, int device, int 
         L.G.nslots = e->upload(L.sp.nslots);
         L.G.fcn = e->upload(L.sp.fcn);
         L.G.fcn32 = e->upload(mp.fcn32);
+        L.G.fcn_lo = e->upload(mp.fcn_lo);
         L.G.area = e->upload(L.sp.area);
         L.G.coef = e->upload(mp.coef);
         L.G.slot_edge = e->upload(mp.slot_edge);

@@ -43,6 +43,7 @@ struct PhysParams {
   double fric_k;
   double gam_m1, fric_ak;  // gam - 1 and alpha * fric_k (mixed-path update)
   float gam_f, e_acc_f, alpha_f, omega_ns_f, fric_ak_f;
+  float gam_m1_h, gam_m1_l;  // gam - 1 as a double-word (nearest float + residual)
   float omega_acc_f[3];
   float depletion_f;     // -(acc_rate 4 pi) / total_mass (adiabatic.hpp:430-436)
 };
@@ -54,6 +55,8 @@ inline void derive_params(PhysParams& P) {
   P.gam_m1 = P.gam - 1.0;
   P.fric_ak = P.alpha * P.fric_k;
   P.fric_ak_f = (float)P.fric_ak;
+  P.gam_m1_h = (float)P.gam_m1;
+  P.gam_m1_l = (float)(P.gam_m1 - (double)P.gam_m1_h);
   P.gam_f = (float)P.gam;
   P.e_acc_f = (float)P.e_acc;
   P.alpha_f = (float)P.alpha;
@@ -100,7 +103,8 @@ struct DevGeomMixed {
   int max_slots;
   const int8_t* nslots;
   const double* fcn;      // 3 planes, FP64 unit face centre
-  const float* fcn32;     // 3 planes, FP32 copy (source term)
+  const float* fcn32;     // 3 planes, FP32 copy (source term), the nearest float
+  const float* fcn_lo;    // 3 planes, fcn - fcn32 rounded to a float (fcn as a double-word)
   const double* area;
   const double* acc_src;  // accretion mass source, FP64
   const float* coef;      // per slot: round_diff * chord / area

@@ -195,6 +195,8 @@ MixedPlanes make_mixed_planes(const SlotPlanes& sp) {
   MixedPlanes mp;
   const size_t PS = sp.PS();
   mp.fcn32.assign(sp.fcn.begin(), sp.fcn.end());
+  mp.fcn_lo.resize(sp.fcn.size());
+  for (size_t i = 0; i < sp.fcn.size(); ++i) mp.fcn_lo[i] = (float)(sp.fcn[i] - (double)mp.fcn32[i]);
   mp.coef.assign(PS, 0.0f);
 #pragma omp parallel for schedule(static)
   for (int i = 0; i < sp.n_faces; ++i)

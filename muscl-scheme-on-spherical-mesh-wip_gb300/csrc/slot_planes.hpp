@@ -59,7 +59,7 @@ std::vector<double> accretion_source_fcn(const std::vector<double>& fcn, int n_f
 // slot is reconstructed with the owner's centre and the negated normal.
 // Per-edge records hold four interleaved values (one 16-byte load each).
 struct MixedPlanes {
-  std::vector<float> fcn32, coef;      // per face; per slot (slot planes)
+  std::vector<float> fcn32, fcn_lo, coef;  // per face (nearest float, residual); per slot (slot planes)
   int n_edges = 0, epad = 0;           // epad: n_edges rounded up to 32
   std::vector<int> slot_edge;          // [max_slots * fpad]
   std::vector<int> e_ids;              // [epad][4]: f | n_f << 28, g | n_g << 28, bits of (n x R).z, 0

@@ -15,6 +15,7 @@
 
 #include <cstdint>
 
+#include "dword.cuh"
 #include "fp_convert.cuh"
 #include "kernels.hpp"
 #include "physics_fp64.cuh"
@@ -78,10 +79,6 @@ __device__ __forceinline__ void st5(float* base, int n, int i, const float* v) {
   base[4 * (size_t)n + i] = v[4];
 }
 
-__device__ __forceinline__ f64::D3 plane3d(const double* p, int stride, int i) {
-  return f64::D3{p[i], p[stride + i], p[2 * stride + i]};
-}
-
 // The min key holds the signed square of the extra dt; 1e40 = (1e20)^2 is
 // the reference's initial extra dt (adiabatic.hpp:545) and the isothermal
 // solver's only candidate (isothermal.hpp:262-267).
@@ -117,41 +114,18 @@ __device__ __forceinline__ void fold_candidates(double vmax2, double dmin, unsig
   }
 }
 
-// 1/x in FP64 by one Newton-Raphson step r1 = r0 + r0 (1 - x r0) from the
-// FP32 reciprocal r0: the step squares the seed's relative error (about
-// 2^-22), so r1 is within about 2^-43 of 1/x, far below the FP32 rounding of
-// every value it feeds (face states) and irrelevant to the dt candidates.
-// Two FP64 fused multiply-adds instead of a correctly rounded division.  An
-// x outside the FP32 range (seed 0, inf or NaN; x = 0 included) takes the
-// exact division, so zeros, infinities and NaN behave as 1.0 / x.
-__device__ __forceinline__ double recip_nr(double x) {
-  const float rf = 1.0f / fpc::d2f(x);
-  if (!(fabsf(rf) <= 3.0e38f) || rf == 0.0f) return 1.0 / x;
-  const double r0 = fpc::f2d(rf);
-  return fma(r0, fma(-x, r0, 1.0), r0);
-}
-
-// FP64 pressure recovery: Pi = (E - |r x l|^2/(2 Sigma))(gam-1), floored at
-// 1e-16 like MUSCL_base.hpp:538.  Also returns |v|^2 and 1/Sigma for the dt
-// candidates.
-__device__ __forceinline__ double pressure_recover(const double* u, f64::D3 r, double gam_m1,
-                                                   double& v2, double& inv_rho) {
-  const f64::D3 c = f64::cross3(r, f64::d3(u[1], u[2], u[3]));
-  inv_rho = recip_nr(u[0]);
-  const double c2 = c.x * c.x + c.y * c.y + c.z * c.z;
-  v2 = c2 * inv_rho * inv_rho;
-  const double p = (u[4] - 0.5 * c2 * inv_rho) * gam_m1;
-  return (1e-16 < p) ? p : 1e-16;
-}
-
-// stores the FP32 face state (Sigma, l, Pi) of u and pressure p, returned in v
-__device__ __forceinline__ void store_w32(float* W32, int fp, int f, const double* u, double p, float* v) {
-  v[0] = fpc::d2f(u[0]);
-  v[1] = fpc::d2f(u[1]);
-  v[2] = fpc::d2f(u[2]);
-  v[3] = fpc::d2f(u[3]);
-  v[4] = fpc::d2f(p);
-  st5(W32, fp, f, v);
+// The FP32 face state (Sigma, l, Pi) of the FP64 state u of face f, stored
+// to W32 and returned in w: the pressure recovery Pi = (E - |r x l|^2 /
+// (2 Sigma)) (gam - 1), floored at 1e-16 (MUSCL_base.hpp:538), runs in
+// double-word FP32 arithmetic (dword.cuh), accurate to the FP32 rounding of
+// Pi down to kinetic energies within 1e-5 of E, instead of on the FP64 pipe
+// (about 2 lanes per SM per clock here); lo holds the FP32 residuals of the
+// unit centre r32.
+__device__ __forceinline__ void store_face_state(float* W32, int fp, int f, const double* u, F3 r32, F3 lo,
+                                                 const PhysParams& P, float* w) {
+  const dw::DW r[3] = {{r32.x, lo.x}, {r32.y, lo.y}, {r32.z, lo.z}};
+  dw::face_state_dw(u, r, dw::DW{P.gam_m1_h, P.gam_m1_l}, w);
+  st5(W32, fp, f, w);
 }
 
 // dt candidates in FP32 from the FP32 face state w = (Sigma, l, Pi) (the
@@ -274,11 +248,8 @@ __device__ __forceinline__ void prepare_face(const DevGeomMixed& G, const DevSta
   if (P.solver == kSolverIsoHLLE) {
     iso_w32_candidates(u, r32, S.W32, G.fpad, f, vmax, dmin);
   } else {
-    const f64::D3 r = plane3d(G.fcn, G.fpad, f);
-    double v2, inv_rho;
-    const double p = pressure_recover(u, r, P.gam_m1, v2, inv_rho);
     float w[kDim];
-    store_w32(S.W32, G.fpad, f, u, p, w);
+    store_face_state(S.W32, G.fpad, f, u, r32, plane3f(G.fcn_lo, G.fpad, f), P, w);
     dt_candidates_f32(w, r32, P, vmax, dmin);
   }
 }
@@ -527,9 +498,8 @@ __device__ __forceinline__ void update_body(const DevGeomMixed& G, const DevStat
                                             int f) {
   const int fp = G.fpad;
   const bool live = f < G.n_faces;
-  F3 fcn32 = f3(0.f, 0.f, 0.f);
+  F3 fcn32 = f3(0.f, 0.f, 0.f), fcn_lo = f3(0.f, 0.f, 0.f);
   double acc0 = 0.0;
-  f64::D3 r{0.0, 0.0, 0.0};
   int n = 0;
   // the slots' edges and flux coefficients: geometry, loaded before the wait
   int se[kMaxFaceSlots];
@@ -537,7 +507,7 @@ __device__ __forceinline__ void update_body(const DevGeomMixed& G, const DevStat
   if (live) {
     fcn32 = plane3f(G.fcn32, fp, f);
     acc0 = G.acc_src[f];
-    r = plane3d(G.fcn, fp, f);
+    if (P.solver != kSolverIsoHLLE) fcn_lo = plane3f(G.fcn_lo, fp, f);
     n = G.nslots[f];
   }
 #pragma unroll
@@ -591,10 +561,8 @@ __device__ __forceinline__ void update_body(const DevGeomMixed& G, const DevStat
         dmin = dm;
       }
     } else {
-      double v2, inv_rho;
-      const double p = pressure_recover(u, r, P.gam_m1, v2, inv_rho);
       float w32[kDim];
-      store_w32(S.W32, fp, f, u, p, w32);
+      store_face_state(S.W32, fp, f, u, fcn32, fcn_lo, P, w32);
       if (STAGE == 2) {
 #pragma unroll
         for (int k = 0; k < kDim; ++k) S.U[k * fp + f] = u[k];
