@@ -4,9 +4,10 @@
 // reconstruction and a flux + update launch), with the work split:
 //   FP32: slopes and limiter, edge states, Riemann fluxes, source terms,
 //         the per-slot flux contributions;
-//   FP64: the conserved state U, the RK combine U0 + dt*Phi, pressure
-//         recovery Pi = (E - |r x l|^2 / (2 Sigma)) (gam - 1), the CFL / extra
+//   FP64: the conserved state U, the RK combine U0 + dt*Phi, the CFL / extra
 //         dt reduction, simulation time, and the accretion mass source;
+//   double-word FP32 (FP32 pairs, dword.cuh): the pressure recovery
+//         Pi = (E - |r x l|^2 / (2 Sigma)) (gam - 1);
 //   compensated: the per-face sum of the FP32 contributions is carried as an
 //         FP32 (hi, lo) pair and folded into FP64.
 // W32 holds (Sigma, l, Pi) of the current stage input in FP32; every thread
@@ -489,10 +490,10 @@ __global__ void __launch_bounds__(kBlock, 7) edge_kernel(DevGeomMixed G, DevStat
 // reverse side) summed in slot order (Neumaier-compensated FP32), plus
 // dt_here times the source in FP32 from the face state
 // (physics/adiabatic.hpp:396-541), rounded once and added to the FP64 U0;
-// the accretion mass source in FP64; the density floor, FP64 pressure
-// recovery, the FP32 face state of the next stage, and in stage 2 the new U
-// and the dt candidates.  Every lane of the calling warp must call it (the
-// candidates fold per warp).
+// the accretion mass source in FP64; the density floor, the pressure
+// recovery (double-word FP32), the FP32 face state of the next stage, and in
+// stage 2 the new U and the dt candidates.  Every lane of the calling warp
+// must call it (the candidates fold per warp).
 template <int STAGE>
 __device__ __forceinline__ void update_body(const DevGeomMixed& G, const DevState& S, const PhysParams& P,
                                             int f) {
