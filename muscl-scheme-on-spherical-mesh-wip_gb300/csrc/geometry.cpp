@@ -347,8 +347,10 @@ RefGeometry build_ref_geometry(const MeshArrays& mesh, int threads) {
     }
   }
 
-  // h0: minimum great-circle edge length (MUSCL_base.hpp:63-91)
+  // h0: minimum great-circle edge length (MUSCL_base.hpp:63-91); the
+  // minimum is exact in any order
   double h0 = 10;
+#pragma omp parallel for schedule(static) reduction(min : h0)
   for (int f = 0; f < nf; ++f) {
     const int n = off[f + 1] - off[f];
     for (int j = 0; j < n; ++j) {

@@ -3,6 +3,12 @@
 #include <algorithm>
 #include <cmath>
 #include <numeric>
+#include <utility>
+#include <vector>
+
+#ifdef _OPENMP
+#include <parallel/algorithm>
+#endif
 
 namespace splash {
 
@@ -50,9 +56,19 @@ std::vector<int> hilbert_order(const double* xyz, int n) {
     const double r = std::sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
     key[i] = hilbert_key3(p[0] / r, p[1] / r, p[2] / r, 21);
   }
+  // (key, index) pairs are distinct, so any sort of them gives the order of a
+  // stable sort by key; the parallel sort of libstdc++ when OpenMP is on
+  std::vector<std::pair<uint64_t, int>> kv(n);
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < n; ++i) kv[i] = {key[i], i};
+#ifdef _OPENMP
+  __gnu_parallel::sort(kv.begin(), kv.end());
+#else
+  std::sort(kv.begin(), kv.end());
+#endif
   std::vector<int> order(n);
-  std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return key[a] < key[b]; });
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < n; ++i) order[i] = kv[i].second;
   return order;
 }
 
