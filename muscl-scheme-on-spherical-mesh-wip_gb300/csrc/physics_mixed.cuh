@@ -11,7 +11,15 @@
 //     E = Pi/(gam-1) + Sigma |v|^2/2 (a sum of positive terms) where the flux
 //     needs it;
 //   * the unit edge centre is used without the |ec| ~ 1 rescale;
-//   * integer powers are multiplications and pow(1-r, 0.1) is exp(0.1 log).
+//   * integer powers are multiplications and pow(1-r, 0.1) is exp(0.1 log);
+//   * quotients and reciprocals are __fdividef (the approximate reciprocal
+//     of the divisor times the dividend): within 2 ulp like the full-range
+//     division the path is compiled with otherwise, and equal to it for
+//     divisors below 2^126 in magnitude (every divisor here: densities,
+//     pressures, wave-speed differences, slopes; measured bit-identical
+//     states), without its range handling; zero, infinite and NaN divisors
+//     give the same infinities and NaN, which the limiter and the flux
+//     checks handle.
 #pragma once
 
 #include <cmath>
@@ -54,10 +62,10 @@ struct EdgeState {
 __device__ __forceinline__ EdgeState edge_state(const float* u, const SlotGeomF& g, float gam) {
   EdgeState s;
   s.rho = u[0];
-  const float inv = -1.0f / u[0];
+  const float inv = __fdividef(-1.0f, u[0]);
   s.vel = scal(cross3(g.ec, f3(u[1], u[2], u[3])), inv);
   s.p = smax(1e-16f, u[4]);
-  s.E = u[4] / (gam - 1.0f) + 0.5f * u[0] * dot3(s.vel, s.vel);
+  s.E = __fdividef(u[4], gam - 1.0f) + 0.5f * u[0] * dot3(s.vel, s.vel);
   s.vn = dot3(s.vel, g.en);
   return s;
 }
@@ -75,18 +83,18 @@ __device__ __forceinline__ void phys_flux(const float* u, const EdgeState& s, co
 // PVRS wave speeds, physics/adiabatic.hpp:594-683
 __device__ __forceinline__ void char_vel(const EdgeState& L, const EdgeState& R, float gam,
                                          float& S_L, float& S_R, float& a_L, float& a_R) {
-  a_L = sqrtf(gam * L.p / L.rho);
-  a_R = sqrtf(gam * R.p / R.rho);
+  a_L = sqrtf(__fdividef(gam * L.p, L.rho));
+  a_R = sqrtf(__fdividef(gam * R.p, R.rho));
   const float p_pvrs = 0.5f * (L.p + R.p) - 0.125f * (R.vn - L.vn) * (L.rho + R.rho) * (a_L + a_R);
   const float p_star = smax(0.f, p_pvrs);
-  const float k = (gam + 1.0f) / (2.0f * gam);
+  const float k = __fdividef(gam + 1.0f, 2.0f * gam);
   float q_R = 1.f, q_L = 1.f;
   if (!(p_star <= R.p)) {
-    q_R = sqrtf(1.f + k * (p_star / R.p - 1.f));
+    q_R = sqrtf(1.f + k * (__fdividef(p_star, R.p) - 1.f));
     if (isnan(q_R) || isinf(q_R)) q_R = 1.f;
   }
   if (!(p_star <= L.p)) {
-    q_L = sqrtf(1.f + k * (p_star / L.p - 1.f));
+    q_L = sqrtf(1.f + k * (__fdividef(p_star, L.p) - 1.f));
     if (isnan(q_L) || isinf(q_L)) q_L = 1.f;
   }
   S_L = L.vn - a_L * q_L;
@@ -113,7 +121,7 @@ __device__ __forceinline__ unsigned flux_star(const float* uL, const float* uR, 
 #pragma unroll
       for (int i = 0; i < kDim; ++i) F[i] = FL[i];
     } else if (S_L < 0 && S_R > 0) {
-      const float inv = 1.0f / (S_R - S_L);
+      const float inv = __fdividef(1.0f, S_R - S_L);
 #pragma unroll
       for (int i = 0; i < kDim; ++i) F[i] = (S_R * FL[i] - S_L * FR[i] + S_R * S_L * (qR[i] - qL[i])) * inv;
     } else {
@@ -124,8 +132,8 @@ __device__ __forceinline__ unsigned flux_star(const float* uL, const float* uR, 
     return bits;
   }
   const float V_L = L.vn, V_R = R.vn;
-  float S_star = (R.p - L.p + L.rho * V_L * (S_L - V_L) - R.rho * V_R * (S_R - V_R)) /
-                 (L.rho * (S_L - V_L) - R.rho * (S_R - V_R));
+  float S_star = __fdividef(R.p - L.p + L.rho * V_L * (S_L - V_L) - R.rho * V_R * (S_R - V_R),
+                            L.rho * (S_L - V_L) - R.rho * (S_R - V_R));
   if (isnan(S_star) || isinf(S_star)) S_star = 0.5f * (V_L + V_R);
   int side;
   if (S_L >= 0) {
@@ -150,21 +158,21 @@ __device__ __forceinline__ unsigned flux_star(const float* uL, const float* uR, 
   const float Sk = (side == 1) ? S_L : S_R;
   const float* qk = (side == 1) ? qL : qR;
   const float* Fk = (side == 1) ? FL : FR;
-  const float inv = 1.0f / (Sk - S_star);
+  const float inv = __fdividef(1.0f, Sk - S_star);
 #pragma unroll
   for (int i = 0; i < kDim; ++i) F[i] = (S_star * (Sk * qk[i] - Fk[i]) + Sk * P_LR * D[i]) * inv;
   if (solver == 3) {
     const float phi_L = L.rho * (S_L - V_L);
     const float phi_R = R.rho * (S_R - V_R);
-    const float M = smin(1.f, smax(norm3(L.vel) / a_L, norm3(R.vel) / a_R));
+    const float M = smin(1.f, smax(__fdividef(norm3(L.vel), a_L), __fdividef(norm3(R.vel), a_R)));
     int lambd = 0;
     if ((V_L - a_L) > 0 && (V_R - a_R) < 0) lambd = 1;
     if ((V_L + a_L) > 0 && (V_R + a_R) < 0) lambd = 1;
     if ((V_R - a_R) > 0 && (V_L - a_L) < 0) lambd = 1;
     if ((V_R + a_R) > 0 && (V_L + a_L) < 0) lambd = 1;
     float f_star = 1.f;
-    if (lambd == 0) f_star = M * sqrtf(4.f + (1.f - M * M) * (1.f - M * M)) / (1.f + M * M);
-    const float h = smin(L.p / R.p, R.p / L.p);
+    if (lambd == 0) f_star = __fdividef(M * sqrtf(4.f + (1.f - M * M) * (1.f - M * M)), 1.f + M * M);
+    const float h = smin(__fdividef(L.p, R.p), __fdividef(R.p, L.p));
     const float gsw = 1.f - __expf(M * __logf(h));
     const float dV = V_R - V_L;
     const F3 dv = sub(R.vel, L.vel);
@@ -173,7 +181,7 @@ __device__ __forceinline__ unsigned flux_star(const float* uL, const float* uR, 
     const F3 vff = f3(fs * g.en.x + cs * (dv.x - dV * g.en.x), fs * g.en.y + cs * (dv.y - dV * g.en.y),
                       fs * g.en.z + cs * (dv.z - dV * g.en.z));
     const F3 am = cross3(g.ec, vff);
-    const float w = phi_L * phi_R / (phi_R - phi_L);
+    const float w = __fdividef(phi_L * phi_R, phi_R - phi_L);
     F[1] += am.x * w;
     F[2] += am.y * w;
     F[3] += am.z * w;
@@ -197,8 +205,8 @@ __device__ __forceinline__ void iso_phys_flux(const float* u, F3 vel, float vn, 
 }
 
 __device__ __forceinline__ unsigned iso_flux_star(const float* uL, const float* uR, const SlotGeomF& g, float* F) {
-  const F3 vL = scal(cross3(g.ec, f3(uL[1], uL[2], uL[3])), -1.0f / uL[0]);
-  const F3 vR = scal(cross3(g.ec, f3(uR[1], uR[2], uR[3])), -1.0f / uR[0]);
+  const F3 vL = scal(cross3(g.ec, f3(uL[1], uL[2], uL[3])), __fdividef(-1.0f, uL[0]));
+  const F3 vR = scal(cross3(g.ec, f3(uR[1], uR[2], uR[3])), __fdividef(-1.0f, uR[0]));
   const float vnL = dot3(vL, g.en), vnR = dot3(vR, g.en);
   const float S_L = smin(vnL, vnR) - 1.f;
   const float S_R = smax(vnL, vnR) + 1.f;
@@ -210,7 +218,7 @@ __device__ __forceinline__ unsigned iso_flux_star(const float* uL, const float* 
 #pragma unroll
     for (int i = 0; i < kDim; ++i) F[i] = FL[i];
   } else if (S_L < 0 && S_R > 0) {
-    const float inv = 1.0f / (S_R - S_L);
+    const float inv = __fdividef(1.0f, S_R - S_L);
 #pragma unroll
     for (int i = 0; i < 4; ++i) F[i] = (S_R * FL[i] - S_L * FR[i] + S_R * S_L * (uR[i] - uL[i])) * inv;
     F[4] = 0.f;

@@ -381,15 +381,15 @@ __device__ __forceinline__ void recon_slot(const float* W, int fp, int f, int n,
   if (P.solver == kSolverIsoHLLE) {
     // isothermal: 4 fields, superbee limiter with the Courant factor
     // (a + v.n) dt arc / area (physics/isothermal.hpp:269-320)
-    const F3 vel = scal(cross3(ec, f3(w[1], w[2], w[3])), -1.0f / w[0]);
+    const F3 vel = scal(cross3(ec, f3(w[1], w[2], w[3])), __fdividef(-1.0f, w[0]));
     const float nu_plus = (1.f + dot3(vel, en)) * dt * arc_a;
     const float eta = sc.eta_m;
-    const float sb_scale = eta * 2.f / ((float)(2 * n) * nu_plus);
+    const float sb_scale = __fdividef(eta * 2.f, (float)(2 * n) * nu_plus);
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       const float pp = (bp0 * wa[k] + bp1 * wb[k] - w[k]) * ihp;
       const float pm = (w[k] - (bm0 * wc[k] + bm1 * wd[k])) * ihm;
-      const float lim = iso_limiter_field(pm / pp, eta, sb_scale);
+      const float lim = iso_limiter_field(__fdividef(pm, pp), eta, sb_scale);
       up[k] = w[k] + pp * lim * bmd;
     }
     up[4] = 0.f;
@@ -398,22 +398,22 @@ __device__ __forceinline__ void recon_slot(const float* W, int fp, int f, int n,
   const float* Wp = W + 4 * (size_t)fp;
   const float wp = Wp[f];
   const float gam = P.gam_f;
-  const float inv_rho = -1.0f / w[0];
-  const float c = sqrtf(gam * wp / w[0]);
+  const float inv_rho = __fdividef(-1.0f, w[0]);
+  const float c = sqrtf(__fdividef(gam * wp, w[0]));
   const F3 vel = scal(cross3(ec, f3(w[1], w[2], w[3])), inv_rho);
   const float nu_plus = (c + dot3(vel, en)) * dt * arc_a;
-  const float sb_scale = sc.eta_m / ((float)(2 * n) * nu_plus);
+  const float sb_scale = __fdividef(sc.eta_m, (float)(2 * n) * nu_plus);
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     const float pp = (bp0 * wa[k] + bp1 * wb[k] - w[k]) * ihp;
     const float pm = (w[k] - (bm0 * wc[k] + bm1 * wd[k])) * ihm;
-    const float lim = limiter_field(pm / pp, nu_plus, sc.eta_p, sb_scale);
+    const float lim = limiter_field(__fdividef(pm, pp), nu_plus, sc.eta_p, sb_scale);
     up[k] = w[k] + pp * lim * bmd;
   }
   {
     const float pp = (bp0 * Wp[ia] + bp1 * Wp[ib] - wp) * ihp;
     const float pm = (wp - (bm0 * Wp[ic] + bm1 * Wp[id])) * ihm;
-    const float lim = limiter_field(pm / pp, nu_plus, sc.eta_p, sb_scale);
+    const float lim = limiter_field(__fdividef(pm, pp), nu_plus, sc.eta_p, sb_scale);
     up[4] = wp + pp * lim * bmd;
   }
 }
@@ -447,10 +447,10 @@ __device__ __forceinline__ void edge_body(const DevGeomMixed& G, const DevState&
     sr.hh = reinterpret_cast<const float4*>(G.e_h)[G.epad + e];
   }
   // H+/BM and H-/BM from the distances: 1 / ((1/H) BM)
-  so.eta_p = 1.0f / (so.hh.x * so.hh.z);
-  so.eta_m = 1.0f / (so.hh.y * so.hh.z);
-  sr.eta_p = 1.0f / (sr.hh.x * sr.hh.z);
-  sr.eta_m = 1.0f / (sr.hh.y * sr.hh.z);
+  so.eta_p = __fdividef(1.0f, so.hh.x * so.hh.z);
+  so.eta_m = __fdividef(1.0f, so.hh.y * so.hh.z);
+  sr.eta_p = __fdividef(1.0f, sr.hh.x * sr.hh.z);
+  sr.eta_m = __fdividef(1.0f, sr.hh.y * sr.hh.z);
   griddep_wait();
   unsigned bits = 0;
   if (live) {
