@@ -11,7 +11,8 @@
 //     E = Pi/(gam-1) + Sigma |v|^2/2 (a sum of positive terms) where the flux
 //     needs it;
 //   * the unit edge centre is used without the |ec| ~ 1 rescale;
-//   * integer powers are multiplications and pow(1-r, 0.1) is exp(0.1 log);
+//   * integer powers are multiplications, pow(1-r, 0.1) is 2^(0.1 log2) and
+//     the switch's exponentials are powers of two (hardware ex2 / lg2);
 //   * quotients and reciprocals are __fdividef (the approximate reciprocal
 //     of the divisor times the dividend): within 2 ulp like the full-range
 //     division the path is compiled with otherwise, and equal to it for
@@ -42,6 +43,21 @@ __device__ __forceinline__ F3 cross3(F3 a, F3 b) {
   return F3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
 }
 __device__ __forceinline__ float smax(float a, float b) { return (a < b) ? b : a; }
+
+// 2^x and log2(x) as the hardware approximations (PTX ex2.approx.ftz,
+// lg2.approx.ftz); e^x = 2^(x log2 e) and x^m = 2^(m log2 x) are written in
+// base 2 so that no base conversion is evaluated at run time.
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float lg2_approx(float x) {
+  float y;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+constexpr float kLog2e = 1.4426950408889634f;
 __device__ __forceinline__ float smin(float a, float b) { return (b < a) ? b : a; }
 
 struct SlotGeomF {
@@ -173,7 +189,7 @@ __device__ __forceinline__ unsigned flux_star(const float* uL, const float* uR, 
     float f_star = 1.f;
     if (lambd == 0) f_star = __fdividef(M * sqrtf(4.f + (1.f - M * M) * (1.f - M * M)), 1.f + M * M);
     const float h = smin(__fdividef(L.p, R.p), __fdividef(R.p, L.p));
-    const float gsw = 1.f - __expf(M * __logf(h));
+    const float gsw = 1.f - ex2_approx(M * lg2_approx(h));
     const float dV = V_R - V_L;
     const F3 dv = sub(R.vel, L.vel);
     const float cs = Sk * inv * gsw;
@@ -251,9 +267,11 @@ __device__ __forceinline__ float iso_limiter_field(float r, float eta, float sb_
 __device__ __forceinline__ float limiter_switch(float r) {
   const bool lo = r < 1.f && r > 0.f;
   const bool hi = r >= 1.f;
-  const float y = 4.f * (r * r) * __expf(0.1f * __logf(lo ? 1.f - r : 1.f));
+  // 2y log2(e) and 20 x^3 log2(e), clamped at 80 log2(e): e^{2y} and
+  // e^{min(20 x^3, 80)} as powers of two
+  const float y2 = (8.f * kLog2e) * (r * r) * ex2_approx(0.1f * lg2_approx(lo ? 1.f - r : 1.f));
   const float x = r - 1.f;
-  const float e = __expf(lo ? 2.f * y : fminf(20.f * (x * x * x), 80.f));
+  const float e = ex2_approx(lo ? y2 : fminf((20.f * kLog2e) * (x * x * x), 80.f * kLog2e));
   const float q = __fdividef(1.f, 1.f + e);
   const float t = (e - 1.f) * q;
   const float t2 = t * t;
@@ -267,7 +285,7 @@ __device__ __forceinline__ float limiter_field(float r, float nu_plus, float eta
   const float sb = fmaxf(0.f, fmaxf(fminf(1.f, r * sb_scale), fminf(r, eta_p)));
   const float to = fmaxf(0.f, fminf(sb, 1.f + (1.f + nu_plus) * (1.f / 3.f) * (r - 1.f)));
   const float hv = limiter_switch(r);
-  return (1.f - hv) * to + hv * sb;
+  return to + hv * (sb - to);
 }
 
 // Neumaier-compensated FP32 accumulator: the sum of the FP32 terms is kept
