@@ -143,7 +143,7 @@ __device__ __forceinline__ void store_face_state(float* W32, int fp, int f, cons
 // level when the clip is active.  Returned as doubles for the keys.
 __device__ __forceinline__ void dt_candidates_f32(const float* w, F3 r, const PhysParams& P, double& vmax2,
                                                   double& dmin_sq) {
-  const float ir = 1.0f / w[0];
+  const float ir = __fdividef(1.0f, w[0]);
   const F3 c = cross3(r, f3(w[1], w[2], w[3]));
   const float v2 = dot3(c, c) * (ir * ir);
   const float vm = fmaxf(v2, P.gam_f * w[4] * ir);
@@ -162,13 +162,15 @@ __device__ __forceinline__ void dt_candidates_f32(const float* w, F3 r, const Ph
 
 // physics/adiabatic.hpp:396-541 in FP32, except the accretion mass source
 // (a geometric constant kept in FP64 and added by the caller).  w[4] = Pi.
+// Quotients are __fdividef like the edge path's (divisors: the floored
+// Sigma and Pi, 1 + C with C >= 0, C above the switch value).
 __device__ __forceinline__ void source_f32(const float* w, F3 fcn, float acc0, const PhysParams& P,
                                            float* res) {
 #pragma unroll
   for (int i = 0; i < kDim; ++i) res[i] = 0.f;
   if (!P.accretion_on) return;
   const float gam = P.gam_f;
-  const F3 vel = scal(cross3(fcn, f3(w[1], w[2], w[3])), -1.0f / w[0]);
+  const F3 vel = scal(cross3(fcn, f3(w[1], w[2], w[3])), __fdividef(-1.0f, w[0]));
   const F3 omega_acc = f3(P.omega_acc_f[0], P.omega_acc_f[1], P.omega_acc_f[2]);
   const F3 omxr = cross3(omega_acc, fcn);
   const F3 rxo = cross3(fcn, omxr);
@@ -185,7 +187,7 @@ __device__ __forceinline__ void source_f32(const float* w, F3 fcn, float acc0, c
     res[1] += dmdt * rxv.x;
     res[2] += dmdt * rxv.y;
     res[3] += dmdt * rxv.z;
-    res[4] += dmdt * (gam / (gam - 1.f) * w[4] / w[0] + 0.5f * v2);
+    res[4] += dmdt * (__fdividef(gam / (gam - 1.f) * w[4], w[0]) + 0.5f * v2);
   }
   const float GM = 0.217909f;
   const float g_eff = GM - v2;
@@ -193,14 +195,14 @@ __device__ __forceinline__ void source_f32(const float* w, F3 fcn, float acc0, c
   // so that no intermediate leaves the FP32 range
   const float k1 = (float)(12. / 5 * 1.6e-13);
   const float q = (float)(3. / 4 * 4.85e36) * 1e-36f;  // scaled by 1e-36, undone by 10^9 below
-  const float C = k1 * w[0] / w[4] * (sqrtf(sqrtf(q * g_eff * w[0])) * 1e9f);
+  const float C = __fdividef(k1 * w[0], w[4]) * (sqrtf(sqrtf(q * g_eff * w[0])) * 1e9f);
   const float beta_switch = 0.736194670678821f;
   const float C_switch = -1.f - 1.f / (beta_switch - 1.f);
   float beta;
   if (C <= C_switch) {
-    beta = 1.f - 1.f / (1.f + C);
+    beta = 1.f - __fdividef(1.f, 1.f + C);
   } else {
-    const float x = 2.f / C;
+    const float x = __fdividef(2.f, C);
     const float x2 = x * x;
     beta = 1.f - x2 * x2;
   }
@@ -210,7 +212,7 @@ __device__ __forceinline__ void source_f32(const float* w, F3 fcn, float acc0, c
   res[4] -= g_eff / 3.4e6f * (1.f - beta);
   if (P.friction_on) {
     const float gam3d = 1.f / (2.f - gam);
-    const float rho = gam3d / (2.f * gam3d - 1.f) * g_eff * w[0] * w[0] / w[4];
+    const float rho = __fdividef(gam3d / (2.f * gam3d - 1.f) * g_eff * w[0] * w[0], w[4]);
     const F3 vel0 = cross3(f3(0.f, 0.f, P.omega_ns_f), fcn);
     const F3 dv = sub(vel, vel0);
     const float dvn = norm3(dv);
@@ -222,10 +224,10 @@ __device__ __forceinline__ void source_f32(const float* w, F3 fcn, float acc0, c
     res[3] += l_fr.z;
     res[4] += dot3(wr, vel0);
     res[0] -= ar;
-    res[1] -= ar / w[0] * w[1];
-    res[2] -= ar / w[0] * w[2];
-    res[3] -= ar / w[0] * w[3];
-    res[4] -= ar * (0.5f * v2 + w[4] * gam / ((gam - 1.f) * w[0]));
+    res[1] -= __fdividef(ar, w[0]) * w[1];
+    res[2] -= __fdividef(ar, w[0]) * w[2];
+    res[3] -= __fdividef(ar, w[0]) * w[3];
+    res[4] -= ar * (0.5f * v2 + __fdividef(w[4] * gam, (gam - 1.f) * w[0]));
   }
 }
 
