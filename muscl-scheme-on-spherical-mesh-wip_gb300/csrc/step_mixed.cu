@@ -115,6 +115,39 @@ __device__ __forceinline__ void fold_candidates(double vmax2, double dmin, unsig
   }
 }
 
+// The same for launches of kBlock threads: the warps' keys meet in shared
+// memory and one atomic per key and block reaches the L2 (every warp folding
+// into the same two addresses serialised at the L2: 2.2 us of the stage-2
+// update on hex(7)).  All threads of the block must call it.  The batched
+// launches keep the per-warp fold: their warps belong to different members,
+// and a per-member fold within the block measured 1% slower.
+__device__ __forceinline__ void fold_candidates_block(double vmax2, double dmin, unsigned long long* keys) {
+  unsigned long long kmax = fpc::is_nan_bits(vmax2) ? 0ull : order_key(vmax2);
+  unsigned long long kmin = fpc::is_nan_bits(dmin) ? ~0ull : order_key(dmin);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long a = __shfl_down_sync(0xffffffffu, kmax, o);
+    const unsigned long long b = __shfl_down_sync(0xffffffffu, kmin, o);
+    kmax = a > kmax ? a : kmax;
+    kmin = b < kmin ? b : kmin;
+  }
+  __shared__ unsigned long long s_max[kBlock / 32], s_min[kBlock / 32];
+  if ((threadIdx.x & 31) == 0) {
+    s_max[threadIdx.x >> 5] = kmax;
+    s_min[threadIdx.x >> 5] = kmin;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int w = 1; w < kBlock / 32; ++w) {
+      kmax = s_max[w] > kmax ? s_max[w] : kmax;
+      kmin = s_min[w] < kmin ? s_min[w] : kmin;
+    }
+    atomicMax(&keys[0], kmax);
+    atomicMin(&keys[1], kmin);
+  }
+}
+
 // The FP32 face state (Sigma, l, Pi) of the FP64 state u of face f, stored
 // to W32 and returned in w: the pressure recovery Pi = (E - |r x l|^2 /
 // (2 Sigma)) (gam - 1), floored at 1e-16 (MUSCL_base.hpp:538), runs in
@@ -309,7 +342,7 @@ __global__ void __launch_bounds__(kBlock) scatter_prepare_kernel(const double* _
     }
     prepare_face(G, S, P, f, u, vmax, dmin);
   }
-  fold_candidates(vmax, dmin, S.keys);
+  fold_candidates_block(vmax, dmin, S.keys);
 }
 
 // initial keys: max |v|^2 starts at (1e-8)^2 and min extra dt at 1e20 (as
@@ -496,7 +529,7 @@ __global__ void __launch_bounds__(kBlock, 7) edge_kernel(DevGeomMixed G, DevStat
 // recovery (double-word FP32), the FP32 face state of the next stage, and in
 // stage 2 the new U and the dt candidates.  Every lane of the calling warp
 // must call it (the candidates fold per warp).
-template <int STAGE>
+template <int STAGE, bool BLOCK_FOLD = false>  // true: kBlock-thread launches of one solver
 __device__ __forceinline__ void update_body(const DevGeomMixed& G, const DevState& S, const PhysParams& P,
                                             int f) {
   const int fp = G.fpad;
@@ -573,13 +606,18 @@ __device__ __forceinline__ void update_body(const DevGeomMixed& G, const DevStat
       }
     }
   }
-  if (STAGE == 2) fold_candidates(vmax, dmin, S.keys);
+  if (STAGE == 2) {
+    if (BLOCK_FOLD)
+      fold_candidates_block(vmax, dmin, S.keys);
+    else
+      fold_candidates(vmax, dmin, S.keys);
+  }
 }
 
 template <int STAGE>
 __global__ void __launch_bounds__(kBlock) update_kernel(DevGeomMixed G, DevState S, PhysParams P) {
   griddep_launch_dependents();
-  update_body<STAGE>(G, S, P, blockIdx.x * blockDim.x + threadIdx.x);
+  update_body<STAGE, true>(G, S, P, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // ---------------------------------------------------------------- ensemble
