@@ -549,8 +549,8 @@ def run_ours(args):
     lt = mixed.launch_times(reps, DT0)
     ms64 = fp64.kernel_times(reps, DT0)
     # mean ms per launch of each kernel, and each kernel's ms per step
-    # (launches: finalize, edge 1, update 1, edge 2, update 2)
-    kern = {"finalize": lt[0], "edge": (lt[1] + lt[3]) / 2, "update": (lt[2] + lt[4]) / 2,
+    # (slots: dt clip (empty: the stage-1 edge launch clips dt), edge 1, update 1, edge 2, update 2)
+    kern = {"dt_clip_slot": lt[0], "edge": (lt[1] + lt[3]) / 2, "update": (lt[2] + lt[4]) / 2,
             "edge_stage1": lt[1], "edge_stage2": lt[3], "update_stage1": lt[2], "update_stage2": lt[4]}
     per_step = {"edge": lt[1] + lt[3], "update": lt[2] + lt[4]}
     kern64 = {"dt_reduce": ms64[0], "reconstruct": (ms64[1] + ms64[3]) / 2,
@@ -573,7 +573,7 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
         "config": {**workload_config(F, "mixed FP32/FP64"), "parallelism": f"replicas{world}",
                    "working_set_mb": round((geo_b + st_b) / 1e6, 1)},
-        "gpu_launches": 5 * args.steps,
+        "gpu_launches": 4 * args.steps,
         "e2e": {"value": F * e2e_steps / e2e_secs, "unit": METRIC, "h2d_bytes_per_step": bytes_io,
                 "d2h_bytes_per_step": bytes_io, "host_buffers": "pinned (page-locked) FP64 [F][5] arrays"},
         "fp64": {"value": value64, "ms_per_step": secs64 / args.steps * 1e3, "kernel_ms": kern64},

@@ -150,7 +150,9 @@ SPLASH_API int splash_synchronize(splash_solver* s);
 SPLASH_API int splash_stream(splash_solver* s, void** stream);
 /* Runs `reps` un-captured steps with CUDA events between the step's phases
  * and returns the mean device time per phase in milliseconds:
- * ms[0] dt reduction (finalize); FP64 path: ms[1] reconstruct (stage 1),
+ * ms[0] dt reduction (FP64 path; on the mixed path the stage-1 edge
+ * launch clips dt itself and ms[0] is an empty slot); FP64 path: ms[1]
+ * reconstruct (stage 1),
  * ms[2] flux+update (stage 1), ms[3] reconstruct (stage 2), ms[4]
  * flux+update (stage 2); mixed path: ms[1] edge (reconstruction + Riemann
  * flux, stage 1), ms[2] update (stage 1), ms[3] edge (stage 2), ms[4] update
@@ -159,10 +161,12 @@ SPLASH_API int splash_kernel_times(splash_solver* s, int reps, double dt0, doubl
 /* Mean device ms of every launch of one step over `reps` un-captured steps,
  * with a CUDA event between consecutive launches (which serialises the
  * step's programmatic overlap, so the sum exceeds the captured step's time).
- * Five launches on either path: mixed, finalize, edge (reconstruction +
- * Riemann flux, stage 1), update (stage 1), edge (stage 2), update
- * (stage 2); FP64, dt reduction, reconstruct, flux+update, reconstruct,
- * flux+update.  Writes min(cap, *count) values; *count = launches per step.
+ * Five slots on either path: mixed, the dt clip (an empty slot: the
+ * stage-1 edge launch clips dt itself, so a mixed step is four launches),
+ * edge (reconstruction + Riemann flux, stage 1), update (stage 1), edge
+ * (stage 2), update (stage 2); FP64, dt reduction, reconstruct,
+ * flux+update, reconstruct, flux+update.  Writes min(cap, *count) values;
+ * *count = 5.
  * The steps advance the state like do_step(dt0). */
 SPLASH_API int splash_launch_times(splash_solver* s, int reps, double dt0, double* ms, int cap, int* count);
 /* Device bytes held by the solver: out[0] geometry, out[1] state + scratch. */

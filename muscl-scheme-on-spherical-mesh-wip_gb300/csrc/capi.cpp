@@ -339,7 +339,7 @@ int Solver::capture_graph() {
       if (t != cudaGraphNodeTypeKernel) continue;
       cudaKernelNodeParams kp{};
       SPLASH_CUDA(cudaGraphKernelNodeGetParams(nd, &kp));
-      if (kp.func == mixed_finalize_kernel_ptr()) dt0_node = nd;
+      if (kp.func == mixed_dt0_kernel_ptr()) dt0_node = nd;
     }
     if (!dt0_node) return fail(SPLASH_E_CUDA, "dt node not found in the captured step");
     // the same step kGraphSteps times in one graph
@@ -366,7 +366,7 @@ int Solver::capture_graph() {
       if (t != cudaGraphNodeTypeKernel) continue;
       cudaKernelNodeParams kp{};
       SPLASH_CUDA(cudaGraphKernelNodeGetParams(nd, &kp));
-      if (kp.func == mixed_finalize_kernel_ptr()) dt0_nodes_k.push_back(nd);
+      if (kp.func == mixed_dt0_kernel_ptr()) dt0_nodes_k.push_back(nd);
     }
     if ((int)dt0_nodes_k.size() != kGraphSteps)
       return fail(SPLASH_E_CUDA, "dt nodes not found in the captured steps");
@@ -376,11 +376,11 @@ int Solver::capture_graph() {
 
 int Solver::set_graph_dt0(double dt0) {
   if (dt0 == graph_dt0) return SPLASH_OK;
-  // new dt0: rewrite the finalize nodes' arguments in the instantiated
+  // new dt0: rewrite the stage-1 edge nodes' arguments in the instantiated
   // graphs (takes effect from the next launch; launches in flight keep theirs)
   cudaKernelNodeParams kp{};
   SPLASH_CUDA(cudaGraphKernelNodeGetParams(dt0_node, &kp));
-  void* args[] = {&S, &P, &dt0};
+  void* args[] = {&GM, &S, &P, &dt0};
   kp.kernelParams = args;
   kp.extra = nullptr;
   SPLASH_CUDA(cudaGraphExecKernelNodeSetParams(graph_exec, dt0_node, &kp));

@@ -29,15 +29,17 @@ cudaError_t fp64_gather_state(const double* U, const int* iperm, double* aos, in
                               cudaStream_t st, int dim = kDim);
 
 // ---- FP32/FP64 mixed path (step_mixed.cu) ----
-// One do_step: the dt finalize (1 thread, argument dt0) then the four
-// stage launches.  Capturable; the finalize node's dt0 can be updated in an
-// instantiated graph (mixed_finalize_kernel_ptr identifies the node).
-// ev (optional): six events recorded on st around the step's five launches
-// (before the step, after finalize, after each stage's edge launch and
-// update launch); per_launch gives the same layout.
+// One do_step: four stage launches (edge, update per stage); the stage-1
+// edge launch (argument dt0) clips the step's dt from the keys the previous
+// stage-2 update (or set_state) folded, and the stage-1 update restarts
+// them.  Capturable; the stage-1 edge node's dt0 can be updated in an
+// instantiated graph (mixed_dt0_kernel_ptr identifies the node).
+// ev (optional): six events recorded on st (before the step, an empty dt
+// slot, after each stage's edge launch and update launch); per_launch gives
+// the same layout.
 cudaError_t mixed_step(const DevGeomMixed& G, const DevState& S, const PhysParams& P, double dt0,
                        cudaStream_t st, cudaEvent_t* ev = nullptr, bool per_launch = false);
-const void* mixed_finalize_kernel_ptr();
+const void* mixed_dt0_kernel_ptr();
 // set_state + prepare in one pass: aos is the caller's [n_faces][dim] array
 // in reference order (host memory the device can access, or device memory),
 // iperm maps reference to internal face indices.

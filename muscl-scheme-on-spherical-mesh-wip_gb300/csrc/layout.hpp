@@ -44,6 +44,7 @@ struct PhysParams {
   double gam_m1, fric_ak;  // gam - 1 and alpha * fric_k (mixed-path update)
   float gam_f, e_acc_f, alpha_f, omega_ns_f, fric_ak_f;
   float gam_m1_h, gam_m1_l;  // gam - 1 as a double-word (nearest float + residual)
+  float cfl_num_f;           // h0 * 0.1 rounded to a float (numerator of the CFL bound)
   float omega_acc_f[3];
   float depletion_f;     // -(acc_rate 4 pi) / total_mass (adiabatic.hpp:430-436)
 };
@@ -57,6 +58,7 @@ inline void derive_params(PhysParams& P) {
   P.fric_ak_f = (float)P.fric_ak;
   P.gam_m1_h = (float)P.gam_m1;
   P.gam_m1_l = (float)(P.gam_m1 - (double)P.gam_m1_h);
+  P.cfl_num_f = (float)(P.h0 * 0.1);
   P.gam_f = (float)P.gam;
   P.e_acc_f = (float)P.e_acc;
   P.alpha_f = (float)P.alpha;

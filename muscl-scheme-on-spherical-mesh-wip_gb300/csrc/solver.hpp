@@ -66,7 +66,7 @@ struct Solver {
   std::vector<void*> dev_allocs;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
-  cudaGraphNode_t dt0_node = nullptr;  // mixed path: the finalize node taking dt0
+  cudaGraphNode_t dt0_node = nullptr;  // mixed path: the stage-1 edge node taking dt0
   double graph_dt0 = 0.0;              // dt0 the instantiated graphs currently use
   // mixed path: kGraphSteps consecutive steps in one graph, so that each
   // step's first launch overlaps the previous step's last one (programmatic
@@ -92,10 +92,10 @@ struct Solver {
   int set_graph_dt0(double dt0);  // mixed path: rewrite dt0 in the instantiated graphs
   int steps_n(int n, double dt0);  // n steps (K-step graphs where they fit)
   int step(double dt0);
-  // one un-captured step; ev as for mixed_step (the FP64 step has five
-  // launches, so its two layouts coincide)
+  // one un-captured step; ev as for mixed_step (six events, five slots on
+  // both paths)
   cudaError_t launch_step(cudaEvent_t* ev, double dt0, bool per_launch = false);
-  int launches_per_step() const { return 5; }
+  int launches_per_step() const { return 5; }  // timing slots (the mixed step launches 4 kernels)
   cudaError_t launch_prepare();
   static int check_cuda(cudaError_t e, const char* what);
 };

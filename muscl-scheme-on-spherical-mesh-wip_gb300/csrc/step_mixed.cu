@@ -355,40 +355,77 @@ __global__ void reset_keys_kernel(unsigned long long* keys) {
 
 // dt = min(dt0, 0.1 h0 / max_vel, extra_dt) (MUSCL_base.hpp:100-115), time,
 // and a fresh start for the keys the step's stage-2 launch will fold into.
-__device__ __forceinline__ void finalize_body(const DevState& S, const PhysParams& P, double dt0) {
-  griddep_wait();
-  // the candidates are FP32 values (see dt_candidates_f32), so the clip is
-  // evaluated in FP32 and only the chosen bound is widened to FP64
-  const float max_vel_f = sqrtf(fpc::d2f(key_value(S.keys[0])));
-  const double max_vel = fpc::f2d(max_vel_f);
-  const double xs = key_value(S.keys[1]);
-  double extra = 1e20;
+// The step's dt from the two keys (the dt candidates folded by the previous
+// stage-2 update or by set_state): dt = min(dt0, 0.1 h0 / max_vel, extra_dt)
+// (MUSCL_base.hpp:100-115).  The candidates are FP32 values (see
+// dt_candidates_f32), so the clip is evaluated in FP32 and only the chosen
+// bound is widened to FP64.
+struct StepDt {
+  double dt, max_vel, extra;
+  bool neg_extra;
+};
+__device__ __forceinline__ StepDt clip_dt(const unsigned long long* keys, const PhysParams& P, double dt0) {
+  StepDt d;
+  const float max_vel_f = sqrtf(fpc::d2f(key_value(keys[0])));
+  d.max_vel = fpc::f2d(max_vel_f);
+  const double xs = key_value(keys[1]);
+  d.extra = 1e20;
   if (xs < kNoExtraSq) {
     const float xf = fpc::d2f(xs);
-    extra = fpc::f2d(xf < 0.f ? -sqrtf(-xf) : sqrtf(xf));
+    d.extra = fpc::f2d(xf < 0.f ? -sqrtf(-xf) : sqrtf(xf));
   }
-  if (extra < 0) {
-    atomicOr(S.err, 8u);  // SPLASH_STOP_NEG_EXTRA_DT
-    extra = 1e20;
-  }
-  const double cfl = fpc::f2d(fpc::d2f(P.h0 * 0.1) / max_vel_f);
-  double dt = dt0;
-  if (dt > cfl) dt = cfl;
-  if (dt > extra) dt = extra;
-  S.scal[kScDt] = dt;
-  S.scal[kScDtHalf] = dt / 2;
-  *reinterpret_cast<float2*>(S.scal + kScDtF) = make_float2((float)dt, (float)(dt / 2));
-  S.scal[kScDt0] = dt0;
-  S.scal[kScMaxVel] = max_vel;
-  S.scal[kScExtraDt] = extra;
-  S.scal[kScTime] = S.scal[kScTime] + dt;
-  S.keys[0] = order_key(1e-16);
-  S.keys[1] = order_key(kNoExtraSq);
+  d.neg_extra = d.extra < 0;
+  if (d.neg_extra) d.extra = 1e20;
+  const double cfl = fpc::f2d(P.cfl_num_f / max_vel_f);
+  d.dt = dt0;
+  if (d.dt > cfl) d.dt = cfl;
+  if (d.dt > d.extra) d.dt = d.extra;
+  return d;
 }
 
-__global__ void finalize_kernel(DevState S, PhysParams P, double dt0) {
-  griddep_launch_dependents();
-  finalize_body(S, P, dt0);
+// (float) clip_dt(...).dt without FP64 instructions, for every thread of a
+// launch: the bounds are FP32 values and rounding is monotone, so clipping
+// the rounded dt0 by the FP32 bounds gives the rounded clipped dt (NaN
+// bounds clip nothing in either form).
+__device__ __forceinline__ float clip_dt_f32(const unsigned long long* keys, const PhysParams& P, double dt0) {
+  const unsigned long long k0 = keys[0], k1 = keys[1];
+  const float max_vel_f = sqrtf(fpc::d2f(key_value(k0)));
+  float extra = 1e20f;
+  if (k1 < order_key(kNoExtraSq)) {
+    const float xf = fpc::d2f(key_value(k1));
+    extra = xf < 0.f ? -sqrtf(-xf) : sqrtf(xf);
+    if (extra < 0.f) extra = 1e20f;
+  }
+  const float cfl = P.cfl_num_f / max_vel_f;
+  float dt = fpc::d2f(dt0);
+  if (dt > cfl) dt = cfl;
+  if (dt > extra) dt = extra;
+  return dt;
+}
+
+// the step scalars of d: dt, dt/2 (FP64 and FP32), dt0, the bounds, time
+__device__ __forceinline__ void publish_dt(const DevState& S, const StepDt& d, double dt0) {
+  if (d.neg_extra) atomicOr(S.err, 8u);  // SPLASH_STOP_NEG_EXTRA_DT
+  S.scal[kScDt] = d.dt;
+  S.scal[kScDtHalf] = d.dt / 2;
+  *reinterpret_cast<float2*>(S.scal + kScDtF) = make_float2((float)d.dt, (float)(d.dt / 2));
+  S.scal[kScDt0] = dt0;
+  S.scal[kScMaxVel] = d.max_vel;
+  S.scal[kScExtraDt] = d.extra;
+  S.scal[kScTime] = S.scal[kScTime] + d.dt;
+}
+
+// fresh keys for the next fold
+__device__ __forceinline__ void restart_keys(unsigned long long* keys) {
+  keys[0] = order_key(1e-16);
+  keys[1] = order_key(kNoExtraSq);
+}
+
+// One thread: dt, the scalars and fresh keys (the batched launches).
+__device__ __forceinline__ void finalize_body(const DevState& S, const PhysParams& P, double dt0) {
+  griddep_wait();
+  publish_dt(S, clip_dt(S.keys, P, dt0), dt0);
+  restart_keys(S.keys);
 }
 
 // find_U_edges (MUSCL_base.hpp:361-434) in FP32 for one slot: the edge
@@ -463,9 +500,13 @@ __device__ __forceinline__ void recon_slot(const float* W, int fp, int f, int n,
 // from its neighbour.  The edge states never go to memory, except in stage 2
 // when the state has an edge-state buffer (edge-major, for the writers that
 // read the last stage's edge states; batched instances have none).
-// Stop bits are folded per warp.
-template <int STAGE>
-__device__ __forceinline__ void edge_body(const DevGeomMixed& G, const DevState& S, const PhysParams& P, int e) {
+// Stop bits are folded per warp.  With OWN_DT (the stage-1 launch of one
+// solver) every thread clips its step's dt from the keys itself and the
+// first thread publishes the step scalars; otherwise dt comes from the
+// scalars.
+template <int STAGE, bool OWN_DT>
+__device__ __forceinline__ void edge_body(const DevGeomMixed& G, const DevState& S, const PhysParams& P, int e,
+                                          double dt0) {
   const bool live = e < G.n_edges;
   int4 ids = make_int4(0, 0, 0, 0);
   float4 ce = make_float4(0.f, 0.f, 0.f, 0.f), ne = ce;
@@ -487,9 +528,15 @@ __device__ __forceinline__ void edge_body(const DevGeomMixed& G, const DevState&
   sr.eta_p = __fdividef(1.0f, sr.hh.x * sr.hh.z);
   sr.eta_m = __fdividef(1.0f, sr.hh.y * sr.hh.z);
   griddep_wait();
+  float dt;
+  if (OWN_DT) {
+    dt = clip_dt_f32(S.keys, P, dt0);
+    if (e == 0) publish_dt(S, clip_dt(S.keys, P, dt0), dt0);
+  } else {
+    dt = reinterpret_cast<const float2*>(S.scal + kScDtF)->x;
+  }
   unsigned bits = 0;
   if (live) {
-    const float dt = reinterpret_cast<const float2*>(S.scal + kScDtF)->x;
     SlotGeomF g;
     g.ec = f3(ce.x, ce.y, ce.z);
     g.en = f3(ne.x, ne.y, ne.z);
@@ -515,9 +562,9 @@ __device__ __forceinline__ void edge_body(const DevGeomMixed& G, const DevState&
 // at most 73 registers (7 blocks of 128 per SM; a small spill, measured best
 // of 5 to 8 blocks)
 template <int STAGE>
-__global__ void __launch_bounds__(kBlock, 7) edge_kernel(DevGeomMixed G, DevState S, PhysParams P) {
+__global__ void __launch_bounds__(kBlock, 7) edge_kernel(DevGeomMixed G, DevState S, PhysParams P, double dt0) {
   griddep_launch_dependents();
-  edge_body<STAGE>(G, S, P, blockIdx.x * blockDim.x + threadIdx.x);
+  edge_body<STAGE, STAGE == 1>(G, S, P, blockIdx.x * blockDim.x + threadIdx.x, dt0);
 }
 
 // res2d + RK combine (MUSCL_base.hpp:238-276, 124-161) of face f: the
@@ -529,7 +576,10 @@ __global__ void __launch_bounds__(kBlock, 7) edge_kernel(DevGeomMixed G, DevStat
 // recovery (double-word FP32), the FP32 face state of the next stage, and in
 // stage 2 the new U and the dt candidates.  Every lane of the calling warp
 // must call it (the candidates fold per warp).
-template <int STAGE, bool BLOCK_FOLD = false>  // true: kBlock-thread launches of one solver
+// BLOCK_FOLD: kBlock-thread launches of one solver; RESTART_KEYS: the
+// stage-1 update of one solver gives the keys a fresh start (the stage-1
+// edge launch that read them has completed)
+template <int STAGE, bool BLOCK_FOLD = false, bool RESTART_KEYS = false>
 __device__ __forceinline__ void update_body(const DevGeomMixed& G, const DevState& S, const PhysParams& P,
                                             int f) {
   const int fp = G.fpad;
@@ -552,6 +602,7 @@ __device__ __forceinline__ void update_body(const DevGeomMixed& G, const DevStat
     co[j] = (j < n) ? G.coef[j * fp + f] : 0.f;
   }
   griddep_wait();
+  if (RESTART_KEYS && f == 0) restart_keys(S.keys);
   double vmax = 0.0, dmin = kNoExtraSq;
   if (live) {
     const float2 dtf2 = *reinterpret_cast<const float2*>(S.scal + kScDtF);
@@ -617,7 +668,7 @@ __device__ __forceinline__ void update_body(const DevGeomMixed& G, const DevStat
 template <int STAGE>
 __global__ void __launch_bounds__(kBlock) update_kernel(DevGeomMixed G, DevState S, PhysParams P) {
   griddep_launch_dependents();
-  update_body<STAGE, true>(G, S, P, blockIdx.x * blockDim.x + threadIdx.x);
+  update_body<STAGE, true, STAGE == 1>(G, S, P, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // ---------------------------------------------------------------- ensemble
@@ -658,7 +709,7 @@ __global__ void __launch_bounds__(kBlock, 7) ens_edge_kernel(const EnsInstance* 
   if (tile >= n_tiles) return;  // whole warps: stop bits fold per warp
   const int2 t = tiles[tile];
   const EnsInstance& I = inst[t.x];
-  edge_body<STAGE>(I.G, I.S, I.P, t.y + (threadIdx.x & 31));
+  edge_body<STAGE, false>(I.G, I.S, I.P, t.y + (threadIdx.x & 31), 0.0);
 }
 
 // update: one 32-face tile per warp
@@ -678,7 +729,7 @@ inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
 }  // namespace
 }  // namespace mx
 
-const void* mixed_finalize_kernel_ptr() { return (const void*)mx::finalize_kernel; }
+const void* mixed_dt0_kernel_ptr() { return (const void*)mx::edge_kernel<1>; }
 
 cudaError_t mixed_scatter_prepare(const double* aos, const int* iperm, const DevGeomMixed& G, const DevState& S,
                                   const PhysParams& P, int dim, cudaStream_t st) {
@@ -709,21 +760,22 @@ cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStre
 }  // namespace
 
 cudaError_t mixed_step(const DevGeomMixed& G, const DevState& S, const PhysParams& P, double dt0,
-                       cudaStream_t st, cudaEvent_t* ev, bool /*per_launch: five launches, same layout*/) {
+                       cudaStream_t st, cudaEvent_t* ev, bool /*per_launch: four launches, same layout*/) {
   const dim3 egrid(mx::blocks_for(G.n_edges));
   const dim3 ugrid(mx::blocks_for(G.n_faces));
   cudaError_t e = cudaSuccess;
   auto chk = [&](cudaError_t r) {
     if (e == cudaSuccess) e = r;
   };
+  // ev[0]..ev[1] is the (empty) slot of the dt clip, which the stage-1 edge
+  // launch evaluates itself
   if (ev) cudaEventRecord(ev[0], st);
-  chk(launch_pdl(mx::finalize_kernel, dim3(1), dim3(1), st, S, P, dt0));
   if (ev) cudaEventRecord(ev[1], st);
-  chk(launch_pdl(mx::edge_kernel<1>, egrid, dim3(mx::kBlock), st, G, S, P));
+  chk(launch_pdl(mx::edge_kernel<1>, egrid, dim3(mx::kBlock), st, G, S, P, dt0));
   if (ev) cudaEventRecord(ev[2], st);
   chk(launch_pdl(mx::update_kernel<1>, ugrid, dim3(mx::kBlock), st, G, S, P));
   if (ev) cudaEventRecord(ev[3], st);
-  chk(launch_pdl(mx::edge_kernel<2>, egrid, dim3(mx::kBlock), st, G, S, P));
+  chk(launch_pdl(mx::edge_kernel<2>, egrid, dim3(mx::kBlock), st, G, S, P, dt0));
   if (ev) cudaEventRecord(ev[4], st);
   chk(launch_pdl(mx::update_kernel<2>, ugrid, dim3(mx::kBlock), st, G, S, P));
   if (ev) cudaEventRecord(ev[5], st);
