@@ -1,11 +1,13 @@
 // FP32/FP64 mixed-precision kernels of the MUSCL time step.
 //
-// Same launch structure as the FP64 path (dt clip, then per stage a
-// reconstruction and a flux + update launch), with the work split:
+// One step is four launches: per stage an edge launch (reconstruction of
+// both slots of every interior edge and one Riemann flux per edge; the
+// stage-1 launch also clips the step's dt) and a per-face update launch.
+// The batched (ensemble) launches add a dt finalize per step.  Work split:
 //   FP32: slopes and limiter, edge states, Riemann fluxes, source terms,
-//         the per-slot flux contributions;
-//   FP64: the conserved state U, the RK combine U0 + dt*Phi, the CFL / extra
-//         dt reduction, simulation time, and the accretion mass source;
+//         the per-slot flux contributions, the dt candidates;
+//   FP64: the conserved state U, the RK combine U0 + dt*Phi, the dt and
+//         simulation time, and the accretion mass source;
 //   double-word FP32 (FP32 pairs, dword.cuh): the pressure recovery
 //         Pi = (E - |r x l|^2 / (2 Sigma)) (gam - 1);
 //   compensated: the per-face sum of the FP32 contributions is carried as an
