@@ -623,7 +623,11 @@ def run_reference(args):
 
     cores = os.cpu_count() or 1
     o = Oracle(geom, U0, gam, 0.0, True, sg.SolverParams(**PARAMS).as_list(), 3, threads=cores)
-    for _ in range(min(args.warmup, 1)):
+    # at least 3 warm-up steps like the GPU arm (a hex(7) oracle step takes
+    # tens of ms on the host cores), at most 10; a bounded sample of at most
+    # 10 timed steps
+    warm = max(3, min(args.warmup, 10))
+    for _ in range(warm):
         o.do_step(DT0)
     n = max(1, min(args.steps, 10))
     t0 = time.perf_counter()
@@ -632,7 +636,7 @@ def run_reference(args):
     value = geom.n_faces * n / secs
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 0,
-        "steps": n, "warmup": min(args.warmup, 1), "ms_per_step": secs / n * 1e3,
+        "steps": n, "warmup": warm, "ms_per_step": secs / n * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "config": workload_config(geom.n_faces, "fp64"),
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": "port",
