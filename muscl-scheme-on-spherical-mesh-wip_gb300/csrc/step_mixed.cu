@@ -170,7 +170,7 @@ __device__ __forceinline__ void store_face_state(float* W32, int fp, int f, cons
 // extra_dt_constr (physics/adiabatic.hpp:543-580), d = A / (B |v - v0|) with
 // A = 0.01 Pi, B = alpha k g_eff Sigma, k = gam3d / (2 gam3d - 1), reduced as
 // the signed square sgn(B) A^2 / (B^2 |v - v0|^2) (x |x| is increasing, so
-// the minimum is the same; the finalize takes one square root).  The sign
+// the minimum is the same; the dt clip takes one square root).  The sign
 // comes from B's sign bit, so zero denominators give the direct quotient's
 // signed infinities; a bound past the FP32 range (d above ~1.8e19) reads as
 // no bound, like the initial 1e20.  Both candidates carry FP32 rounding

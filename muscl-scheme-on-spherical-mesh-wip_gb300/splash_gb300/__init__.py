@@ -367,9 +367,10 @@ class Solver:
         return out
 
     def launch_times(self, reps: int, dt0: float) -> np.ndarray:
-        """Mean device ms of every launch of one step (mixed: finalize, edge 1,
-        update 1, edge 2, update 2; FP64: dt, recon1, flux1, recon2, flux2),
-        with events between launches."""
+        """Mean device ms of every timing slot of one step (mixed: the dt clip
+        (an empty slot: the stage-1 edge launch clips dt), edge 1, update 1,
+        edge 2, update 2; FP64: dt, recon1, flux1, recon2, flux2), with events
+        between launches."""
         out = np.zeros(8)
         n = C.c_int(0)
         _check(self._lib.splash_launch_times(self.handle, reps, dt0, _dptr(out), 8, C.byref(n)))
