@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "diagnostics.hpp"
+#include "fp_convert.cuh"
 #include "geometry.hpp"
 #include "hilbert.hpp"
 #include "kernels.hpp"
@@ -380,7 +381,8 @@ int Solver::set_graph_dt0(double dt0) {
   // graphs (takes effect from the next launch; launches in flight keep theirs)
   cudaKernelNodeParams kp{};
   SPLASH_CUDA(cudaGraphKernelNodeGetParams(dt0_node, &kp));
-  void* args[] = {&GM, &S, &P, &dt0};
+  float dt0f = splash::fpc::d2f(dt0);
+  void* args[] = {&GM, &S, &P, &dt0, &dt0f};
   kp.kernelParams = args;
   kp.extra = nullptr;
   SPLASH_CUDA(cudaGraphExecKernelNodeSetParams(graph_exec, dt0_node, &kp));

@@ -288,16 +288,16 @@ __device__ __forceinline__ float limiter_field(float r, float nu_plus, float eta
   return to + hv * (sb - to);
 }
 
-// Neumaier-compensated FP32 accumulator: the sum of the FP32 terms is kept
-// as hi + lo (about twice FP32 precision) and folded into FP64 at the end.
+// Compensated FP32 accumulator (Neumaier's scheme): the sum of the FP32
+// terms is kept as hi + lo (about twice FP32 precision) and folded into FP64
+// at the end.  Each addition's exact rounding error comes from Knuth's
+// branch-free TwoSum, the same value Neumaier's magnitude test selects.
 struct Acc {
   float hi, lo;
   __device__ __forceinline__ void add(float x) {
     const float t = hi + x;
-    if (fabsf(hi) >= fabsf(x))
-      lo += (hi - t) + x;
-    else
-      lo += (x - t) + hi;
+    const float xx = t - hi;
+    lo += (hi - (t - xx)) + (x - xx);
     hi = t;
   }
 };

@@ -386,10 +386,11 @@ __device__ __forceinline__ StepDt clip_dt(const unsigned long long* keys, const 
 }
 
 // (float) clip_dt(...).dt without FP64 instructions, for every thread of a
-// launch: the bounds are FP32 values and rounding is monotone, so clipping
-// the rounded dt0 by the FP32 bounds gives the rounded clipped dt (NaN
-// bounds clip nothing in either form).
-__device__ __forceinline__ float clip_dt_f32(const unsigned long long* keys, const PhysParams& P, double dt0) {
+// launch, from dt0f = dt0 rounded to the nearest float (fpc::d2f): the
+// bounds are FP32 values and rounding is monotone, so clipping the rounded
+// dt0 by the FP32 bounds gives the rounded clipped dt (NaN bounds clip
+// nothing in either form).
+__device__ __forceinline__ float clip_dt_f32(const unsigned long long* keys, const PhysParams& P, float dt0f) {
   const unsigned long long k0 = keys[0], k1 = keys[1];
   const float max_vel_f = sqrtf(fpc::d2f(key_value(k0)));
   float extra = 1e20f;
@@ -399,7 +400,7 @@ __device__ __forceinline__ float clip_dt_f32(const unsigned long long* keys, con
     if (extra < 0.f) extra = 1e20f;
   }
   const float cfl = P.cfl_num_f / max_vel_f;
-  float dt = fpc::d2f(dt0);
+  float dt = dt0f;
   if (dt > cfl) dt = cfl;
   if (dt > extra) dt = extra;
   return dt;
@@ -508,7 +509,7 @@ __device__ __forceinline__ void recon_slot(const float* W, int fp, int f, int n,
 // scalars.
 template <int STAGE, bool OWN_DT>
 __device__ __forceinline__ void edge_body(const DevGeomMixed& G, const DevState& S, const PhysParams& P, int e,
-                                          double dt0) {
+                                          double dt0, float dt0f) {
   const bool live = e < G.n_edges;
   int4 ids = make_int4(0, 0, 0, 0);
   float4 ce = make_float4(0.f, 0.f, 0.f, 0.f), ne = ce;
@@ -532,7 +533,7 @@ __device__ __forceinline__ void edge_body(const DevGeomMixed& G, const DevState&
   griddep_wait();
   float dt;
   if (OWN_DT) {
-    dt = clip_dt_f32(S.keys, P, dt0);
+    dt = clip_dt_f32(S.keys, P, dt0f);
     if (e == 0) publish_dt(S, clip_dt(S.keys, P, dt0), dt0);
   } else {
     dt = reinterpret_cast<const float2*>(S.scal + kScDtF)->x;
@@ -564,9 +565,10 @@ __device__ __forceinline__ void edge_body(const DevGeomMixed& G, const DevState&
 // at most 73 registers (7 blocks of 128 per SM; a small spill, measured best
 // of 5 to 8 blocks)
 template <int STAGE>
-__global__ void __launch_bounds__(kBlock, 7) edge_kernel(DevGeomMixed G, DevState S, PhysParams P, double dt0) {
+__global__ void __launch_bounds__(kBlock, 7) edge_kernel(DevGeomMixed G, DevState S, PhysParams P, double dt0,
+                                                         float dt0f) {
   griddep_launch_dependents();
-  edge_body<STAGE, STAGE == 1>(G, S, P, blockIdx.x * blockDim.x + threadIdx.x, dt0);
+  edge_body<STAGE, STAGE == 1>(G, S, P, blockIdx.x * blockDim.x + threadIdx.x, dt0, dt0f);
 }
 
 // res2d + RK combine (MUSCL_base.hpp:238-276, 124-161) of face f: the
@@ -711,7 +713,7 @@ __global__ void __launch_bounds__(kBlock, 7) ens_edge_kernel(const EnsInstance* 
   if (tile >= n_tiles) return;  // whole warps: stop bits fold per warp
   const int2 t = tiles[tile];
   const EnsInstance& I = inst[t.x];
-  edge_body<STAGE, false>(I.G, I.S, I.P, t.y + (threadIdx.x & 31), 0.0);
+  edge_body<STAGE, false>(I.G, I.S, I.P, t.y + (threadIdx.x & 31), 0.0, 0.f);
 }
 
 // update: one 32-face tile per warp
@@ -773,11 +775,12 @@ cudaError_t mixed_step(const DevGeomMixed& G, const DevState& S, const PhysParam
   // launch evaluates itself
   if (ev) cudaEventRecord(ev[0], st);
   if (ev) cudaEventRecord(ev[1], st);
-  chk(launch_pdl(mx::edge_kernel<1>, egrid, dim3(mx::kBlock), st, G, S, P, dt0));
+  const float dt0f = fpc::d2f(dt0);
+  chk(launch_pdl(mx::edge_kernel<1>, egrid, dim3(mx::kBlock), st, G, S, P, dt0, dt0f));
   if (ev) cudaEventRecord(ev[2], st);
   chk(launch_pdl(mx::update_kernel<1>, ugrid, dim3(mx::kBlock), st, G, S, P));
   if (ev) cudaEventRecord(ev[3], st);
-  chk(launch_pdl(mx::edge_kernel<2>, egrid, dim3(mx::kBlock), st, G, S, P, dt0));
+  chk(launch_pdl(mx::edge_kernel<2>, egrid, dim3(mx::kBlock), st, G, S, P, dt0, dt0f));
   if (ev) cudaEventRecord(ev[4], st);
   chk(launch_pdl(mx::update_kernel<2>, ugrid, dim3(mx::kBlock), st, G, S, P));
   if (ev) cudaEventRecord(ev[5], st);
