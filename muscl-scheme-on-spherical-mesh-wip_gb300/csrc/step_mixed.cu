@@ -34,7 +34,6 @@ namespace mx {
 namespace {
 
 constexpr int kBlock = 128;
-constexpr int kFaceTile = 32;  // faces (or edges) per tile of the batched launches
 // slot bound of the mixed path: solvers and ensembles reject meshes with
 // faces of more than 8 edges at creation
 constexpr int kMaxFaceSlots = 8;
