@@ -528,7 +528,7 @@ int splash_create(const splash_mesh_desc* mesh, const double* U_in, int dim, dou
     }
     S.scal = s->dalloc<double>(splash::kScCount);
     S.err = s->dalloc<unsigned int>(4);
-    S.keys = s->dalloc<unsigned long long>(2);
+    S.keys = s->dalloc<unsigned>(2);
     s->d_stage = s->dalloc<double>((size_t)s->n_faces * dim);
     s->d_perm = s->upload(s->perm);
     s->d_iperm = s->upload(s->iperm);

@@ -64,7 +64,7 @@ struct Ensemble {
   double *U = nullptr, *acc = nullptr, *scal = nullptr, *U_snap = nullptr, *scal_snap = nullptr;
   float *W32 = nullptr, *fe32 = nullptr;
   unsigned int *err = nullptr, *err_snap = nullptr;
-  unsigned long long* keys = nullptr;
+  unsigned* keys = nullptr;
   int2 *d_ftiles = nullptr, *d_etiles = nullptr;
   int n_ftiles = 0, n_etiles = 0;
   int order = 0, recon_width = 128;  // tile order; threads per block of the edge launch
@@ -336,7 +336,7 @@ int splash_ensemble_create(const splash_member* members, int n, int device, int 
     e->scal_snap = e->dalloc<double>((size_t)n * kScCount);
     e->err = e->dalloc<unsigned int>((size_t)n * 4);
     e->err_snap = e->dalloc<unsigned int>((size_t)n * 4);
-    e->keys = e->dalloc<unsigned long long>((size_t)n * 2);
+    e->keys = e->dalloc<unsigned>((size_t)n * 2);
     ENS_CUDA(cudaMemset(e->U, 0, faces * kDim * sizeof(double)));
     ENS_CUDA(cudaMemset(e->W32, 0, faces * kDim * sizeof(float)));
     ENS_CUDA(cudaMemset(e->scal, 0, (size_t)n * kScCount * sizeof(double)));

@@ -136,7 +136,7 @@ struct DevState {
   double* partial;  // per-block partial records (kPartialStride doubles)
   double* scal;   // device scalars, see ScalarSlot
   unsigned int* err;  // stop bits
-  unsigned long long* keys;  // mixed path: [0] max |v|^2 key, [1] min extra-dt key
+  unsigned* keys;  // mixed path: [0] max |v|^2 key, [1] min signed-square extra-dt key (FP32 order keys)
 };
 
 // One member of an ensemble: its mesh level's geometry (shared between

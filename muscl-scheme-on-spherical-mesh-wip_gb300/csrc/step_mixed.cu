@@ -84,29 +84,31 @@ __device__ __forceinline__ void st5(float* base, int n, int i, const float* v) {
 // The min key holds the signed square of the extra dt; 1e40 = (1e20)^2 is
 // the reference's initial extra dt (adiabatic.hpp:545) and the isothermal
 // solver's only candidate (isothermal.hpp:262-267).
-constexpr double kNoExtraSq = 1e40;
+constexpr float kNoBound = __builtin_huge_valf();  // +inf: no extra-dt bound
+// the initial max |v|^2, (1e-8)^2 (MUSCL_base.hpp:314) rounded to a float
+constexpr float kMinVel2 = (float)1e-16;
 
-// Order-preserving 64-bit keys of doubles: unsigned comparison of the keys
-// orders the values, so the dt clip's max and min are exact integer
-// atomics (no FP64 work, independent of the reduction order).
-__device__ __forceinline__ unsigned long long order_key(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+// Order-preserving 32-bit keys of the FP32 dt candidates: unsigned
+// comparison of the keys orders the values, so the dt clip's max and min
+// are exact integer atomics (no FP64 work, independent of the reduction
+// order).
+__device__ __forceinline__ unsigned order_key(float x) {
+  const unsigned b = __float_as_uint(x);
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
 }
-__device__ __forceinline__ double key_value(unsigned long long k) {
-  const unsigned long long b = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
-  return __longlong_as_double((long long)b);
+__device__ __forceinline__ float key_value(unsigned k) {
+  return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
 }
 
 // Warp-reduces the dt candidates (NaN ignored, like the reference's
 // comparisons) and folds them into the global keys with one atomic each.
-__device__ __forceinline__ void fold_candidates(double vmax2, double dmin, unsigned long long* keys) {
-  unsigned long long kmax = fpc::is_nan_bits(vmax2) ? 0ull : order_key(vmax2);
-  unsigned long long kmin = fpc::is_nan_bits(dmin) ? ~0ull : order_key(dmin);
+__device__ __forceinline__ void fold_candidates(float vmax2, float dmin, unsigned* keys) {
+  unsigned kmax = isnan(vmax2) ? 0u : order_key(vmax2);
+  unsigned kmin = isnan(dmin) ? ~0u : order_key(dmin);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long a = __shfl_down_sync(0xffffffffu, kmax, o);
-    const unsigned long long b = __shfl_down_sync(0xffffffffu, kmin, o);
+    const unsigned a = __shfl_down_sync(0xffffffffu, kmax, o);
+    const unsigned b = __shfl_down_sync(0xffffffffu, kmin, o);
     kmax = a > kmax ? a : kmax;
     kmin = b < kmin ? b : kmin;
   }
@@ -122,17 +124,17 @@ __device__ __forceinline__ void fold_candidates(double vmax2, double dmin, unsig
 // update on hex(7)).  All threads of the block must call it.  The batched
 // launches keep the per-warp fold: their warps belong to different members,
 // and a per-member fold within the block measured 1% slower.
-__device__ __forceinline__ void fold_candidates_block(double vmax2, double dmin, unsigned long long* keys) {
-  unsigned long long kmax = fpc::is_nan_bits(vmax2) ? 0ull : order_key(vmax2);
-  unsigned long long kmin = fpc::is_nan_bits(dmin) ? ~0ull : order_key(dmin);
+__device__ __forceinline__ void fold_candidates_block(float vmax2, float dmin, unsigned* keys) {
+  unsigned kmax = isnan(vmax2) ? 0u : order_key(vmax2);
+  unsigned kmin = isnan(dmin) ? ~0u : order_key(dmin);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long a = __shfl_down_sync(0xffffffffu, kmax, o);
-    const unsigned long long b = __shfl_down_sync(0xffffffffu, kmin, o);
+    const unsigned a = __shfl_down_sync(0xffffffffu, kmax, o);
+    const unsigned b = __shfl_down_sync(0xffffffffu, kmin, o);
     kmax = a > kmax ? a : kmax;
     kmin = b < kmin ? b : kmin;
   }
-  __shared__ unsigned long long s_max[kBlock / 32], s_min[kBlock / 32];
+  __shared__ unsigned s_max[kBlock / 32], s_min[kBlock / 32];
   if ((threadIdx.x & 31) == 0) {
     s_max[threadIdx.x >> 5] = kmax;
     s_min[threadIdx.x >> 5] = kmin;
@@ -174,9 +176,9 @@ __device__ __forceinline__ void store_face_state(float* W32, int fp, int f, cons
 // signed infinities; a bound past the FP32 range (d above ~1.8e19) reads as
 // no bound, like the initial 1e20.  Both candidates carry FP32 rounding
 // (~1e-7 relative), so the mixed path's dt follows the FP64 path's to that
-// level when the clip is active.  Returned as doubles for the keys.
-__device__ __forceinline__ void dt_candidates_f32(const float* w, F3 r, const PhysParams& P, double& vmax2,
-                                                  double& dmin_sq) {
+// level when the clip is active.
+__device__ __forceinline__ void dt_candidates_f32(const float* w, F3 r, const PhysParams& P, float& vmax2,
+                                                  float& dmin_sq) {
   const float ir = __fdividef(1.0f, w[0]);
   const F3 c = cross3(r, f3(w[1], w[2], w[3]));
   const float v2 = dot3(c, c) * (ir * ir);
@@ -190,8 +192,8 @@ __device__ __forceinline__ void dt_candidates_f32(const float* w, F3 r, const Ph
   const float A = 0.01f * w[4];
   const float B = P.fric_ak_f * g_eff * w[0];
   const float q = (A * A) / ((B * B) * d2);
-  vmax2 = fpc::f2d(vm);
-  dmin_sq = fpc::f2d(signbit(B) ? -q : q);
+  vmax2 = vm;
+  dmin_sq = signbit(B) ? -q : q;
 }
 
 // physics/adiabatic.hpp:396-541 in FP32, except the accretion mass source
@@ -269,18 +271,18 @@ __device__ __forceinline__ void source_f32(const float* w, F3 fcn, float acc0, c
 // the CFL candidate is max(|v|^2, a^2) with a = 1 (find_v_max with the
 // isothermal sound speed); no extra constraint (isothermal.hpp:262-267).
 __device__ __forceinline__ void iso_w32_candidates(const double* u, F3 r, float* W32, int fp, int f,
-                                                   double& vmax2, double& dmin) {
+                                                   float& vmax2, float& dmin) {
   const float v[kDim] = {fpc::d2f(u[0]), fpc::d2f(u[1]), fpc::d2f(u[2]), fpc::d2f(u[3]), 0.f};
   st5(W32, fp, f, v);
   const float ir = 1.0f / v[0];
   const F3 c = cross3(r, f3(v[1], v[2], v[3]));
-  vmax2 = fpc::f2d(fmaxf(dot3(c, c) * (ir * ir), 1.f));
-  dmin = kNoExtraSq;
+  vmax2 = fmaxf(dot3(c, c) * (ir * ir), 1.f);
+  dmin = kNoBound;
 }
 
 // W32 and the dt candidates of the state u of internal face f
 __device__ __forceinline__ void prepare_face(const DevGeomMixed& G, const DevState& S, const PhysParams& P, int f,
-                                             const double* u, double& vmax, double& dmin) {
+                                             const double* u, float& vmax, float& dmin) {
   const F3 r32 = plane3f(G.fcn32, G.fpad, f);
   if (P.solver == kSolverIsoHLLE) {
     iso_w32_candidates(u, r32, S.W32, G.fpad, f, vmax, dmin);
@@ -295,7 +297,7 @@ __device__ __forceinline__ void prepare_face(const DevGeomMixed& G, const DevSta
 // warp call it; lanes past the last face contribute neutral values).
 __device__ __forceinline__ void prepare_body(const DevGeomMixed& G, const DevState& S,
                                              const PhysParams& P, int f) {
-  double vmax = 0.0, dmin = kNoExtraSq;
+  float vmax = 0.f, dmin = kNoBound;
   if (f < G.n_faces) {
     double u[kDim];
 #pragma unroll
@@ -331,7 +333,7 @@ __global__ void __launch_bounds__(kBlock) scatter_prepare_kernel(const double* _
     for (int k = threadIdx.x; k < ne; k += kBlock) rows[k] = src[k];
   }
   __syncthreads();
-  double vmax = 0.0, dmin = kNoExtraSq;
+  float vmax = 0.f, dmin = kNoBound;
   const int t = threadIdx.x;
   if (t < nr) {
     const int f = iperm[r0 + t];
@@ -346,12 +348,12 @@ __global__ void __launch_bounds__(kBlock) scatter_prepare_kernel(const double* _
   fold_candidates_block(vmax, dmin, S.keys);
 }
 
-// initial keys: max |v|^2 starts at (1e-8)^2 and min extra dt at 1e20 (as
-// its square), the reference's initial values (MUSCL_base.hpp:314,
-// adiabatic.hpp:545)
-__global__ void reset_keys_kernel(unsigned long long* keys) {
-  keys[0] = order_key(1e-16);
-  keys[1] = order_key(kNoExtraSq);
+// initial keys: max |v|^2 starts at (1e-8)^2 (MUSCL_base.hpp:314) and the
+// min extra-dt square at +inf, no bound, for which the clip takes the
+// reference's initial 1e20 (adiabatic.hpp:545)
+__global__ void reset_keys_kernel(unsigned* keys) {
+  keys[0] = order_key(kMinVel2);
+  keys[1] = order_key(kNoBound);
 }
 
 // dt = min(dt0, 0.1 h0 / max_vel, extra_dt) (MUSCL_base.hpp:100-115), time,
@@ -365,14 +367,13 @@ struct StepDt {
   double dt, max_vel, extra;
   bool neg_extra;
 };
-__device__ __forceinline__ StepDt clip_dt(const unsigned long long* keys, const PhysParams& P, double dt0) {
+__device__ __forceinline__ StepDt clip_dt(const unsigned* keys, const PhysParams& P, double dt0) {
   StepDt d;
-  const float max_vel_f = sqrtf(fpc::d2f(key_value(keys[0])));
+  const float max_vel_f = sqrtf(key_value(keys[0]));
   d.max_vel = fpc::f2d(max_vel_f);
-  const double xs = key_value(keys[1]);
   d.extra = 1e20;
-  if (xs < kNoExtraSq) {
-    const float xf = fpc::d2f(xs);
+  if (keys[1] < order_key(kNoBound)) {
+    const float xf = key_value(keys[1]);
     d.extra = fpc::f2d(xf < 0.f ? -sqrtf(-xf) : sqrtf(xf));
   }
   d.neg_extra = d.extra < 0;
@@ -389,12 +390,12 @@ __device__ __forceinline__ StepDt clip_dt(const unsigned long long* keys, const 
 // bounds are FP32 values and rounding is monotone, so clipping the rounded
 // dt0 by the FP32 bounds gives the rounded clipped dt (NaN bounds clip
 // nothing in either form).
-__device__ __forceinline__ float clip_dt_f32(const unsigned long long* keys, const PhysParams& P, float dt0f) {
-  const unsigned long long k0 = keys[0], k1 = keys[1];
-  const float max_vel_f = sqrtf(fpc::d2f(key_value(k0)));
+__device__ __forceinline__ float clip_dt_f32(const unsigned* keys, const PhysParams& P, float dt0f) {
+  const unsigned k0 = keys[0], k1 = keys[1];
+  const float max_vel_f = sqrtf(key_value(k0));
   float extra = 1e20f;
-  if (k1 < order_key(kNoExtraSq)) {
-    const float xf = fpc::d2f(key_value(k1));
+  if (k1 < order_key(kNoBound)) {
+    const float xf = key_value(k1);
     extra = xf < 0.f ? -sqrtf(-xf) : sqrtf(xf);
     if (extra < 0.f) extra = 1e20f;
   }
@@ -418,9 +419,9 @@ __device__ __forceinline__ void publish_dt(const DevState& S, const StepDt& d, d
 }
 
 // fresh keys for the next fold
-__device__ __forceinline__ void restart_keys(unsigned long long* keys) {
-  keys[0] = order_key(1e-16);
-  keys[1] = order_key(kNoExtraSq);
+__device__ __forceinline__ void restart_keys(unsigned* keys) {
+  keys[0] = order_key(kMinVel2);
+  keys[1] = order_key(kNoBound);
 }
 
 // One thread: dt, the scalars and fresh keys (the batched launches).
@@ -606,7 +607,7 @@ __device__ __forceinline__ void update_body(const DevGeomMixed& G, const DevStat
   }
   griddep_wait();
   if (RESTART_KEYS && f == 0) restart_keys(S.keys);
-  double vmax = 0.0, dmin = kNoExtraSq;
+  float vmax = 0.f, dmin = kNoBound;
   if (live) {
     const float2 dtf2 = *reinterpret_cast<const float2*>(S.scal + kScDtF);
     const float dtf = (STAGE == 1) ? dtf2.y : dtf2.x;
@@ -642,7 +643,7 @@ __device__ __forceinline__ void update_body(const DevGeomMixed& G, const DevStat
     if (u[0] < 1e-8) u[0] = 1e-8;
     if (P.solver == kSolverIsoHLLE) {
       u[4] = 0.0;
-      double vm, dm;
+      float vm, dm;
       iso_w32_candidates(u, fcn32, S.W32, fp, f, vm, dm);
       if (STAGE == 2) {
 #pragma unroll
@@ -688,8 +689,8 @@ __global__ void __launch_bounds__(32) ens_prepare_kernel(const EnsInstance* __re
 __global__ void ens_reset_keys_kernel(const EnsInstance* __restrict__ inst, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) {
-    inst[i].S.keys[0] = order_key(1e-16);
-    inst[i].S.keys[1] = order_key(kNoExtraSq);
+    inst[i].S.keys[0] = order_key(kMinVel2);
+    inst[i].S.keys[1] = order_key(kNoBound);
   }
 }
 
