@@ -114,9 +114,15 @@ void HalfedgeMesh::adjust_outgoing(int v) {
 int HalfedgeMesh::add_face(const std::vector<int>& loop) {
   const size_t n = loop.size();
   if (n < 3) throw std::runtime_error("add_face: fewer than three vertices");
-  std::vector<int> he(n, kInvalid);
-  std::vector<char> fresh(n, 0), adjust(n, 0);
-  std::vector<std::pair<int, int>> links;
+  // per-thread scratch, reused across calls (a mesh build adds millions of
+  // faces; the algorithm and the resulting numbering are unchanged)
+  thread_local std::vector<int> he;
+  thread_local std::vector<char> fresh, adjust;
+  thread_local std::vector<std::pair<int, int>> links;
+  he.assign(n, kInvalid);
+  fresh.assign(n, 0);
+  adjust.assign(n, 0);
+  links.clear();
   links.reserve(3 * n);
 
   // Existing half-edges along the loop; every corner must lie on the
