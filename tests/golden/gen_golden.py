@@ -172,6 +172,31 @@ def state_case(name, mesh, level, solver, gam, acc, params, dt, nsteps, dump_eve
     print(f"state_{name}: steps {rec['steps'].tolist()} dt {rec['dt'][-1]:.6g} stop {rec['stop'].tolist()}")
 
 
+def state_subset_case(name, mesh, level, solver, gam, acc, params, dt, nsteps, recipe, seed,
+                      stride=61):
+    """A state run on a mesh too large for a full fixture: the initial state's
+    SHA-256 (the test regenerates it from the recipe), the reference's final
+    state on every stride-th face (reference order), its per-field sums over
+    all faces, and dt, t and the stop flag of the last step."""
+    g, _, _ = geometry(mesh, level)
+    U0 = recipe(unit(g["face_centers"]), gam, seed=seed)
+    res = run("run", mesh, level, solver, gam, 0.0, acc, dt, nsteps, nsteps, U0, params)
+    st = parse_states(res["_states.bin"], len(g["area"]))[-1]
+    idx = np.arange(0, len(g["area"]), stride, dtype=np.int64)
+    rec = {"U0_sha256": hashlib.sha256(np.ascontiguousarray(U0, "<f8").tobytes()).hexdigest(),
+           "seed": seed, "gam": np.float64(gam), "dt0": np.float64(dt),
+           "solver": SOLVERS[solver], "accretion_on": int(acc), "mesh": mesh, "level": level,
+           "params": np.array([params[k] for k in ("accretion_rate", "e_acc", "omega_acc_abs",
+                                                   "tilt_angle", "acc_width", "alpha")]
+                              + [1.0 if params["friction_on"] else 0.0]),
+           "steps": st["steps"], "t": st["t"], "dt": st["dt"], "stop": st["stop"],
+           "index": idx, "U_subset": st["U"][idx], "U_sum": st["U"].sum(axis=0),
+           "U_absmax": np.abs(st["U"]).max(axis=0)}
+    np.savez_compressed(HERE / f"state_{name}.npz", **rec)
+    print(f"state_{name}: steps {st['steps']} dt {st['dt']:.6g} stop {st['stop']} "
+          f"({len(idx)} of {len(g['area'])} faces kept)")
+
+
 def funcs_case(name, solver, params, acc=True, mesh="hex", level=3, nsamp=300, seed=11):
     res = run("functions", mesh, level, solver, 1.25, 0.0, acc, 7e-4, 0, 0, None, params,
               seed=seed, nsamp=nsamp)
@@ -228,11 +253,30 @@ def writers_case(name, mesh, level, solver, gam, acc, params, dt, nsteps, recipe
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--only", choices=["isothermal", "writers"], default=None,
-                    help="regenerate one group of fixtures only")
+    ap.add_argument("--only", choices=["isothermal", "writers", "large_geometry", "mid_state"],
+                    default=None, help="regenerate one group of fixtures only")
     a = ap.parse_args()
     if not RUNNER.exists():
         sys.exit(f"{RUNNER} missing: make -C oracle/ref REF=<reference checkout>")
+    if a.only == "mid_state":
+        # the accreting mid-size workload itself: icosphere_hex(7), 163,842
+        # faces, HLLC+, quiet noise of seed 1, dt0 = 2e-4, 100 steps
+        state_subset_case("c1_hex7_hllcp", "hex", 7, "HLLCplus", ic.gam2d(4 / 3), True,
+                          ACC_PARAMS, 2e-4, 100,
+                          lambda r, g_, seed: ic.quiet_noise(r, g_, seed=seed), 1)
+        return
+    if a.only == "large_geometry":
+        # the large-mesh workloads' geometries (hex(9): 2,621,442 faces, quad(9):
+        # 1,572,864), hashed and merged into geom_hashes.json
+        path = HERE / "geom_hashes.json"
+        data = json.loads(path.read_text())
+        for mesh, level in (("hex", 9), ("quad", 9)):
+            g, ac, _ = geometry(mesh, level)
+            data["hashes"][f"{mesh}{level}"] = array_hashes(g)
+            data["scalars"][f"{mesh}{level}"] = {"area_coeff_acc_width_0.1": ac}
+            print(f"{mesh}{level}: {len(g['area'])} faces hashed")
+        path.write_text(json.dumps(data, indent=1))
+        return
     if a.only == "isothermal":
         iso_funcs_case("hlle_hex3")
         iso_funcs_case("hlle_quad3", mesh="quad", seed=17)

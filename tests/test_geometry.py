@@ -29,8 +29,10 @@ def test_geometry_bit_exact(kind, level):
     assert g.h0 == float(ref["h0"])
 
 
-@pytest.mark.parametrize("key", ["hex4", "hex6", "hex7", "quad4", "quad6"])
+@pytest.mark.parametrize("key", ["hex4", "hex6", "hex7", "quad4", "quad6", "hex9", "quad9"])
 def test_geometry_hashes(key):
+    """Every geometry array, up to the large-mesh workloads' hex(9) (2,621,442
+    faces) and quad(9) (1,572,864), hashed against the reference's members."""
     import splash_gb300 as sg
 
     data = json.loads((GOLDEN / "geom_hashes.json").read_text())["hashes"][key]
