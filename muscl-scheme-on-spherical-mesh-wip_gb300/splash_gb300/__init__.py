@@ -20,6 +20,8 @@ from pathlib import Path
 import numpy as np
 
 from . import initial_conditions  # noqa: F401  (re-exported helper module)
+from . import input_recipes  # noqa: F401  (the reference's make_input.py recipes)
+from . import workloads  # noqa: F401  (seeded synthetic workloads)
 
 PKG_DIR = Path(__file__).resolve().parent.parent
 LIB_PATH = PKG_DIR / "lib" / "libsplash_gb300.so"
@@ -672,3 +674,20 @@ def read_input_dat(path, n_faces: int, dim: int) -> np.ndarray:
     if vals.size < need:
         vals = np.concatenate([vals, np.ones(need - vals.size)])
     return vals[:need].reshape(n_faces, dim)
+
+
+def read_final_state(path, n_faces: int, dim: int) -> np.ndarray:
+    """results/final_state.dat as a restart state: the reference restarts by
+    reading that file in place of input/input.dat (test.cpp:34-35), with the
+    same reader rule; the file holds six significant digits per value
+    (physics/adiabatic.hpp:335-348), so a restart starts from the rounded
+    state, as the reference's does."""
+    return read_input_dat(path, n_faces, dim)
+
+
+def format_final_state(U) -> str:
+    """The text write_final_state produces for a state U [F, dim] in
+    reference face order: every value in the C++ stream's default format
+    (%g, six significant digits) followed by a space, one row per face
+    (physics/adiabatic.hpp:335-348)."""
+    return "".join("".join(f"{x:g} " for x in row) + "\n" for row in np.asarray(U, dtype=np.float64))
