@@ -323,38 +323,28 @@ def algorithmic_bytes(geom, kernel: str) -> float:
 
 
 # ------------------------------------------------------------------ arms
+STOP_BITS = {1: "nan_flux", 2: "nan_wave_speed", 4: "wave_order", 8: "negative_extra_dt"}
+
+
+def stop_bit_names(err: int) -> list[str]:
+    """The stop causes in an error word (include/splash_gb300.h SPLASH_STOP_*)."""
+    return [name for bit, name in STOP_BITS.items() if err & bit]
+
+
 def ensemble_workload(sg, torch, steps=500, n_members=512, seed=3):
     """The batched workload: 512 independent members on icosphere_hex(3..7)
     (level drawn with weights 2^-(level-3), seed 3), mixed precision, dim 4
-    or 5 drawn 50/50: dim 5 members run MUSCL_HLLCplus with per-member
-    accretion_rate log-uniform in [1e-4, 1e-1], tilt_angle uniform in
-    [0, pi/2], omega_acc_abs uniform in [0, 1], acc_width 0.1, e_acc 0.5;
-    dim 4 members run the isothermal MUSCL_HLLE (HLLC+ is adiabatic only, and
-    the isothermal solver has no source).  Sigma = Pi = 1 +- 1e-3 (own seed);
-    each member runs `steps` steps with its own CFL dt (dt0 = 1 never
-    binds)."""
-    rng = np.random.default_rng(seed)
+    or 5 drawn 50/50 (splash_gb300.workloads.ensemble_draws: dim-5 members
+    run MUSCL_HLLCplus with their own accretion parameters, dim-4 members the
+    isothermal MUSCL_HLLE).  Sigma = Pi = 1 +- 1e-3 (own seed); each member
+    runs `steps` steps with its own CFL dt (dt0 = 1 never binds)."""
+    from splash_gb300 import workloads
+
+    draws = workloads.ensemble_draws(n_members, seed)
+    draw = np.array([d["level"] for d in draws])
+    dims = np.array([d["dim"] for d in draws])
     levels = np.arange(3, 8)
-    w = 2.0 ** -(levels - 3)
-    draw = rng.choice(levels, size=n_members, p=w / w.sum())
-    dims = rng.choice([4, 5], size=n_members)
-    gam = sg.initial_conditions.gam2d(4 / 3)
-    centres = {}
-    members = []
-    for i, lv in enumerate(draw):
-        lv = int(lv)
-        if lv not in centres:
-            centres[lv] = sg.Geometry(sg.icosphere_hex(lv)).unit_face_centers()
-        U = sg.initial_conditions.quiet_noise(centres[lv], gam, seed=1000 + i)
-        params = sg.SolverParams(accretion_rate=float(10 ** rng.uniform(-4, -1)), e_acc=0.5,
-                                 omega_acc_abs=float(rng.uniform(0, 1)),
-                                 tilt_angle=float(rng.uniform(0, np.pi / 2)), acc_width=0.1,
-                                 alpha=1e-6, friction_on=True)
-        solver = sg.SOLVER_HLLCPLUS
-        if dims[i] == 4:
-            solver, U = sg.SOLVER_HLLE, np.ascontiguousarray(U[:, :4])
-        members.append({"mesh": sg.icosphere_hex(lv), "U_in": U, "gam": gam, "omega_ns": 0.0,
-                        "accretion_on": True, "params": params, "solver": solver})
+    members = workloads.ensemble_members(sg, draws)
     t0 = time.perf_counter()
     ens = sg.Ensemble(members, autotune=True)
     setup = time.perf_counter() - t0
@@ -369,12 +359,18 @@ def ensemble_workload(sg, torch, steps=500, n_members=512, seed=3):
     b.record(stream)
     b.synchronize()
     secs = a.elapsed_time(b) / 1e3
-    dts = [ens.member_info(i)["dt"] for i in range(n)]
-    stops = sum(1 for i in range(n) if ens.member_info(i)["err"])
+    infos = [ens.member_info(i) for i in range(n)]
+    dts = [x["dt"] for x in infos]
+    stops = sum(1 for x in infos if x["err"])
+    # every member whose error word is non-zero, with what it latched
+    stop_members = [{"member": i, "level": draws[i]["level"], "dim": draws[i]["dim"], "err": infos[i]["err"],
+                     "bits": stop_bit_names(infos[i]["err"]), "params": draws[i]["params"]}
+                    for i in range(n) if infos[i]["err"]]
     out = {"members": n, "total_faces": total, "levels_drawn": {int(l): int((draw == l).sum()) for l in levels},
            "steps": steps, "value": total * steps / secs, "unit": METRIC,
            "ms_per_step": secs / steps * 1e3, "setup_s": setup, "schedule": ens.schedule(),
            "dt_range": [min(dts), max(dts)], "members_with_stop_flag": stops,
+           "stop_members": stop_members,
            "dims_drawn": {"4": int((dims == 4).sum()), "5": int((dims == 5).sum())}}
     ens.close()
     return out
@@ -434,53 +430,101 @@ def adjoint_workload(sg, torch, steps=1000, checkpoint_every=50, level=6, seed=4
     return out
 
 
-def shear_workload(sg, torch, fp64_steps=20, mixed_steps=200, level=9, seed=2, dt0=1e-4):
-    """The large-mesh shear layer at reduced length: icosphere_hex(9)
-    (2,621,442 faces), MUSCL_HLLCplus, dim 5, no accretion, u_phi = 0.5
-    tanh(latitude / 0.05), Sigma = 1 + 1e-2 random Y_lm (l <= 8, seed 2),
-    Pi = Sigma^gam2d, do_step(1e-4) with the CFL clip.  Both precisions run
-    `fp64_steps` steps from the same state (face-updates/s of each and the
-    mixed state's error against FP64 after those steps); the mixed path then
-    runs `mixed_steps` more for its rate.  The 1000-step comparison of the
-    full workload is shear_check.py."""
+SHEAR_CASES = {
+    # name: (mesh kind, level, solver, dim)
+    "hex9_hllcp": (0, 9, 3, 5),   # icosphere_hex(9), 2,621,442 faces, MUSCL_HLLCplus
+    "quad9_hllc": (1, 9, 2, 5),   # quad_sphere(9), 1,572,864 faces, MUSCL_HLLC
+    "quad9_hlle": (1, 9, 4, 4),   # quad_sphere(9), isothermal MUSCL_HLLE (dim 4)
+}
+
+
+def timed_steps(torch, solver, steps, dt0):
+    """CUDA-event time of `steps` do_step calls replayed back to back."""
+    stream = torch.cuda.ExternalStream(solver.stream())
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    solver.do_steps(steps, dt0)
+    b.record(stream)
+    b.synchronize()
+    return a.elapsed_time(b) / 1e3
+
+
+def shear_workload(sg, torch, case="hex9_hllcp", steps=1000, seed=2, dt0=1e-4, warmup=3):
+    """The large-mesh shear layer: u_phi = 0.5 tanh(latitude / 0.05), Sigma =
+    1 + 1e-2 x random real Y_lm (l <= 8, seed 2), Pi = Sigma^gam2d, gam3d =
+    4/3, no accretion, do_step(1e-4) with the CFL clip picking dt.  Both
+    precisions run `steps` steps from the same state (state resident; the
+    working sets are GBs, far larger than the L2).  Reported: face-updates/s
+    of each, mixed/FP64, the mixed state's relative L1 and L-infinity error
+    per field against FP64 (angular momentum also against the momentum scale
+    Sigma c_s), total mass and angular-momentum drift of each run, the last
+    dt and the stop flags."""
+    kind, level, solver_kind, dim = SHEAR_CASES[case]
+    mesh = sg.Mesh(kind, level)
     gam = sg.initial_conditions.gam2d(4 / 3)
-    mesh = sg.icosphere_hex(level)
-    nf = 10 * 4 ** level + 2
     t0 = time.perf_counter()
-    fp64 = sg.MUSCL_HLLCplus(mesh, np.ones((nf, 5)), 5, gam, 0.0, False, precision=sg.PREC_FP64)
-    r, area = fp64.face_geometry()
-    U0 = sg.initial_conditions.shear_layer(r, gam, seed=seed)
-    mixed = sg.MUSCL_HLLCplus(mesh, U0, 5, gam, 0.0, False, precision=sg.PREC_MIXED)
-    setup = time.perf_counter() - t0
-
-    def timed(s, n):
-        stream = torch.cuda.ExternalStream(s.stream())
-        a = torch.cuda.Event(enable_timing=True)
-        b = torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        s.do_steps(n, dt0)
-        b.record(stream)
-        b.synchronize()
-        return a.elapsed_time(b) / 1e3
-
-    for s in (fp64, mixed):
-        s.do_steps(3, dt0)
+    geo = sg.Geometry(mesh)
+    r, area = geo.unit_face_centers(), geo["area"].copy()
+    nf = geo.n_faces
+    del geo
+    U0 = np.ascontiguousarray(sg.initial_conditions.shear_layer(r, gam, seed=seed)[:, :dim])
+    setup = {"geometry_s": time.perf_counter() - t0}
+    out = {"workload": f"{['icosphere_hex', 'quad_sphere'][kind]}({level}) {nf} faces, solver {solver_kind}, "
+                       f"dim {dim}, shear layer seed {seed}, dt0={dt0} (CFL-clipped)",
+           "faces": nf, "steps": steps, "unit": METRIC}
+    states = {}
+    for name, prec in (("fp64", sg.PREC_FP64), ("mixed", sg.PREC_MIXED)):
+        t0 = time.perf_counter()
+        s = sg.Solver(mesh, U0, dim, gam, 0.0, False, params=sg.SolverParams(), solver=solver_kind,
+                      precision=prec)
+        setup[f"create_{name}_s"] = time.perf_counter() - t0
+        s.do_steps(warmup, dt0)
         s.synchronize()
         s.set_state(U0)
-    t64 = timed(fp64, fp64_steps)
-    t32 = timed(mixed, fp64_steps)
-    U64, U32 = fp64.get_state(), mixed.get_state()
-    t32b = timed(mixed, mixed_steps)
-    out = {"workload": f"icosphere_hex({level}) {nf} faces, HLLC+, shear layer, dt0={dt0} (CFL-clipped)",
-           "fp64": {"value": nf * fp64_steps / t64, "ms_per_step": t64 / fp64_steps * 1e3, "steps": fp64_steps},
-           "mixed": {"value": nf * mixed_steps / t32b, "ms_per_step": t32b / mixed_steps * 1e3,
-                     "steps": mixed_steps},
-           "unit": METRIC, "mixed_over_fp64": (nf * mixed_steps / t32b) / (nf * fp64_steps / t64),
-           "l1_rel_per_field_after_fp64_steps": l1_rel(U32, U64, area).tolist(),
-           "last_dt": fp64.last_dt(), "setup_s": setup}
-    fp64.close()
-    mixed.close()
+        d0 = s.diagnostics()
+        secs = timed_steps(torch, s, steps, dt0)
+        d1 = s.diagnostics()
+        states[name] = s.get_state()
+        out[name] = {"value": nf * steps / secs, "ms_per_step": secs / steps * 1e3, "t": s.time(),
+                     "last_dt": s.last_dt(), "stop": s.get_stop_check(), "error_word": s.error_word(),
+                     "mass_drift": float(d1[0] / d0[0] - 1),
+                     "angular_momentum_drift": drift_l(d0, d1, U0, area)}
+        s.close()
+    a, b = states["fp64"], states["mixed"]
+    out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    out["l1_rel_per_field"] = l1_rel(b, a, area).tolist()
+    out["linf_rel_per_field"] = (np.max(np.abs(b - a), axis=0) /
+                                 np.maximum(np.max(np.abs(a), axis=0), 1e-300)).tolist()
+    out["l1_angular_momentum_vs_sigma_cs"] = l1_momentum_scale(b, a, area, gam, dim).tolist()
+    out["setup_s"] = setup
     return out
+
+
+def drift_l(d0, d1, U0, area) -> float:
+    """|L(t) - L(0)| over the total absolute angular momentum sum A |l| of the
+    initial state (the total L of a symmetric flow can be ~0)."""
+    scale = float(np.sum(area * np.linalg.norm(U0[:, 1:4], axis=1)))
+    return float(np.linalg.norm(np.asarray(d1[1:4]) - np.asarray(d0[1:4])) / max(scale, 1e-300))
+
+
+def l1_momentum_scale(a, b, area, gam, dim=5):
+    """Relative L1 of the angular-momentum fields against the momentum scale
+    Sigma c_s (c_s the sound speed of b; the isothermal c_s is 1):
+    sum A |l_a - l_b| / sum A Sigma_b c_s."""
+    if dim == 5:
+        cs = np.sqrt(np.maximum(gam * pressure_of(b, gam) / b[:, 0], 0.0))
+    else:
+        cs = np.ones(len(b))
+    den = np.sum(area * b[:, 0] * cs)
+    return np.sum(area[:, None] * np.abs(a[:, 1:4] - b[:, 1:4]), axis=0) / den
+
+
+def pressure_of(U, gam):
+    """Pi = (E - |l|^2 / (2 Sigma)) (gam - 1): |v| = |r x l| / Sigma = |l| / Sigma
+    for tangential l (MUSCL_base.hpp:517-539, without the 1e-16 floor)."""
+    l2 = np.sum(U[:, 1:4] * U[:, 1:4], axis=1)
+    return (U[:, 4] - l2 / (2 * U[:, 0])) * (gam - 1)
 
 
 def l1_rel(a, b, area):
@@ -526,6 +570,7 @@ def run_ours(args):
                               device=local)
     fp64 = sg.MUSCL_HLLCplus(mesh, U0, 5, gam, 0.0, True, params=params, precision=sg.PREC_FP64,
                              device=local)
+    dm0, d640 = mixed.diagnostics(), fp64.diagnostics()
     # one full replica per GPU: the step does not shard
     with ClockSampler(local) as clocks:
         if world > 1:
@@ -540,9 +585,20 @@ def run_ours(args):
     value64 = F * args.steps / secs64
     # accuracy of the timed runs: both advanced warmup + steps from the same state
     Um, U64 = mixed.get_state(), fp64.get_state()
-    acc = {"steps": args.warmup + args.steps, "l1_rel_per_field": l1_rel(Um, U64, geom["area"]).tolist(),
+    area = geom["area"]
+    dm1, d641 = mixed.diagnostics(), fp64.diagnostics()
+    acc = {"steps": args.warmup + args.steps, "l1_rel_per_field": l1_rel(Um, U64, area).tolist(),
            "linf_rel_per_field": (np.max(np.abs(Um - U64), axis=0) /
                                   np.max(np.abs(U64), axis=0)).tolist(),
+           # l starts at ~0 (the flow starts at rest), so its error is also
+           # measured against the momentum scale Sigma c_s
+           "l1_angular_momentum_vs_sigma_cs": l1_momentum_scale(Um, U64, area, gam).tolist(),
+           "mass_change": {"mixed": float(dm1[0] / dm0[0] - 1), "fp64": float(d641[0] / d640[0] - 1),
+                           "note": "relative change of the total mass over the run (accretion adds mass)"},
+           "mass_mixed_vs_fp64": float(dm1[0] / d641[0] - 1),
+           "angular_momentum_mixed_vs_fp64": float(np.linalg.norm(dm1[1:4] - d641[1:4]) /
+                                                   np.sum(area * U64[:, 0] * np.sqrt(
+                                                       gam * pressure_of(U64, gam) / U64[:, 0]))),
            "reference": "GPU FP64 path (1e-10 of the reference on the golden states)"}
     # per-kernel device times (un-captured launches, CUDA events on the solver stream)
     reps = max(3, min(20, args.steps))
@@ -599,7 +655,9 @@ def run_ours(args):
     if not args.no_adjoint:
         line["adjoint"] = adjoint_workload(sg, torch)
     if not args.no_shear:
-        line["shear_layer"] = shear_workload(sg, torch)
+        for i, case in enumerate(args.shear_cases):
+            line["shear_layer" if i == 0 else f"shear_layer_{case}"] = shear_workload(
+                sg, torch, case, steps=args.shear_steps)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(geom, U0, gam)
     if rank == 0:
@@ -623,13 +681,12 @@ def run_reference(args):
 
     cores = os.cpu_count() or 1
     o = Oracle(geom, U0, gam, 0.0, True, sg.SolverParams(**PARAMS).as_list(), 3, threads=cores)
-    # at least 3 warm-up steps like the GPU arm (a hex(7) oracle step takes
-    # tens of ms on the host cores), at most 10; a bounded sample of at most
-    # 10 timed steps
-    warm = max(3, min(args.warmup, 10))
+    # the same warm-up (at least 3) and step counts as the GPU arm: a hex(7)
+    # oracle step takes tens of ms on the host cores
+    warm = max(3, args.warmup)
     for _ in range(warm):
         o.do_step(DT0)
-    n = max(1, min(args.steps, 10))
+    n = max(1, args.steps)
     t0 = time.perf_counter()
     o.do_steps(n, DT0)
     secs = time.perf_counter() - t0
@@ -647,6 +704,56 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_profile(args):
+    """A profiler harness: builds one solver (or the adjoint) and runs a few
+    steps, nothing else, so that an ncu capture sees only the step's kernels.
+
+    --profile mixed|fp64: `--profile-steps` do_step replays of the given mesh
+      and solver; initial state Sigma = Pi = 1 +- 1e-3 (seed 1), accretion on
+      with the mid-size workload's parameters.
+    --profile adjoint: one gradient (checkpointed forward + backward) of the
+      adjoint workload at reduced length (rotating blob, seed 4; HLLC; dt0 =
+      5e-4; loss target from accretion_rate 2e-2, tilt 0.3), then with --tlm
+      one tangent-linear run."""
+    import splash_gb300 as sg
+
+    mesh = sg.Mesh({"hex": 0, "quad": 1, "ico": 2}[args.mesh], args.level)
+    geom = sg.Geometry(mesh)
+    gam = sg.initial_conditions.gam2d(4 / 3)
+    if args.profile == "adjoint":
+        U0 = sg.initial_conditions.rotating_blob(geom.unit_face_centers(), gam, seed=4)
+        theta = np.array([1e-2, 0.1, 0.5])
+        params = sg.SolverParams(accretion_rate=theta[0], e_acc=0.5, omega_acc_abs=theta[2],
+                                 tilt_angle=theta[1], acc_width=0.1, alpha=1e-6, friction_on=True)
+        base = sg.Solver(mesh, U0, 5, gam, 0.0, True, params=params, solver=args.solver,
+                         precision=sg.PREC_FP64)
+        adj = sg.Adjoint(base, checkpoint_every=args.checkpoint_every)
+        target = adj.forward(U0, np.array([2e-2, 0.3, 0.5]), args.profile_steps, 5e-4)[:, 0].copy()
+        loss, _, gth = adj.run(U0, theta, args.profile_steps, 5e-4, target)
+        info = adj.info()
+        print(f"{args.mesh}({args.level}) F={base.n_faces} solver={args.solver}: {args.profile_steps} steps, "
+              f"K={args.checkpoint_every}: forward {info['ms_forward']:.2f} ms, backward "
+              f"{info['ms_backward']:.2f} ms, loss {loss:.6e}, grad_theta {gth}")
+        if args.tlm:
+            rng = np.random.default_rng(0)
+            adj.tlm(U0, theta, rng.normal(size=U0.shape), None, args.profile_steps, 5e-4)
+            print(f"tlm {adj.info()['ms_tlm']:.2f} ms")
+        adj.close()
+        base.close()
+        return
+    U0 = sg.initial_conditions.quiet_noise(geom.unit_face_centers(), gam, seed=1)
+    prec = sg.PREC_MIXED if args.profile == "mixed" else sg.PREC_FP64
+    s = sg.Solver(mesh, U0, 5, gam, 0.0, True, params=sg.SolverParams(**PARAMS), solver=args.solver,
+                  precision=prec)
+    t0 = time.perf_counter()
+    s.do_steps(args.profile_steps, DT0)
+    s.synchronize()
+    dt = time.perf_counter() - t0
+    print(f"{args.mesh}({args.level}) F={geom.n_faces} solver={args.solver} {args.profile}: "
+          f"{args.profile_steps} steps in {dt * 1e3:.2f} ms, stop={s.get_stop_check()}")
+    s.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -657,7 +764,21 @@ def main():
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-shear", action="store_true")
+    ap.add_argument("--shear-cases", nargs="*", default=["hex9_hllcp"], choices=list(SHEAR_CASES),
+                    help="large-mesh shear-layer cases, 1000 steps each in both precisions")
+    ap.add_argument("--shear-steps", type=int, default=1000)
+    # profiler harness (no JSON line): see run_profile
+    ap.add_argument("--profile", choices=["mixed", "fp64", "adjoint"], default=None)
+    ap.add_argument("--mesh", default="hex", choices=["hex", "quad", "ico"])
+    ap.add_argument("--level", type=int, default=LEVEL)
+    ap.add_argument("--solver", type=int, default=3, choices=[1, 2, 3])
+    ap.add_argument("--profile-steps", type=int, default=5)
+    ap.add_argument("--checkpoint-every", type=int, default=10)
+    ap.add_argument("--tlm", action="store_true")
     args = ap.parse_args()
+    if args.profile:
+        run_profile(args)
+        return
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.impl == "reference":

@@ -282,21 +282,27 @@ SPLASH_API int splash_ensemble_size(splash_ensemble* e, int* n_members, int64_t*
  * allocate device memory when they need the time step (a coupling code that
  * owns all device memory through its own pool, or code about to capture its
  * stream into a CUDA graph).  Computes, on the CURRENT CUDA device and on
- * `stream` (NULL = the default stream), the dt that do_step(dt0) would use
- * for a conserved state already on the device:
+ * `stream` (NULL = the default stream), the dt that an FP64 adiabatic
+ * (dim 5) solver's do_step(dt0) would use for a conserved state already on
+ * the device (a mixed-precision solver clips from FP32 candidates, within
+ * ~1e-7 relative of this value; dim-4 isothermal states are not accepted):
  *   U            [n_faces][5] conserved state (device)
  *   unit_centres [n_faces][3] unit face centres, fc/|fc| (device)
  *   area         [n_faces] face areas (device)
  *   h0           minimum edge arc length (splash_geometry_info scalars[0])
  *   out          9 doubles (device): dt, max_vel, extra_dt, stop (1.0 when
  *                extra_dt_constr was negative), then the sums of
- *                Sigma*A, l_x*A, l_y*A, l_z*A, E*A.
+ *                Sigma*A, l_x*A, l_y*A, l_z*A, E*A.  dt, max_vel and
+ *                extra_dt equal the solver's bit for bit; the sums are
+ *                reduced in another order and agree to rounding.
  * It allocates nothing: the reduction's partial records live in a static
  * 1 MiB __device__ array inside the library (held by every GPU that loads
  * it until exit), so n_faces is limited to 4,194,304 (larger sizes return
  * SPLASH_E_INVALID).  The first call on a device looks up that array's
- * device address; make it before any stream capture.  All calls share the
- * array: calls that overlap on the GPU race.  Asynchronous on `stream`. */
+ * device address; make it before any stream capture (calls outside a
+ * capture look it up again, calls inside one reuse the last).  All calls
+ * share the array: calls that overlap on the GPU race.  Asynchronous on
+ * `stream`. */
 SPLASH_API int splash_cfl_dt_noalloc(const double* U, const double* unit_centres, const double* area,
                           int n_faces, double gam, double omega_ns, double alpha, double h0,
                           double dt0, double* out, void* stream);

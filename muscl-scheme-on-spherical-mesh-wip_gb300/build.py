@@ -113,9 +113,15 @@ def build_oracle(verbose: bool = False, force: bool = False) -> Path:
     return out
 
 
-def build_reference_runner(ref_root: Path | None = None, verbose: bool = False) -> Path | None:
-    """Compiles the reference solver (oracle/_ref/ref_runner) when its checkout exists."""
-    ref = Path(ref_root or os.environ.get("SPLASH_REFERENCE", "/root/reference"))
+def build_reference_runner(ref_root: str | Path | None = None, verbose: bool = False) -> Path | None:
+    """Compiles the reference solver (oracle/_ref/ref_runner) from the
+    reference checkout at ref_root (or $SPLASH_REFERENCE); returns None when
+    neither names a checkout (fixture generation only: the tests use the
+    committed fixtures)."""
+    root = ref_root or os.environ.get("SPLASH_REFERENCE")
+    if not root:
+        return None
+    ref = Path(root)
     if not (ref / "src" / "MUSCL_base" / "MUSCL_base.hpp").exists():
         return None
     cmd = ["make", "-s", "-C", str(ORACLE / "ref"), f"REF={ref}", f"-j{os.cpu_count() or 4}"]
@@ -130,4 +136,4 @@ if __name__ == "__main__":
     f = "--force" in sys.argv
     print(build_library(verbose=v, force=f))
     print(build_oracle(verbose=v, force=f))
-    print(build_reference_runner(verbose=v))
+    print(build_reference_runner(os.environ.get("SPLASH_REFERENCE"), verbose=v))

@@ -19,7 +19,13 @@
 //
 // The kernels are the FP64 path's own per-face candidates and reduction
 // (physics_fp64.cuh, reduce.cuh), and this file is compiled with the same
-// -fmad=false as step_fp64.cu, so the dt is the one splash_do_step uses.
+// -fmad=false as step_fp64.cu.  dt, max_vel and extra_dt are maxima and
+// minima, exact in any order, so they equal what an FP64 adiabatic (dim 5)
+// solver's splash_do_step computes for the same state; the five sums are
+// reduced over 256-face blocks here and 64-face blocks in the solver, so
+// they agree to rounding, not bit for bit.  A mixed-precision solver clips
+// dt from FP32 candidates of its FP32 face state (within ~1e-7 relative of
+// this value), and the isothermal (dim 4) state layout is not accepted.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -129,12 +135,21 @@ extern "C" int splash_cfl_dt_noalloc(const double* U, const double* unit_centres
     return set_error(SPLASH_E_CUDA, "splash_cfl_dt_noalloc: cudaGetDevice: %s", cudaGetErrorString(e));
   if (dev < 0 || dev >= kMaxDevices)
     return set_error(SPLASH_E_INVALID, "splash_cfl_dt_noalloc: device %d beyond %d", dev, kMaxDevices);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  e = cudaStreamIsCapturing(st, &cap);
+  if (e != cudaSuccess)
+    return set_error(SPLASH_E_CUDA, "splash_cfl_dt_noalloc: cudaStreamIsCapturing: %s",
+                     cudaGetErrorString(e));
   double* scratch = nullptr;
   {
-    // once per device, with that device current: the device address of the
-    // static array (its host-side name is only a stand-in)
+    // the device address of the static array (its host-side name is only a
+    // stand-in), with this device current: looked up on every call made
+    // outside stream capture (so that a context torn down and recreated,
+    // e.g. by cudaDeviceReset, gets the reloaded image's address), and kept
+    // per device for calls inside a capture, which reuse the last one
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch_ptr[dev]) {
+    if (!g_scratch_ptr[dev] || cap == cudaStreamCaptureStatusNone) {
       void* p = nullptr;
       e = cudaGetSymbolAddress(&p, g_scratch);
       if (e != cudaSuccess || p == nullptr)
@@ -151,7 +166,6 @@ extern "C" int splash_cfl_dt_noalloc(const double* U, const double* unit_centres
   P.h0 = h0;
   derive_params(P);
   const int nb = (n_faces + kBlock - 1) / kBlock;
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
   candidates_kernel<<<nb, kBlock, 0, st>>>(U, unit_centres, area, n_faces, P, scratch);
   finalize_kernel<<<1, 256, 0, st>>>(scratch, nb, P, dt0, out);
   e = cudaGetLastError();

@@ -68,6 +68,43 @@ def test_fp64_matches_oracle_larger_mesh(kind, level, solver, acc):
     s.close()
 
 
+def test_fp64_mid_size_workload_100_steps():
+    """The accreting mid-size workload itself: icosphere_hex(7) (163,842
+    faces), MUSCL_HLLCplus, accretion on (rate 1e-2, e_acc 0.5, omega_acc
+    0.5, tilt 0.2, width 0.1, friction on), quiet noise of seed 1, dt0 =
+    2e-4, 100 steps.  The GPU FP64 state is compared with the oracle on every
+    face and with the reference's own state (state_c1_hex7_hllcp.npz, written
+    by the reference on every 61st face) at 1e-10 relative L-infinity per
+    field; dt, t and the stop flag equal."""
+    import hashlib
+
+    import splash_gb300 as sg
+
+    c = load("state_c1_hex7_hllcp.npz")
+    g = sg.Geometry(mesh_of(str(c["mesh"]), int(c["level"])))
+    U0 = sg.initial_conditions.quiet_noise(g.unit_face_centers(), float(c["gam"]), seed=int(c["seed"]))
+    assert hashlib.sha256(np.ascontiguousarray(U0, "<f8").tobytes()).hexdigest() == str(c["U0_sha256"])
+    case = {k: c[k] for k in ("gam", "accretion_on", "solver", "mesh", "level", "params")}
+    case["U0"] = U0
+    nsteps, dt0 = int(c["steps"]), float(c["dt0"])
+    s = gpu_solver(case)
+    s.do_steps(nsteps, dt0)
+    U = s.get_state()
+    # the reference's own faces
+    idx = c["index"]
+    err_ref = np.max(np.abs(U[idx] - c["U_subset"]), axis=0) / c["U_absmax"]
+    assert np.all(err_ref < TOL), err_ref
+    assert abs(s.last_dt() - float(c["dt"])) <= 1e-13 * float(c["dt"])
+    assert abs(s.time() - float(c["t"])) <= 1e-12 * float(c["t"])
+    assert s.get_stop_check() == bool(c["stop"])
+    # every face against the oracle
+    o = make_oracle(g, case)
+    o.do_steps(nsteps, dt0)
+    err = rel_linf(U, o.get_state())
+    assert np.all(err < TOL), err
+    s.close()
+
+
 def test_step_is_deterministic_and_graph_replay_equals_single_steps():
     c = load("state_hex3_hllcp_acc.npz")
     a = gpu_solver(c)

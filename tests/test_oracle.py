@@ -88,6 +88,30 @@ def test_states_match_reference(case, geoms):
             assert np.all(rel_linf(U, c["U"][k]) < 1e-10), (case, nstep)
 
 
+def test_mid_size_workload_matches_reference():
+    """The accreting mid-size workload (icosphere_hex(7), 163,842 faces, HLLC+,
+    quiet noise of seed 1, dt0 = 2e-4) after 100 steps, against the
+    reference's own state on every 61st face and its per-field sums over all
+    faces."""
+    import hashlib
+
+    import splash_gb300 as sg
+
+    c = load("state_c1_hex7_hllcp.npz")
+    g = sg.Geometry(mesh_of(str(c["mesh"]), int(c["level"])))
+    U0 = sg.initial_conditions.quiet_noise(g.unit_face_centers(), float(c["gam"]), seed=int(c["seed"]))
+    assert hashlib.sha256(np.ascontiguousarray(U0, "<f8").tobytes()).hexdigest() == str(c["U0_sha256"])
+    case = {k: c[k] for k in ("gam", "accretion_on", "solver", "params")}
+    case["U0"] = U0
+    o = make_oracle(g, case)
+    o.do_steps(int(c["steps"]), float(c["dt0"]))
+    info, U = o.info(), o.get_state()
+    assert bool(info["stop"]) == bool(c["stop"])
+    assert _same(info["dt"], c["dt"]) and _same(info["t"], c["t"])
+    assert _same(U[c["index"]], c["U_subset"])
+    assert np.allclose(U.sum(axis=0), c["U_sum"], rtol=1e-12, atol=0)
+
+
 def test_oracle_thread_count_invariance(geoms):
     """The reference is bit-identical across OpenMP thread counts; so is the oracle."""
     c = load("state_hex3_hllcp_acc.npz")
