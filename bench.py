@@ -17,6 +17,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import platform
 import statistics
@@ -51,6 +52,20 @@ def measured_traffic(kernel: str):
         if len(parts) == 2 and parts[0] == kernel and not line.startswith("#"):
             return float(parts[1])
     return None
+
+
+def fp64_pipe_busy():
+    """FP64-pipe utilisation of the FP64 path's kernels from the committed ncu
+    summary (profiles/fp64_pipe_hex7.txt), or None."""
+    p = REPO / "profiles" / "fp64_pipe_hex7.txt"
+    if not p.exists():
+        return None
+    out = {}
+    for line in p.read_text().splitlines():
+        parts = line.split()
+        if len(parts) == 2 and not line.startswith("#"):
+            out[parts[0]] = float(parts[1])
+    return {"per_kernel": out, "source": "profiles/fp64_pipe_hex7.txt (ncu sm__pipe_fp64_cycles_active)"} if out else None
 
 
 def peaks():
@@ -287,10 +302,9 @@ def algorithmic_bytes_mixed(geom, kernel: str) -> float:
 
     edge (reconstruction + Riemann flux, one thread per edge): the edge
       record (face ids, edge centre, normal, n x R: 48 B) and per side the
-      stencil, weights and distances (2 x 48 B); every face
-      state W32 read once (20 B per face); write the edge flux (20 B per
-      edge) and, in stage 2, both edge states (2 x 20 B per edge; mean of the
-      two stages).
+      stencil, weights and distances (2 x 48 B); every face state read once
+      (20 B per face); write the edge flux (20 B per edge).  (The stage-2
+      edge states are no longer stored: the writers recompute them.)
     update (mean of the two stages): per face W32 (20 B), U0 (40 B), unit
       centre FP64 + FP32 (24 + 12 B), accretion source (8 B), slot count
       (1 B); per slot edge id and flux coefficient (8 B); every edge flux once
@@ -300,7 +314,7 @@ def algorithmic_bytes_mixed(geom, kernel: str) -> float:
     S = geom.n_slots
     E = S // 2
     if kernel == "edge":
-        return E * (48 + 96 + 20 + 40 / 2) + F * 20
+        return E * (48 + 96 + 20) + F * 20
     return F * (20 + 40 + 24 + 12 + 8 + 1) + S * 8 + E * 20 + F * (20 + 40 / 2)
 
 
@@ -360,6 +374,27 @@ def ensemble_workload(sg, torch, steps=500, n_members=512, seed=3):
     b.synchronize()
     secs = a.elapsed_time(b) / 1e3
     infos = [ens.member_info(i) for i in range(n)]
+    sched = ens.schedule()
+    # both designs timed over 100 more steps each: one persistent launch per
+    # do_steps call, and five launches per step (the fastest width the
+    # autotuner timed for the chosen tile order)
+    order = ["member", "largest-first", "round-robin"].index(sched["order"])
+    widths = [32, 64, 128]
+    w5 = widths[int(np.argmin(sched["trial_ms"][order]))]
+    designs = {}
+    for name, width in (("persistent", 0), ("five_launches", w5)):
+        try:
+            ens.set_schedule(order, width)
+        except sg.SplashError as exc:
+            designs[name] = {"unavailable": str(exc)}
+            continue
+        ens.do_steps(2, 1.0)
+        ens.synchronize()
+        a.record(stream)
+        ens.do_steps(100, 1.0)
+        b.record(stream)
+        b.synchronize()
+        designs[name] = {"ms_per_step": a.elapsed_time(b) / 100, "edge_block": width}
     dts = [x["dt"] for x in infos]
     stops = sum(1 for x in infos if x["err"])
     # every member whose error word is non-zero, with what it latched
@@ -368,7 +403,7 @@ def ensemble_workload(sg, torch, steps=500, n_members=512, seed=3):
                     for i in range(n) if infos[i]["err"]]
     out = {"members": n, "total_faces": total, "levels_drawn": {int(l): int((draw == l).sum()) for l in levels},
            "steps": steps, "value": total * steps / secs, "unit": METRIC,
-           "ms_per_step": secs / steps * 1e3, "setup_s": setup, "schedule": ens.schedule(),
+           "ms_per_step": secs / steps * 1e3, "setup_s": setup, "schedule": sched, "designs_100_steps": designs,
            "dt_range": [min(dts), max(dts)], "members_with_stop_flag": stops,
            "stop_members": stop_members,
            "dims_drawn": {"4": int((dims == 4).sum()), "5": int((dims == 5).sum())}}
@@ -376,16 +411,11 @@ def ensemble_workload(sg, torch, steps=500, n_members=512, seed=3):
     return out
 
 
-def adjoint_workload(sg, torch, steps=1000, checkpoint_every=50, level=6, seed=4):
-    """The discrete-adjoint workload: icosphere_hex(6), HLLC, dim 5, FP64,
-    1000 steps at dt0 = 5e-4, checkpoints every 50 steps; rotating-blob
-    initial state (seed 4); accretion on (rate 1e-2, tilt 0.1, omega_acc 0.5,
-    width 0.1, e_acc 0.5, friction on); loss 1/2 sum area (Sigma - Sigma*)^2
-    against a run with rate 2e-2, tilt 0.3.  Cost = gradient time (forward
-    with checkpoints + recomputing backward, CUDA events) over the plain FP64
-    forward of the same steps (graph replays, CUDA events); one seeded
-    direction is checked against the tangent-linear model."""
-    dt0 = 5e-4
+def adjoint_setup(sg, level=6, seed=4, solver=2, checkpoint_every=50):
+    """The discrete-adjoint workload: icosphere_hex(level), MUSCL_HLLC (solver
+    2), dim 5, FP64; rotating-blob initial state (seed 4); accretion on
+    (e_acc 0.5, omega_acc_abs 0.5, width 0.1, friction on, alpha 1e-6);
+    theta = (accretion_rate, tilt_angle, omega_acc_abs) = (1e-2, 0.1, 0.5)."""
     gam = sg.initial_conditions.gam2d(4 / 3)
     mesh = sg.icosphere_hex(level)
     geo = sg.Geometry(mesh)
@@ -393,8 +423,60 @@ def adjoint_workload(sg, torch, steps=1000, checkpoint_every=50, level=6, seed=4
     theta = np.array([1e-2, 0.1, 0.5])
     params = sg.SolverParams(accretion_rate=theta[0], e_acc=0.5, omega_acc_abs=theta[2], tilt_angle=theta[1],
                              acc_width=0.1, alpha=1e-6, friction_on=True)
-    base = sg.MUSCL_HLLC(mesh, U0, 5, gam, 0.0, True, params=params, precision=sg.PREC_FP64)
+    base = sg.Solver(mesh, U0, 5, gam, 0.0, True, params=params, solver=solver, precision=sg.PREC_FP64)
     adj = sg.Adjoint(base, checkpoint_every=checkpoint_every)
+    return base, adj, U0, theta, geo["area"].copy()
+
+
+def fd_check(adj, U0, theta, gU, gth, target, area, steps, dt0, directions, h=1e-6):
+    """Central differences of the loss 1/2 sum area (Sigma - Sigma*)^2 at
+    step h along each direction (dU, dtheta), against the adjoint's
+    directional derivative <gU, dU> + <gth, dtheta>.  The two runs at
+    (U0, theta) +- h (dU, dtheta) are the plain FP64 forward compared with a
+    branch recording made at (U0, theta) just before
+    (splash_adjoint_branch_tape): `crossings` counts the (face, launch)
+    evaluations whose branch path (limiter cases and min/max arguments,
+    Riemann sides, floors) departs from the recorded one in either run,
+    i.e. the kinks between the branches that the difference straddles and
+    the adjoint, which differentiates the recorded branches, does not."""
+    def loss(U):
+        return 0.5 * math.fsum((area * (U[:, 0] - target) ** 2).tolist())
+
+    rows = []
+    for dU, dth in directions:
+        g = float(np.sum(gU * dU) + np.dot(gth, dth))
+        Up, cp = adj.branch_tape(U0 + h * dU, theta + h * dth, steps, "compare")
+        Um, cm = adj.branch_tape(U0 - h * dU, theta - h * dth, steps, "compare")
+        fd = (loss(Up) - loss(Um)) / (2 * h)
+        rows.append({"adjoint": g, "plain_fd": fd, "rel": abs(fd - g) / abs(g), "crossings": cp + cm})
+    return rows
+
+
+def fd_summary(rows, evaluations):
+    """Largest relative difference of a set of fd_check rows, and how many
+    (face, launch) evaluations their runs departed at, of `evaluations` per
+    run."""
+    return {"n": len(rows), "max_rel": max((r["rel"] for r in rows), default=None),
+            "max_crossings": max((r["crossings"] for r in rows), default=0),
+            "evaluations_per_run": evaluations,
+            "no_crossing_max_rel": max((r["rel"] for r in rows if r["crossings"] == 0), default=None)}
+
+
+def adjoint_workload(sg, torch, steps=1000, checkpoint_every=50, level=6, seed=4, n_joint=16, n_param=5,
+                     n_local=4, h=1e-6):
+    """The discrete-adjoint workload (adjoint_setup), 1000 steps at dt0 =
+    5e-4, checkpoints every 50 steps; loss 1/2 sum area (Sigma - Sigma*)^2
+    against a run with accretion_rate 2e-2, tilt 0.3.  Cost = gradient time
+    (forward with checkpoints + recomputing backward, CUDA events) over the
+    plain FP64 forward of the same steps (graph replays, CUDA events).
+    Derivative checks along seeded directions: the TLM (<lambda, J d> =
+    <J^T lambda, d>), and central differences at h = 1e-6 of the forward
+    itself and of the branch-frozen forward (fd_check), along n_joint
+    joint directions (U0 with per-field scales of U0, and theta) and n_param
+    parameter-only directions (the three unit ones first), and n_local
+    state directions supported on the blob's core."""
+    dt0 = 5e-4
+    base, adj, U0, theta, area = adjoint_setup(sg, level, seed, 2, checkpoint_every)
     stream = torch.cuda.ExternalStream(base.stream())
     base.do_steps(3, dt0)
     base.synchronize()
@@ -411,12 +493,34 @@ def adjoint_workload(sg, torch, steps=1000, checkpoint_every=50, level=6, seed=4
     info = adj.info()
     Uf = adj.forward(U0, theta, steps, dt0)
     rng = np.random.default_rng(seed)
-    dU = rng.normal(size=U0.shape) * np.maximum(np.abs(U0).max(axis=0), 1e-3)
+    scale = np.maximum(np.abs(U0).max(axis=0), 1e-3)
+    dU = rng.normal(size=U0.shape) * scale
     dth = rng.normal(size=3) * np.array([1e-2, 0.1, 0.5])
     _, dUt = adj.tlm(U0, theta, dU, dth, steps, dt0)
     tlm_ms = adj.info()["ms_tlm"]
     g_adj = float(np.sum(gU * dU) + np.dot(gth, dth))
-    g_tlm = float(np.sum(geo["area"] * (Uf[:, 0] - target) * dUt[:, 0]))
+    g_tlm = float(np.sum(area * (Uf[:, 0] - target) * dUt[:, 0]))
+    # finite-difference checks: the seeded joint directions (the first is
+    # the TLM's) and the parameter directions
+    joint = [(dU, dth)] + [(rng.normal(size=U0.shape) * scale, rng.normal(size=3) * np.array([1e-2, 0.1, 0.5]))
+                           for _ in range(n_joint - 1)]
+    units = [np.array([1e-2, 0, 0]), np.array([0, 0.1, 0]), np.array([0, 0, 0.5])]
+    params = (units + [rng.normal(size=3) * np.array([1e-2, 0.1, 0.5]) for _ in range(max(0, n_param - 3))])[:n_param]
+    # state directions supported where the blob's density exceeds the far
+    # field by more than 1e-2 (the far field is exactly uniform, and the
+    # blob's tail is uniform to 1e-10, where a relative perturbation of h
+    # decides the limiter ratios by itself)
+    core = (U0[:, 0] - 1.0 > 1e-2).astype(float)[:, None]
+    local = [(rng.normal(size=U0.shape) * scale * core, np.zeros(3)) for _ in range(n_local)]
+    adj.forward(U0, theta, steps, dt0)  # the dt schedule the taped runs follow
+    t0 = time.perf_counter()
+    adj.branch_tape(U0, theta, steps, "record")
+    tape_ms = (time.perf_counter() - t0) * 1e3  # wall clock, including the state upload
+    evaluations = base.n_faces * (1 + 4 * steps)
+    rows_j = fd_check(adj, U0, theta, gU, gth, target, area, steps, dt0, joint[:n_joint], h)
+    rows_p = fd_check(adj, U0, theta, gU, gth, target, area, steps, dt0,
+                      [(np.zeros_like(U0), d) for d in params], h)
+    rows_l = fd_check(adj, U0, theta, gU, gth, target, area, steps, dt0, local, h)
     out = {"workload": f"icosphere_hex({level}) {base.n_faces} faces, HLLC, FP64, {steps} steps dt0={dt0}, "
                        f"checkpoints every {checkpoint_every}",
            "forward_ms": fwd_ms, "gradient_forward_ms": info["ms_forward"],
@@ -424,6 +528,15 @@ def adjoint_workload(sg, torch, steps=1000, checkpoint_every=50, level=6, seed=4
            "adjoint_over_forward": (info["ms_forward"] + info["ms_backward"]) / fwd_ms,
            "tlm_over_forward": tlm_ms / fwd_ms, "clipped_steps": info["clipped_steps"],
            "loss": loss, "grad_theta": gth.tolist(), "rel_adjoint_vs_tlm": abs(g_adj - g_tlm) / abs(g_tlm),
+           "fd_h": h,
+           "fd_parameter": fd_summary(rows_p, evaluations), "fd_core_state": fd_summary(rows_l, evaluations),
+           "fd_joint": fd_summary(rows_j, evaluations),
+           "fd_rows": {"joint": rows_j, "parameter": rows_p, "core_state": rows_l},
+           "core_faces": int(core.sum()),
+           "branch_tape_record_ms": tape_ms,
+           "fd_note": "central differences of the FP64 forward at h; crossings: (face, launch) evaluations whose "
+                      "branch path departs from the one at theta in the two runs, the kinks the difference "
+                      "straddles (the adjoint differentiates the branches taken at theta)",
            "device_bytes": info["device_bytes"]}
     adj.close()
     base.close()
@@ -632,7 +745,8 @@ def run_ours(args):
         "gpu_launches": 4 * args.steps,
         "e2e": {"value": F * e2e_steps / e2e_secs, "unit": METRIC, "h2d_bytes_per_step": bytes_io,
                 "d2h_bytes_per_step": bytes_io, "host_buffers": "pinned (page-locked) FP64 [F][5] arrays"},
-        "fp64": {"value": value64, "ms_per_step": secs64 / args.steps * 1e3, "kernel_ms": kern64},
+        "fp64": {"value": value64, "ms_per_step": secs64 / args.steps * 1e3, "kernel_ms": kern64,
+                 "fp64_pipe_busy": fp64_pipe_busy()},
         "back_to_back": {"value": F * args.steps / secs_bb, "ms_per_step": secs_bb / args.steps * 1e3,
                          "note": "do_steps in 4-step graphs, no L2 flush"},
         "mixed_over_fp64": value / value64,
@@ -653,7 +767,8 @@ def run_ours(args):
     if not args.no_ensemble:
         line["ensemble"] = ensemble_workload(sg, torch)
     if not args.no_adjoint:
-        line["adjoint"] = adjoint_workload(sg, torch)
+        line["adjoint"] = adjoint_workload(sg, torch, n_joint=args.adjoint_joint, n_param=args.adjoint_param,
+                                           n_local=args.adjoint_local)
     if not args.no_shear:
         for i, case in enumerate(args.shear_cases):
             line["shear_layer" if i == 0 else f"shear_layer_{case}"] = shear_workload(
@@ -767,6 +882,14 @@ def main():
     ap.add_argument("--shear-cases", nargs="*", default=["hex9_hllcp"], choices=list(SHEAR_CASES),
                     help="large-mesh shear-layer cases, 1000 steps each in both precisions")
     ap.add_argument("--shear-steps", type=int, default=1000)
+    ap.add_argument("--adjoint-joint", type=int, default=4,
+                    help="joint (state + parameter) directions of the adjoint's finite-difference check")
+    ap.add_argument("--adjoint-param", type=int, default=3, help="parameter-only directions of that check")
+    ap.add_argument("--adjoint-local", type=int, default=2,
+                    help="state directions supported on the blob's core, of that check")
+    ap.add_argument("--adjoint-only", action="store_true",
+                    help="run only the adjoint workload and print its JSON object (the full check: "
+                         "--adjoint-joint 16 --adjoint-param 8)")
     # profiler harness (no JSON line): see run_profile
     ap.add_argument("--profile", choices=["mixed", "fp64", "adjoint"], default=None)
     ap.add_argument("--mesh", default="hex", choices=["hex", "quad", "ico"])
@@ -778,6 +901,14 @@ def main():
     args = ap.parse_args()
     if args.profile:
         run_profile(args)
+        return
+    if args.adjoint_only:
+        import torch
+
+        import splash_gb300 as sg
+
+        print(json.dumps(adjoint_workload(sg, torch, n_joint=args.adjoint_joint, n_param=args.adjoint_param,
+                                          n_local=args.adjoint_local)), flush=True)
         return
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -257,24 +257,35 @@ typedef struct splash_member {
 typedef struct splash_ensemble splash_ensemble;
 
 /* Builds the ensemble (FP32/FP64 mixed precision).  With `autotune` != 0 the
- * block schedule (member order of the face tiles, reconstruction tile width)
- * is picked by timing every candidate for a few steps on the ensemble itself;
- * the state is restored afterwards. */
+ * schedule is picked by timing every candidate for a few steps on the
+ * ensemble itself (the state is restored afterwards): the member order of
+ * the face and edge tiles (member order, largest first, round-robin) and
+ * either five launches per step (per-member dt, edge and update of each
+ * stage) with 32-, 64- or 128-thread edge blocks, or one persistent
+ * cooperative launch per do_steps call that runs all its steps with grid
+ * barriers between the phases. */
 SPLASH_API int splash_ensemble_create(const splash_member* members, int n, int device, int autotune,
                            splash_ensemble** out);
 SPLASH_API int splash_ensemble_destroy(splash_ensemble* e);
-/* n steps of every member: member i advances by min(dt0, its CFL clip). */
+/* n steps of every member: member i advances by min(dt0, its CFL clip).
+ * One graph replay per step, or one (the persistent schedule) for all n. */
 SPLASH_API int splash_ensemble_do_steps(splash_ensemble* e, int n, double dt0);
+/* Waits for the ensemble's stream; SPLASH_E_CUDA if a grid barrier of the
+ * persistent launch timed out (its bounded wait, about 0.25 s). */
 SPLASH_API int splash_ensemble_synchronize(splash_ensemble* e);
+/* Sets the schedule: tile order 0..2 and edge_block 32, 64 or 128 threads
+ * (five launches per step), or 0 for the persistent launch. */
+SPLASH_API int splash_ensemble_set_schedule(splash_ensemble* e, int order, int edge_block);
 SPLASH_API int splash_ensemble_stream(splash_ensemble* e, void** stream);
 SPLASH_API int splash_ensemble_get_state(splash_ensemble* e, int member, double* U);
 /* out = {t, dt of the last step, max_vel, extra_dt}; err = stop bits */
 SPLASH_API int splash_ensemble_member_info(splash_ensemble* e, int member, double out[4], uint32_t* err);
 /* The chosen schedule: tile order (0 member order, 1 largest first, 2
  * round-robin) and the threads per block of the reconstruction + edge-flux
- * launch; and the autotuner's per-candidate ms per step (index
- * order*3 + {32,64,128}-thread blocks). */
-SPLASH_API int splash_ensemble_schedule(splash_ensemble* e, int* order, int* recon_width, double trial_ms[9]);
+ * launch (0: the persistent launch); and the autotuner's ms per step of
+ * each candidate: [order*3 + {32,64,128}-thread blocks] for five launches
+ * per step, [9 + order] for the persistent launch (0 where not timed). */
+SPLASH_API int splash_ensemble_schedule(splash_ensemble* e, int* order, int* recon_width, double trial_ms[12]);
 SPLASH_API int splash_ensemble_size(splash_ensemble* e, int* n_members, int64_t* total_faces);
 
 /* ---- allocation-free CFL clip --------------------------------------------
@@ -350,6 +361,26 @@ SPLASH_API int splash_adjoint_run(splash_adjoint* a, const double* U0, const dou
 SPLASH_API int splash_tlm_run(splash_adjoint* a, const double* U0, const double* theta, const double* dU0,
                               const double* dtheta, int n_steps, double dt0, double* U_final,
                               double* dU_final);
+/* Validation of the derivatives: the FP64 forward of n_steps steps from U0
+ * and theta on the dt schedule of the last splash_adjoint_forward (which
+ * must have run at least n_steps steps), with every branch decision of the
+ * step (limiter cases and min/max arguments, Riemann-solver sides,
+ * wave-speed fallbacks, floors) taped per face and launch:
+ *   mode 1  record the decisions (the run is the plain FP64 forward);
+ *   mode 0  replay the last recording: the branch-frozen map that the
+ *           adjoint and the TLM differentiate; count = replayed decisions
+ *           the run's own values would have taken the other way.  Where a
+ *           replayed branch leads a formula out of its domain (the limiter
+ *           switch's (1 - r)^0.1 on 0 < r < 1) the run returns NaN states;
+ *   mode 2  the plain forward, compared with the recording; count = the
+ *           (face, launch) evaluations whose branch path departs from the
+ *           recorded one: the kink crossings between the two points.
+ * The recording holds 64 bytes per face per launch (1 + 4 n_steps launches:
+ * 10.5 GB for icosphere_hex(6) and 1000 steps).  count may be NULL.
+ * Returns SPLASH_E_UNSUPPORTED if a face makes more decisions in one launch
+ * than its tape slice holds (480).  No counterpart in the reference. */
+SPLASH_API int splash_adjoint_branch_tape(splash_adjoint* a, const double* U0, const double* theta, int n_steps,
+                                          int mode, double* U_final, int64_t* count);
 /* out[8]: steps of the last forward, steps whose dt the CFL clip shortened,
  * min dt, max dt, forward ms, backward ms, last TLM ms (CUDA events), device
  * bytes held. */

@@ -81,7 +81,13 @@ struct Adjoint {
   double *d_lam = nullptr, *d_scrU = nullptr, *d_scrW = nullptr;
   AdjScratch X{};
   unsigned err_bits = 0;
-  float ms_forward = 0.f, ms_backward = 0.f, ms_tlm = 0.f;
+  float ms_forward = 0.f, ms_backward = 0.f, ms_tlm = 0.f, ms_frozen = 0.f;
+  // branch tape of the branch-frozen forward (validation)
+  uint32_t* d_btape = nullptr;
+  size_t btape_cap = 0;  // words
+  int btape_steps = 0;
+  uint32_t* d_bpos = nullptr;
+  unsigned* d_berr = nullptr;
 
   ~Adjoint() {
     if (base) cudaSetDevice(base->device);
@@ -195,6 +201,7 @@ struct Adjoint {
   int backward(const double* lam_final, double* grad_U0, double* grad_theta);
   int tlm(const double* U0, const double* theta, const double* dU0, const double* dtheta, int n, double dt0_,
           double* U_final, double* dU_final);
+  int frozen_forward(const double* U0, const double* theta, int n, int record, double* U_final, int64_t* flips);
 };
 
 int Adjoint::forward(const double* U0, const double* theta, int n, double dt0_, double* U_final) {
@@ -348,6 +355,80 @@ int Adjoint::tlm(const double* U0, const double* theta, const double* dU0, const
     if (rc) return rc;
   }
   if (dU_final) return from_planes(T.dU, dU_final);
+  return SPLASH_OK;
+}
+
+// The FP64 forward on the dt schedule of the last forward run, with every
+// branch decision recorded (mode 1), replayed from the recording (mode 0)
+// or compared with it (mode 2).
+int Adjoint::frozen_forward(const double* U0, const double* theta, int n, int mode_in, double* U_final,
+                            int64_t* flips) {
+  if (n <= 0) return set_error(SPLASH_E_INVALID, "n_steps must be > 0");
+  if (mode_in < 0 || mode_in > 2) return set_error(SPLASH_E_INVALID, "mode must be 0, 1 or 2");
+  const bool record = mode_in == 1;
+  const int tmode = record ? 0 : (mode_in == 0 ? 1 : 2);  // taped.cuh: kRecord, kReplay, kCompare
+  if (!have_forward || n > n_steps)
+    return set_error(SPLASH_E_INVALID,
+                     "the branch-frozen forward runs on the dt schedule of a forward run of at least "
+                     "n_steps steps: call splash_adjoint_forward first");
+  if (!record && n > btape_steps)
+    return set_error(SPLASH_E_INVALID, "no branch tape of %d steps: record one first (mode 1)", n);
+  set_theta(theta);
+  int rc = upload_profile(nullptr);
+  if (rc) return rc;
+  P.total_mass = total_mass(U0);
+  derive_params(P);
+  const size_t RW = (size_t)n_faces * taped_words_per_face();
+  const size_t need = RW * (1 + 4 * (size_t)n);
+  try {
+    if (record && need > btape_cap) {
+      if (d_btape) dfree(d_btape);
+      d_btape = nullptr;
+      btape_cap = 0;
+      btape_steps = 0;
+      d_btape = dalloc<uint32_t>(need);
+      btape_cap = need;
+    }
+    if (!d_bpos) d_bpos = dalloc<uint32_t>(fpad);
+    if (!d_berr) d_berr = dalloc<unsigned>(4);
+  } catch (const std::bad_alloc&) {
+    return set_error(SPLASH_E_NOMEM, "device allocation of the branch tape (%zu bytes) failed",
+                     need * sizeof(uint32_t));
+  }
+  rc = to_planes(U0, S.U);
+  if (rc) return rc;
+  const cudaStream_t st = stream();
+  ADJ_CUDA(cudaMemsetAsync(d_berr, 0, 4 * sizeof(unsigned), st));
+  if (record) {
+    btape_steps = 0;
+    ADJ_CUDA(cudaMemsetAsync(d_btape, 0, need * sizeof(uint32_t), st));
+  }
+  cudaEvent_t e0, e1;
+  ADJ_CUDA(cudaEventCreate(&e0));
+  ADJ_CUDA(cudaEventCreate(&e1));
+  ADJ_CUDA(cudaEventRecord(e0, st));
+  ADJ_CUDA(taped_prim(G, P, S.U, S.W0, d_btape, d_bpos, d_berr, tmode, st));
+  for (int i = 0; i < n; ++i)
+    ADJ_CUDA(taped_step(G, P, d_dts + i, S.U, S.W0, S.W1, S.uplus, d_scrU, d_btape + RW * (1 + 4 * (size_t)i), d_bpos,
+                        d_berr, tmode, st));
+  ADJ_CUDA(cudaEventRecord(e1, st));
+  ADJ_CUDA(cudaEventSynchronize(e1));
+  ADJ_CUDA(cudaEventElapsedTime(&ms_frozen, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  unsigned berr[4] = {0, 0, 0, 0};
+  ADJ_CUDA(cudaMemcpy(berr, d_berr, sizeof berr, cudaMemcpyDeviceToHost));
+  if (berr[0] & 1u)
+    return set_error(SPLASH_E_UNSUPPORTED, "a face made more branch decisions in one launch than its tape slice holds");
+  if (berr[0] & 2u)
+    return set_error(SPLASH_E_INVALID, "the replay asked for branch decisions the recording does not hold");
+  if (flips) {
+    unsigned long long f = 0;
+    std::memcpy(&f, berr + 2, sizeof f);
+    *flips = (int64_t)f;
+  }
+  if (record) btape_steps = n;
+  if (U_final) return from_planes(S.U, U_final);
   return SPLASH_OK;
 }
 
@@ -511,6 +592,13 @@ int splash_tlm_run(splash_adjoint* h, const double* U0, const double* theta, con
   GET_ADJ(h);
   if (!U0) return splash::set_error(SPLASH_E_INVALID, "U0 is NULL");
   return a->tlm(U0, theta, dU0, dtheta, n_steps, dt0, U_final, dU_final);
+}
+
+int splash_adjoint_branch_tape(splash_adjoint* h, const double* U0, const double* theta, int n_steps, int mode,
+                               double* U_final, int64_t* count) {
+  GET_ADJ(h);
+  if (!U0) return splash::set_error(SPLASH_E_INVALID, "U0 is NULL");
+  return a->frozen_forward(U0, theta, n_steps, mode, U_final, count);
 }
 
 int splash_adjoint_info(splash_adjoint* h, double out[8]) {

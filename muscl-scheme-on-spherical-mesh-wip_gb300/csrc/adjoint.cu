@@ -29,6 +29,19 @@
 #include "physics_fp64.cuh"
 #include "reduce.cuh"
 #include "step_body_fp64.cuh"
+#include "taped.cuh"
+
+namespace splash {
+namespace f64 {
+// state planes read and written as Taped values (taped.cuh)
+template <>
+struct Planes<Taped> {
+  double* p;
+  __device__ Taped ld(size_t i) const { return Taped(p[i]); }
+  __device__ void st(size_t i, const Taped& x) const { p[i] = x.v; }
+};
+}  // namespace f64
+}  // namespace splash
 
 namespace splash {
 namespace adj {
@@ -116,6 +129,49 @@ __global__ void __launch_bounds__(kBlock) tlm_flux_kernel(DevGeom G, DevState S,
     }
   }
   if (STAGE == 2) red::block_partials<kBlock>(vmax, dmin, sums, S.partial + (size_t)blockIdx.x * kPartialStride);
+}
+
+// ---------------------------------------------------------------------
+// branch-frozen forward: the step bodies on Taped (taped.cuh)
+__global__ void __launch_bounds__(kRevBlock) tp_prim_kernel(DevGeom G, PhysParams P, const double* __restrict__ U,
+                                                         double* __restrict__ W) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= G.n_faces) return;
+  const int fp = G.fpad;
+  Taped u[kDim], w[kDim];
+#pragma unroll
+  for (int k = 0; k < kDim; ++k) u[k] = Taped(U[(size_t)k * fp + f]);
+  prim_of(u, plane3(G.fcn, fp, f), P.gam, w);
+#pragma unroll
+  for (int k = 0; k < kDim; ++k) W[(size_t)k * fp + f] = w[k].v;
+}
+
+__global__ void __launch_bounds__(kRevBlock) tp_recon_kernel(DevGeom G, PhysParams P, const double* __restrict__ dtp,
+                                                          double* W, double* uplus) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= G.n_faces) return;
+  recon_face<Taped>(G, P, *dtp, Planes<Taped>{W}, Planes<Taped>{uplus}, f);
+}
+
+template <int STAGE>
+__global__ void __launch_bounds__(kRevBlock) tp_flux_kernel(DevGeom G, PhysParams P, const double* __restrict__ dtp,
+                                                         double* Win, double* U0, double* uplus, double* Uout,
+                                                         double* Wout) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= G.n_faces) return;
+  const int fp = G.fpad;
+  const double dt = *dtp;
+  const double dt_here = (STAGE == 1) ? dt / 2 : dt;
+  Taped u[kDim], w[kDim];
+  bool floored;
+  flux_face<Taped, double>(G, P, face_src_params<double>(G, P, f), dt_here, Planes<Taped>{Win}, Planes<Taped>{U0},
+                           Planes<Taped>{uplus}, f, u, floored);
+  prim_of(u, plane3(G.fcn, fp, f), P.gam, w);
+#pragma unroll
+  for (int k = 0; k < kDim; ++k) {
+    Uout[(size_t)k * fp + f] = u[k].v;
+    Wout[(size_t)k * fp + f] = w[k].v;
+  }
 }
 
 // ---------------------------------------------------------------------
@@ -303,6 +359,48 @@ cudaError_t tlm_step(const DevGeom& G, const DevState& S, const TlmTangents& T, 
   adj::tlm_flux_kernel<1><<<nb, adj::kBlock, 0, st>>>(G, S, T, P);
   adj::tlm_recon_kernel<<<nb, adj::kBlock, 0, st>>>(G, P, S.scal, W1, up);
   adj::tlm_flux_kernel<2><<<nb, adj::kBlock, 0, st>>>(G, S, T, P);
+  return cudaGetLastError();
+}
+
+namespace {
+// points the comparisons of the next launch at its tape region (the
+// __constant__ update is ordered on the stream before the launch) and
+// restarts every face's position
+cudaError_t tape_region(const DevGeom& G, uint32_t* region, uint32_t* pos, unsigned* err, int mode,
+                        cudaStream_t st) {
+  // err[2..3] hold the 64-bit flip count
+  const tape::TapeCfg cfg{region, pos, err, reinterpret_cast<unsigned long long*>(err + 2), mode};
+  cudaError_t e = cudaMemcpyToSymbolAsync(tape::g_tape, &cfg, sizeof cfg, 0, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return e;
+  return cudaMemsetAsync(pos, 0, (size_t)G.n_faces * sizeof(uint32_t), st);
+}
+}  // namespace
+
+int taped_words_per_face() { return tape::kTapeWords; }
+
+cudaError_t taped_prim(const DevGeom& G, const PhysParams& P, double* U, double* W, uint32_t* region,
+                       uint32_t* pos, unsigned* err, int mode, cudaStream_t st) {
+  cudaError_t e = tape_region(G, region, pos, err, mode, st);
+  if (e != cudaSuccess) return e;
+  adj::tp_prim_kernel<<<adj::rev_blocks_for(G.n_faces), adj::kRevBlock, 0, st>>>(G, P, U, W);
+  return cudaGetLastError();
+}
+
+cudaError_t taped_step(const DevGeom& G, const PhysParams& P, const double* dtp, double* U, double* W0,
+                       double* W1, double* uplus, double* U1, uint32_t* region, uint32_t* pos, unsigned* err,
+                       int mode, cudaStream_t st) {
+  const int nb = adj::rev_blocks_for(G.n_faces);
+  constexpr int B = adj::kRevBlock;
+  const size_t RW = (size_t)G.n_faces * tape::kTapeWords;
+  cudaError_t e;
+  if ((e = tape_region(G, region, pos, err, mode, st)) != cudaSuccess) return e;
+  adj::tp_recon_kernel<<<nb, B, 0, st>>>(G, P, dtp, W0, uplus);
+  if ((e = tape_region(G, region + RW, pos, err, mode, st)) != cudaSuccess) return e;
+  adj::tp_flux_kernel<1><<<nb, B, 0, st>>>(G, P, dtp, W0, U, uplus, U1, W1);
+  if ((e = tape_region(G, region + 2 * RW, pos, err, mode, st)) != cudaSuccess) return e;
+  adj::tp_recon_kernel<<<nb, B, 0, st>>>(G, P, dtp, W1, uplus);
+  if ((e = tape_region(G, region + 3 * RW, pos, err, mode, st)) != cudaSuccess) return e;
+  adj::tp_flux_kernel<2><<<nb, B, 0, st>>>(G, P, dtp, W1, U, uplus, U, W0);
   return cudaGetLastError();
 }
 

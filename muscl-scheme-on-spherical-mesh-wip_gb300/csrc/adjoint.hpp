@@ -81,4 +81,25 @@ cudaError_t rc_step(const DevGeom& G, const PhysParams& P, const double* dtp, co
 cudaError_t adj_step(const DevGeom& G, const PhysParams& P, double dt, const StepTape& t, const AdjScratch& X,
                      double* lam, cudaStream_t st);
 
+// ---- branch tape of the FP64 step (validation of the derivatives, taped.cuh) ----
+// The FP64 step bodies on a scalar whose comparison outcomes are recorded
+// (mode 0), replayed (mode 1: the branch-frozen map) or compared with the
+// recording (mode 2: the plain step, counting departures), per face and
+// launch in `tape`, a region of kTapeWords 32-bit words per face and launch:
+// one launch for the initial prim(U) and four per step, in that order, each
+// region n_faces * kTapeWords words.  pos: [n_faces] scratch; err (4 words,
+// 8-byte aligned): err[0] bit 1 a face ran out of tape, bit 2 a replay read
+// past what was recorded; err[2..3] a 64-bit count (replay: outcomes the
+// values would have decided otherwise; compare: faces per launch whose
+// branch path departed from the recording).
+// taped_prim writes W = prim(U) (region 0); taped_step advances (U, W0)
+// by one step with dt = *dtp, using W1, uplus and U1 as scratch (regions
+// 4 i + 1 .. 4 i + 4 of step i, passed as `region`).
+cudaError_t taped_prim(const DevGeom& G, const PhysParams& P, double* U, double* W, uint32_t* region,
+                       uint32_t* pos, unsigned* err, int mode, cudaStream_t st);
+cudaError_t taped_step(const DevGeom& G, const PhysParams& P, const double* dtp, double* U, double* W0,
+                       double* W1, double* uplus, double* U1, uint32_t* region, uint32_t* pos, unsigned* err,
+                       int mode, cudaStream_t st);
+int taped_words_per_face();
+
 }  // namespace splash

@@ -510,10 +510,12 @@ int splash_create(const splash_mesh_desc* mesh, const double* U_in, int dim, dou
     S.U = s->dalloc<double>(splash::kDim * fp);
     if (precision == SPLASH_PREC_MIXED) {
       S.W32 = s->dalloc<float>(splash::kDim * fp);
+      S.W32b = s->dalloc<float>(splash::kDim * fp);
       S.uplus32 = s->dalloc<float>(splash::kDim * 2 * (size_t)s->GM.epad);
       S.fe32 = s->dalloc<float>(splash::kDim * (size_t)s->GM.epad);
       S.uplus = nullptr;
       SPLASH_CUDA(cudaMemset(S.W32, 0, splash::kDim * fp * sizeof(float)));
+      SPLASH_CUDA(cudaMemset(S.W32b, 0, splash::kDim * fp * sizeof(float)));
       SPLASH_CUDA(cudaMemset(S.uplus32, 0, splash::kDim * 2 * (size_t)s->GM.epad * sizeof(float)));
       s->n_partials = 0;  // the mixed path reduces the dt candidates as keys
     } else {
@@ -651,8 +653,8 @@ int splash_memory(splash_solver* h, int64_t out[2]) {
   if (!s || !out) return fail(SPLASH_E_INVALID, "NULL argument");
   const size_t fp = (size_t)s->fpad, PS = (size_t)s->max_slots * fp;
   out[0] = (int64_t)s->geometry_bytes;
-  if (s->precision == SPLASH_PREC_MIXED)  // U; W32; edge states (2 per edge); edge fluxes
-    out[1] = (int64_t)(8 * splash::kDim * fp + 4 * splash::kDim * (fp + 3 * (size_t)s->GM.epad));
+  if (s->precision == SPLASH_PREC_MIXED)  // U; W32 and W32b; edge states (2 per edge); edge fluxes
+    out[1] = (int64_t)(8 * splash::kDim * fp + 4 * splash::kDim * (2 * fp + 3 * (size_t)s->GM.epad));
   else
     out[1] = (int64_t)(8 * (3 * splash::kDim * fp + splash::kDim * PS) +
                        8 * (size_t)s->n_partials * splash::kPartialStride);
@@ -836,9 +838,13 @@ int splash_write_t_curl(splash_solver* h, const char* path) {
     SPLASH_CUDA(cudaMemcpy(up.data(), s->S.uplus, up.size() * sizeof(double), cudaMemcpyDeviceToHost));
   } else {
     // packed FP32 edge states of the last stage, edge-major (owner side of
-    // edge e at e, reverse side at epad + e): [2 epad][4] (Sigma, l), then Pi
+    // edge e at e, reverse side at epad + e): [2 epad][4] (Sigma, l), then Pi,
+    // recomputed from the last stage-2 input (zeros before the first step,
+    // like the reference's freshly allocated U_plus)
     const size_t ne = 2 * (size_t)s->GM.epad;
     std::vector<float> up32(splash::kDim * ne);
+    if (s->steps > 0) SPLASH_CUDA(splash::mixed_edge_states(s->GM, s->S, s->P, s->stream));
+    SPLASH_CUDA(cudaStreamSynchronize(s->stream));
     SPLASH_CUDA(cudaMemcpy(up32.data(), s->S.uplus32, up32.size() * sizeof(float), cudaMemcpyDeviceToHost));
     for (int i = 0; i < s->n_faces; ++i) {
       const int n = s->wr_face_off[s->perm[i] + 1] - s->wr_face_off[s->perm[i]];

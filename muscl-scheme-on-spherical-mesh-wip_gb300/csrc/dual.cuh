@@ -43,6 +43,15 @@ struct Dual {
   }
 };
 
+template <class T>
+struct is_dual {
+  static constexpr bool value = false;
+};
+template <int N>
+struct is_dual<Dual<N>> {
+  static constexpr bool value = true;
+};
+
 // value of a plain double or a dual (for branches)
 SPLASH_HD double val(double x) { return x; }
 template <int N>

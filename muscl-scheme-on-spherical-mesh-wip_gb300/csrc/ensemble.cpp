@@ -62,13 +62,20 @@ struct Ensemble {
   std::vector<EnsInstance> inst;
   EnsInstance* d_inst = nullptr;
   double *U = nullptr, *acc = nullptr, *scal = nullptr, *U_snap = nullptr, *scal_snap = nullptr;
-  float *W32 = nullptr, *fe32 = nullptr;
+  float *W32 = nullptr, *W32b = nullptr, *fe32 = nullptr;
   unsigned int *err = nullptr, *err_snap = nullptr;
   unsigned* keys = nullptr;
   int2 *d_ftiles = nullptr, *d_etiles = nullptr;
   int n_ftiles = 0, n_etiles = 0;
   int order = 0, recon_width = 128;  // tile order; threads per block of the edge launch
-  double tuned_ms[9] = {0};
+  double tuned_ms[12] = {0};         // [order * 3 + width index], then [9 + order] persistent
+  // the persistent schedule: one cooperative launch of pgrid blocks per
+  // do_steps call (pgrid 0: the device's occupancy could not be read)
+  bool persistent = false;
+  int pgrid = 0;
+  unsigned* d_bar = nullptr;  // [0..1] grid barrier, [2] status (kEnsBarrierTimeout)
+  cudaGraphNode_t p_node = nullptr;
+  int graph_steps = 1;
   std::vector<void*> allocs;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -156,6 +163,18 @@ struct Ensemble {
   cudaError_t launch_step(double dt0) {
     return ensemble_step(d_inst, n, d_ftiles, n_ftiles, d_etiles, n_etiles, recon_width, dt0, stream);
   }
+  cudaError_t launch_persistent(double dt0, int steps) {
+    return ensemble_persistent(d_inst, n, d_ftiles, n_ftiles, d_etiles, n_etiles, dt0, steps, d_bar, d_bar + 2,
+                               pgrid, stream);
+  }
+  // the persistent launch's status word (after the stream has drained)
+  int check_status() {
+    unsigned st = 0;
+    ENS_CUDA(cudaMemcpy(&st, d_bar + 2, sizeof st, cudaMemcpyDeviceToHost));
+    if (st & kEnsBarrierTimeout)
+      return set_error(SPLASH_E_CUDA, "ensemble: a grid barrier of the persistent launch timed out");
+    return SPLASH_OK;
+  }
 
   // Times every (order, width) candidate over a few steps, keeps the
   // fastest, and restores the state the trials advanced.
@@ -190,10 +209,33 @@ struct Ensemble {
           best_w = widths[wi];
         }
       }
+    // the persistent launch, each tile order: 3 steps in one launch
+    bool best_p = false;
+    for (int o = 0; o < 3 && pgrid > 0; ++o) {
+      int rc = set_schedule(o, 128);
+      if (rc) return rc;
+      ENS_CUDA(launch_persistent(dt0, 1));  // warm-up
+      ENS_CUDA(cudaEventRecord(a, stream));
+      ENS_CUDA(launch_persistent(dt0, 3));
+      ENS_CUDA(cudaEventRecord(b, stream));
+      ENS_CUDA(cudaEventSynchronize(b));
+      float ms = 0;
+      ENS_CUDA(cudaEventElapsedTime(&ms, a, b));
+      tuned_ms[9 + o] = ms / 3;
+      if (ms < best) {
+        best = ms;
+        best_o = o;
+        best_w = 128;
+        best_p = true;
+      }
+    }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
-    int rc = set_schedule(best_o, best_w);
+    int rc = check_status();
     if (rc) return rc;
+    rc = set_schedule(best_o, best_w);
+    if (rc) return rc;
+    persistent = best_p;
     ENS_CUDA(cudaMemcpyAsync(U, U_snap, nU * sizeof(double), cudaMemcpyDeviceToDevice, stream));
     ENS_CUDA(cudaMemcpyAsync(scal, scal_snap, (size_t)n * kScCount * sizeof(double),
                              cudaMemcpyDeviceToDevice, stream));
@@ -203,8 +245,14 @@ struct Ensemble {
   }
 
   int capture() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+    dt0_node = p_node = nullptr;
+    graph_steps = 1;
     ENS_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-    const cudaError_t le = launch_step(graph_dt0);
+    const cudaError_t le = persistent ? launch_persistent(graph_dt0, 1) : launch_step(graph_dt0);
     cudaGraph_t g = nullptr;
     const cudaError_t ce = cudaStreamEndCapture(stream, &g);
     if (le != cudaSuccess) {
@@ -225,8 +273,39 @@ struct Ensemble {
       cudaKernelNodeParams kp{};
       ENS_CUDA(cudaGraphKernelNodeGetParams(nd, &kp));
       if (kp.func == ensemble_finalize_kernel_ptr()) dt0_node = nd;
+      if (kp.func == ensemble_persistent_kernel_ptr()) p_node = nd;
     }
-    if (!dt0_node) return set_error(SPLASH_E_CUDA, "ensemble dt node not found");
+    if (!(persistent ? p_node : dt0_node)) return set_error(SPLASH_E_CUDA, "ensemble dt node not found");
+    return SPLASH_OK;
+  }
+
+  // do_steps: the five-launch graph replayed once per step, or the
+  // persistent graph (one launch) replayed once for all n steps
+  int steps(int nst, double dt0) {
+    if (nst <= 0) return SPLASH_OK;
+    if (!persistent) {
+      for (int i = 0; i < nst; ++i) {
+        const int rc = step(dt0);
+        if (rc) return rc;
+      }
+      return SPLASH_OK;
+    }
+    if (dt0 != graph_dt0 || nst != graph_steps) {
+      cudaKernelNodeParams kp{};
+      ENS_CUDA(cudaGraphKernelNodeGetParams(p_node, &kp));
+      const EnsInstance* di = d_inst;
+      int nn = n, nft = n_ftiles, net = n_etiles, ns = nst;
+      const int2 *ft = d_ftiles, *et = d_etiles;
+      unsigned *bar = d_bar, *status = d_bar + 2;
+      double d0 = dt0;
+      void* args[] = {&di, &nn, &ft, &nft, &et, &net, &d0, &ns, &bar, &status};
+      kp.kernelParams = args;
+      kp.extra = nullptr;
+      ENS_CUDA(cudaGraphExecKernelNodeSetParams(exec, p_node, &kp));
+      graph_dt0 = dt0;
+      graph_steps = nst;
+    }
+    ENS_CUDA(cudaGraphLaunch(exec, stream));
     return SPLASH_OK;
   }
 
@@ -331,6 +410,7 @@ int splash_ensemble_create(const splash_member* members, int n, int device, int 
     e->U_snap = e->dalloc<double>(faces * kDim);
     e->acc = e->dalloc<double>(faces);
     e->W32 = e->dalloc<float>(faces * kDim);
+    e->W32b = e->dalloc<float>(faces * kDim);
     e->fe32 = e->dalloc<float>(edges * kDim);
     e->scal = e->dalloc<double>((size_t)n * kScCount);
     e->scal_snap = e->dalloc<double>((size_t)n * kScCount);
@@ -339,6 +419,7 @@ int splash_ensemble_create(const splash_member* members, int n, int device, int 
     e->keys = e->dalloc<unsigned>((size_t)n * 2);
     ENS_CUDA(cudaMemset(e->U, 0, faces * kDim * sizeof(double)));
     ENS_CUDA(cudaMemset(e->W32, 0, faces * kDim * sizeof(float)));
+    ENS_CUDA(cudaMemset(e->W32b, 0, faces * kDim * sizeof(float)));
     ENS_CUDA(cudaMemset(e->scal, 0, (size_t)n * kScCount * sizeof(double)));
     ENS_CUDA(cudaMemset(e->err, 0, (size_t)n * 4 * sizeof(unsigned)));
     size_t max_fpad = 0;
@@ -362,6 +443,7 @@ int splash_ensemble_create(const splash_member* members, int n, int device, int 
       I.G.acc_src = e->acc + e->off_face[i];
       I.S.U = e->U + e->off_face[i] * kDim;
       I.S.W32 = e->W32 + e->off_face[i] * kDim;
+      I.S.W32b = e->W32b + e->off_face[i] * kDim;
       I.S.uplus32 = nullptr;  // no writer reads a member's edge states
       I.S.fe32 = e->fe32 + e->off_edge[i] * kDim;
       I.S.scal = e->scal + (size_t)i * kScCount;
@@ -393,6 +475,9 @@ int splash_ensemble_create(const splash_member* members, int n, int device, int 
       e->inst.push_back(I);
     }
     e->d_inst = e->upload(e->inst);
+    e->d_bar = e->dalloc<unsigned>(4);
+    ENS_CUDA(cudaMemset(e->d_bar, 0, 4 * sizeof(unsigned)));
+    e->pgrid = ensemble_persistent_grid(device);
     int rc = e->set_schedule(0, 128);
     if (rc) return rc;
     rc = e->prepare();
@@ -402,6 +487,18 @@ int splash_ensemble_create(const splash_member* members, int n, int device, int 
       if (rc) return rc;
     }
     rc = e->capture();
+    if (rc && e->persistent) {
+      // a driver that cannot capture the cooperative launch: the fastest
+      // five-launch schedule of the same tile order
+      cudaGetLastError();
+      const int o = e->order;
+      int wi = 0;
+      for (int k = 1; k < 3; ++k)
+        if (e->tuned_ms[o * 3 + k] > 0 && e->tuned_ms[o * 3 + k] < e->tuned_ms[o * 3 + wi]) wi = k;
+      e->persistent = false;
+      rc = e->set_schedule(o, 32 << wi);
+      if (!rc) rc = e->capture();
+    }
     if (rc) return rc;
     ENS_CUDA(cudaStreamSynchronize(e->stream));
   } catch (const std::bad_alloc&) {
@@ -426,17 +523,27 @@ int splash_ensemble_destroy(splash_ensemble* h) {
 int splash_ensemble_do_steps(splash_ensemble* h, int n, double dt0) {
   GET_ENS(h);
   if (n < 0) return splash::set_error(SPLASH_E_INVALID, "n < 0");
-  for (int i = 0; i < n; ++i) {
-    const int rc = e->step(dt0);
-    if (rc) return rc;
-  }
-  return SPLASH_OK;
+  return e->steps(n, dt0);
 }
 
 int splash_ensemble_synchronize(splash_ensemble* h) {
   GET_ENS(h);
   ENS_CUDA(cudaStreamSynchronize(e->stream));
-  return SPLASH_OK;
+  return e->check_status();
+}
+
+int splash_ensemble_set_schedule(splash_ensemble* h, int order, int edge_block) {
+  GET_ENS(h);
+  if (order < 0 || order > 2) return splash::set_error(SPLASH_E_INVALID, "order must be 0, 1 or 2");
+  if (edge_block != 0 && edge_block != 32 && edge_block != 64 && edge_block != 128)
+    return splash::set_error(SPLASH_E_INVALID, "edge_block must be 0 (persistent), 32, 64 or 128");
+  if (edge_block == 0 && e->pgrid <= 0)
+    return splash::set_error(SPLASH_E_UNSUPPORTED, "the device's occupancy for the persistent launch is unknown");
+  ENS_CUDA(cudaStreamSynchronize(e->stream));
+  int rc = e->set_schedule(order, edge_block == 0 ? 128 : edge_block);
+  if (rc) return rc;
+  e->persistent = edge_block == 0;
+  return e->capture();
 }
 
 int splash_ensemble_stream(splash_ensemble* h, void** stream) {
@@ -455,6 +562,8 @@ int splash_ensemble_get_state(splash_ensemble* h, int member, double* U) {
   ENS_CUDA(cudaMemcpyAsync(e->h_stage, e->inst[member].S.U, (size_t)fp * splash::kDim * sizeof(double),
                            cudaMemcpyDeviceToHost, e->stream));
   ENS_CUDA(cudaStreamSynchronize(e->stream));
+  const int rc = e->check_status();
+  if (rc) return rc;
   for (int q = 0; q < nf; ++q)
     for (int k = 0; k < mdim; ++k) U[(size_t)L.sp.perm[q] * mdim + k] = e->h_stage[(size_t)k * fp + q];
   return SPLASH_OK;
@@ -468,6 +577,8 @@ int splash_ensemble_member_info(splash_ensemble* h, int member, double out[4], u
   ENS_CUDA(cudaMemcpyAsync(sc, e->inst[member].S.scal, sizeof sc, cudaMemcpyDeviceToHost, e->stream));
   ENS_CUDA(cudaMemcpyAsync(&ew, e->inst[member].S.err, sizeof ew, cudaMemcpyDeviceToHost, e->stream));
   ENS_CUDA(cudaStreamSynchronize(e->stream));
+  const int rc = e->check_status();
+  if (rc) return rc;
   out[0] = sc[splash::kScTime];
   out[1] = sc[splash::kScDt];
   out[2] = sc[splash::kScMaxVel];
@@ -476,13 +587,13 @@ int splash_ensemble_member_info(splash_ensemble* h, int member, double out[4], u
   return SPLASH_OK;
 }
 
-int splash_ensemble_schedule(splash_ensemble* h, int* order, int* recon_width, double trial_ms[9]) {
+int splash_ensemble_schedule(splash_ensemble* h, int* order, int* recon_width, double trial_ms[12]) {
   Ensemble* e = reinterpret_cast<Ensemble*>(h);
   if (!e) return splash::set_error(SPLASH_E_INVALID, "ensemble handle is NULL");
   if (order) *order = e->order;
-  if (recon_width) *recon_width = e->recon_width;
+  if (recon_width) *recon_width = e->persistent ? 0 : e->recon_width;
   if (trial_ms)
-    for (int i = 0; i < 9; ++i) trial_ms[i] = e->tuned_ms[i];
+    for (int i = 0; i < 12; ++i) trial_ms[i] = e->tuned_ms[i];
   return SPLASH_OK;
 }
 

@@ -40,6 +40,9 @@ cudaError_t fp64_gather_state(const double* U, const int* iperm, double* aos, in
 cudaError_t mixed_step(const DevGeomMixed& G, const DevState& S, const PhysParams& P, double dt0,
                        cudaStream_t st, cudaEvent_t* ev = nullptr, bool per_launch = false);
 const void* mixed_dt0_kernel_ptr();
+// The last step's stage-2 edge states into S.uplus32 (for write_t_curl),
+// recomputed from the stage-2 input face states S.W32b and the step's dt.
+cudaError_t mixed_edge_states(const DevGeomMixed& G, const DevState& S, const PhysParams& P, cudaStream_t st);
 // set_state + prepare in one pass: aos is the caller's [n_faces][dim] array
 // in reference order (host memory the device can access, or device memory),
 // iperm maps reference to internal face indices.
@@ -55,5 +58,16 @@ cudaError_t ensemble_prepare(const EnsInstance* inst, int n_inst, const int2* ft
 cudaError_t ensemble_step(const EnsInstance* inst, int n_inst, const int2* ftiles, int n_ftiles,
                           const int2* etiles, int n_etiles, int edge_block, double dt0, cudaStream_t st);
 const void* ensemble_finalize_kernel_ptr();
+// The same n_steps steps as one cooperative launch of `grid` resident blocks
+// (ensemble_persistent_grid: the occupancy of the current device, 0 if it
+// cannot be read): per step the dt clip, edge and update of each stage,
+// separated by grid barriers on bar[0..1] (zeroed here before the launch).
+// A barrier wait that runs out sets kEnsBarrierTimeout in *status.
+constexpr unsigned kEnsBarrierTimeout = 1u;
+int ensemble_persistent_grid(int device);
+cudaError_t ensemble_persistent(const EnsInstance* inst, int n_inst, const int2* ftiles, int n_ftiles,
+                                const int2* etiles, int n_etiles, double dt0, int n_steps, unsigned* bar,
+                                unsigned* status, int grid, cudaStream_t st);
+const void* ensemble_persistent_kernel_ptr();
 
 }  // namespace splash

@@ -129,9 +129,11 @@ struct DevState {
   double* W0;     // (Sigma, l, Pi) of U, kDim planes
   double* W1;     // (Sigma, l, Pi) after stage 1, kDim planes
   double* uplus;  // reconstructed edge states, kDim * max_slots planes of fpad
-  float* W32;     // mixed path: (Sigma, l, Pi) in FP32: [fpad] float4 (Sigma, l), then a Pi plane
-  float* uplus32; // mixed path: stage-2 edge states, packed like W32 over 2 * epad entries
-                  // (owner side of edge e at e, reverse side at epad + e); may be null
+  float* W32;     // mixed path: stage-1 input (Sigma, l, Pi) in FP32: [fpad] float4 (Sigma, l), then a Pi plane
+  float* W32b;    // mixed path: stage-2 input, the same layout (written by the stage-1 update)
+  float* uplus32; // mixed path: the last stage-2 edge states, packed like W32 over 2 * epad entries
+                  // (owner side of edge e at e, reverse side at epad + e), recomputed for the
+                  // writers (mixed_edge_states); may be null
   float* fe32;    // mixed path: FP32 Riemann flux of every edge, packed like W32 over epad edges
   double* partial;  // per-block partial records (kPartialStride doubles)
   double* scal;   // device scalars, see ScalarSlot

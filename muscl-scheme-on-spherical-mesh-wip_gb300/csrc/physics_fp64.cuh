@@ -287,7 +287,7 @@ SPLASH_HD T limiter_switch(const T& r) {
 template <class T>
 SPLASH_HD T limiter_field(const T& r, double eta_p, const T& sb_scale, const T& to_scale) {
   if (is_nan(r)) return T(0.);
-  if constexpr (!std::is_same<T, double>::value) {
+  if constexpr (is_dual<T>::value) {
     // r = +-inf (a zero forward difference): the limiter is flat there in r
     // and in the Courant factor; the dual chain would form 0 * inf
     if (is_inf(r)) return T(limiter_field<double>(val(r), eta_p, val(sb_scale), val(to_scale)));

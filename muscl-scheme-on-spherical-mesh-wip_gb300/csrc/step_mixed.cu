@@ -12,8 +12,10 @@
 //         Pi = (E - |r x l|^2 / (2 Sigma)) (gam - 1);
 //   compensated: the per-face sum of the FP32 contributions is carried as an
 //         FP32 (hi, lo) pair and folded into FP64.
-// W32 holds (Sigma, l, Pi) of the current stage input in FP32; every thread
-// writes only its own face, so one buffer serves both stages.
+// W32 and W32b hold (Sigma, l, Pi) in FP32 of the stage-1 and stage-2 input
+// states: the stage-1 update writes W32b, the stage-2 update W32, so the
+// last stage-2 input survives the step (the writers recompute the edge
+// states from it instead of every stage-2 launch storing them).
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -52,6 +54,49 @@ __device__ __forceinline__ F3 plane3f(const float* p, int stride, int i) {
 // block of this one has begun.
 __device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void griddep_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;"); }
+
+// Two FP32 lanes per instruction (PTX .f32x2: round to nearest,
+// flush-to-zero like the rest of this file); each lane rounds exactly as the
+// scalar add / sub / mul.
+__device__ __forceinline__ float2 add2(float2 a, float2 b) {
+  float2 r;
+  asm("{.reg .b64 A, B, D;\n\t"
+      "mov.b64 A, {%2, %3};\n\tmov.b64 B, {%4, %5};\n\t"
+      "add.rn.ftz.f32x2 D, A, B;\n\tmov.b64 {%0, %1}, D;}"
+      : "=f"(r.x), "=f"(r.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
+}
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+  float2 r;
+  asm("{.reg .b64 A, B, D;\n\t"
+      "mov.b64 A, {%2, %3};\n\tmov.b64 B, {%4, %5};\n\t"
+      "sub.rn.ftz.f32x2 D, A, B;\n\tmov.b64 {%0, %1}, D;}"
+      : "=f"(r.x), "=f"(r.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
+}
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
+  float2 r;
+  asm("{.reg .b64 A, B, D;\n\t"
+      "mov.b64 A, {%2, %3};\n\tmov.b64 B, {%4, %5};\n\t"
+      "mul.rn.ftz.f32x2 D, A, B;\n\tmov.b64 {%0, %1}, D;}"
+      : "=f"(r.x), "=f"(r.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
+}
+
+// Two compensated accumulators (Acc, physics_mixed.cuh) in the lanes of
+// float2 values: the same TwoSum steps, one packed instruction for both.
+struct Acc2 {
+  float2 hi, lo;
+  __device__ __forceinline__ void add(float2 x) {
+    const float2 t = add2(hi, x);
+    const float2 xx = sub2(t, hi);
+    lo = add2(lo, add2(sub2(hi, sub2(t, xx)), sub2(x, xx)));
+    hi = t;
+  }
+};
 
 // Packed FP32 states (face states W32 and edge states uplus32): entry i of
 // an n-entry array is a float4 (Sigma, l_x, l_y, l_z) at base + 4 i and Pi
@@ -507,29 +552,69 @@ __device__ __forceinline__ void recon_slot(const float* W, int fp, int f, int n,
 // solver) every thread clips its step's dt from the keys itself and the
 // first thread publishes the step scalars; otherwise dt comes from the
 // scalars.
+// The record of interior edge e (edge centre, normal, n x R, both faces and
+// both slots' stencils, weights and distances) and the slots' limiter
+// constants H+/BM and H-/BM = 1 / ((1/H) BM).
+struct EdgeRec {
+  int4 ids;
+  SlotGeomF g;
+  SlotConsts so, sr;
+};
+__device__ __forceinline__ void load_edge(const DevGeomMixed& G, int e, bool live, EdgeRec& r) {
+  float4 ce = make_float4(0.f, 0.f, 0.f, 0.f), ne = ce;
+  r.ids = make_int4(0, 0, 0, 0);
+  r.so = SlotConsts{};
+  r.sr = SlotConsts{};
+  if (live) {
+    r.ids = reinterpret_cast<const int4*>(G.e_ids)[e];
+    ce = reinterpret_cast<const float4*>(G.e_ec)[e];
+    ne = reinterpret_cast<const float4*>(G.e_en)[e];
+    r.so.st = reinterpret_cast<const int4*>(G.e_sten)[e];
+    r.sr.st = reinterpret_cast<const int4*>(G.e_sten)[G.epad + e];
+    r.so.bt = reinterpret_cast<const float4*>(G.e_beta)[e];
+    r.sr.bt = reinterpret_cast<const float4*>(G.e_beta)[G.epad + e];
+    r.so.hh = reinterpret_cast<const float4*>(G.e_h)[e];
+    r.sr.hh = reinterpret_cast<const float4*>(G.e_h)[G.epad + e];
+  }
+  r.so.eta_p = __fdividef(1.0f, r.so.hh.x * r.so.hh.z);
+  r.so.eta_m = __fdividef(1.0f, r.so.hh.y * r.so.hh.z);
+  r.sr.eta_p = __fdividef(1.0f, r.sr.hh.x * r.sr.hh.z);
+  r.sr.eta_m = __fdividef(1.0f, r.sr.hh.y * r.sr.hh.z);
+  r.g.ec = f3(ce.x, ce.y, ce.z);
+  r.g.en = f3(ne.x, ne.y, ne.z);
+  r.g.nxr = f3(ce.w, ne.w, __int_as_float(r.ids.z));
+}
+
+// the edge states of both slots of an edge from the face states W: the
+// owner slot (face f) and the reverse slot (face g, negated normal)
+__device__ __forceinline__ void recon_edge(const float* W, const DevGeomMixed& G, const PhysParams& P,
+                                           const EdgeRec& r, float dt, float* uL, float* uR) {
+  recon_slot(W, G.fpad, r.ids.x & 0x0fffffff, r.ids.x >> 28, r.so, r.g.ec, r.g.en, dt, P, uL);
+  recon_slot(W, G.fpad, r.ids.y & 0x0fffffff, r.ids.y >> 28, r.sr, r.g.ec, f3(-r.g.en.x, -r.g.en.y, -r.g.en.z),
+             dt, P, uR);
+}
+
+// The stage's input face states: W32 in stage 1 (written by set_state and
+// the stage-2 update), W32b in stage 2 (written by the stage-1 update).
+// Two buffers keep the stage-2 input until the next step's stage-1 update,
+// so the last stage's edge states can be recomputed for the writers instead
+// of being stored by every stage-2 edge launch.
+template <int STAGE>
+__device__ __forceinline__ const float* stage_input(const DevState& S) {
+  return STAGE == 1 ? S.W32 : S.W32b;
+}
+// the next stage's input face states, written by the stage's update
+template <int STAGE>
+__device__ __forceinline__ float* stage_output(const DevState& S) {
+  return STAGE == 1 ? S.W32b : S.W32;
+}
+
 template <int STAGE, bool OWN_DT>
 __device__ __forceinline__ void edge_body(const DevGeomMixed& G, const DevState& S, const PhysParams& P, int e,
                                           double dt0, float dt0f) {
   const bool live = e < G.n_edges;
-  int4 ids = make_int4(0, 0, 0, 0);
-  float4 ce = make_float4(0.f, 0.f, 0.f, 0.f), ne = ce;
-  SlotConsts so{}, sr{};
-  if (live) {
-    ids = reinterpret_cast<const int4*>(G.e_ids)[e];
-    ce = reinterpret_cast<const float4*>(G.e_ec)[e];
-    ne = reinterpret_cast<const float4*>(G.e_en)[e];
-    so.st = reinterpret_cast<const int4*>(G.e_sten)[e];
-    sr.st = reinterpret_cast<const int4*>(G.e_sten)[G.epad + e];
-    so.bt = reinterpret_cast<const float4*>(G.e_beta)[e];
-    sr.bt = reinterpret_cast<const float4*>(G.e_beta)[G.epad + e];
-    so.hh = reinterpret_cast<const float4*>(G.e_h)[e];
-    sr.hh = reinterpret_cast<const float4*>(G.e_h)[G.epad + e];
-  }
-  // H+/BM and H-/BM from the distances: 1 / ((1/H) BM)
-  so.eta_p = __fdividef(1.0f, so.hh.x * so.hh.z);
-  so.eta_m = __fdividef(1.0f, so.hh.y * so.hh.z);
-  sr.eta_p = __fdividef(1.0f, sr.hh.x * sr.hh.z);
-  sr.eta_m = __fdividef(1.0f, sr.hh.y * sr.hh.z);
+  EdgeRec r;
+  load_edge(G, e, live, r);
   griddep_wait();
   float dt;
   if (OWN_DT) {
@@ -540,19 +625,10 @@ __device__ __forceinline__ void edge_body(const DevGeomMixed& G, const DevState&
   }
   unsigned bits = 0;
   if (live) {
-    SlotGeomF g;
-    g.ec = f3(ce.x, ce.y, ce.z);
-    g.en = f3(ne.x, ne.y, ne.z);
-    g.nxr = f3(ce.w, ne.w, __int_as_float(ids.z));
     float uL[kDim], uR[kDim], F[kDim] = {0.f, 0.f, 0.f, 0.f, 0.f};
-    recon_slot(S.W32, G.fpad, ids.x & 0x0fffffff, ids.x >> 28, so, g.ec, g.en, dt, P, uL);
-    recon_slot(S.W32, G.fpad, ids.y & 0x0fffffff, ids.y >> 28, sr, g.ec, f3(-g.en.x, -g.en.y, -g.en.z), dt,
-               P, uR);
-    if (STAGE == 2 && S.uplus32 != nullptr) {
-      st5(S.uplus32, 2 * G.epad, e, uL);
-      st5(S.uplus32, 2 * G.epad, G.epad + e, uR);
-    }
-    bits = (P.solver == kSolverIsoHLLE) ? iso_flux_star(uL, uR, g, F) : flux_star(uL, uR, g, P.gam_f, P.solver, F);
+    recon_edge(stage_input<STAGE>(S), G, P, r, dt, uL, uR);
+    bits = (P.solver == kSolverIsoHLLE) ? iso_flux_star(uL, uR, r.g, F)
+                                        : flux_star(uL, uR, r.g, P.gam_f, P.solver, F);
 #pragma unroll
     for (int k = 0; k < kDim; ++k)
       if (isnan(F[k])) bits |= 1u;
@@ -560,6 +636,22 @@ __device__ __forceinline__ void edge_body(const DevGeomMixed& G, const DevState&
   }
   bits = __reduce_or_sync(0xffffffffu, bits);
   if ((threadIdx.x & 31) == 0 && bits) atomicOr(S.err, bits);
+}
+
+// The last step's stage-2 edge states for the writers (write_t_curl): the
+// stage-2 reconstruction of edge_body, from the stage-2 input W32b and the
+// step's dt, into uplus32 (edge-major: the owner side of edge e at e, the
+// reverse side at epad + e).
+__global__ void __launch_bounds__(kBlock) edge_states_kernel(DevGeomMixed G, DevState S, PhysParams P) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= G.n_edges) return;
+  EdgeRec r;
+  load_edge(G, e, true, r);
+  const float dt = reinterpret_cast<const float2*>(S.scal + kScDtF)->x;
+  float uL[kDim], uR[kDim];
+  recon_edge(stage_input<2>(S), G, P, r, dt, uL, uR);
+  st5(S.uplus32, 2 * G.epad, e, uL);
+  st5(S.uplus32, 2 * G.epad, G.epad + e, uR);
 }
 
 // at most 73 registers (7 blocks of 128 per SM; a small spill, measured best
@@ -611,9 +703,9 @@ __device__ __forceinline__ void update_body(const DevGeomMixed& G, const DevStat
   if (live) {
     const float2 dtf2 = *reinterpret_cast<const float2*>(S.scal + kScDtF);
     const float dtf = (STAGE == 1) ? dtf2.y : dtf2.x;
-    Acc acc[kDim];
-#pragma unroll
-    for (int k = 0; k < kDim; ++k) acc[k] = Acc{0.f, 0.f};
+    // fields 0-1 and 2-3 accumulate in packed pairs, field 4 alone
+    Acc2 a01{make_float2(0.f, 0.f), make_float2(0.f, 0.f)}, a23 = a01;
+    Acc a4{0.f, 0.f};
     // unrolled over the slot bound so that every slot's gather is in flight
     // before the first is summed; the sum stays in slot order
 #pragma unroll
@@ -622,14 +714,19 @@ __device__ __forceinline__ void update_body(const DevGeomMixed& G, const DevStat
         const float cf = dtf * co[j];
         // -cf F with F = Fe on the owner side and -Fe on the reverse side
         const float c = (se[j] < 0) ? cf : -cf;
-        float fe[kDim];
-        ld5(S.fe32, G.epad, se[j] & 0x7fffffff, fe);
-#pragma unroll
-        for (int k = 0; k < kDim; ++k) acc[k].add(c * fe[k]);
+        const int e = se[j] & 0x7fffffff;
+        const float4 fe = ld4(S.fe32, e);
+        const float fe4 = S.fe32[4 * (size_t)G.epad + e];
+        const float2 c2 = make_float2(c, c);
+        a01.add(mul2(c2, make_float2(fe.x, fe.y)));
+        a23.add(mul2(c2, make_float2(fe.z, fe.w)));
+        a4.add(c * fe4);
       }
     }
+    const Acc acc[kDim] = {{a01.hi.x, a01.lo.x}, {a01.hi.y, a01.lo.y}, {a23.hi.x, a23.lo.x},
+                           {a23.hi.y, a23.lo.y}, a4};
     float w[kDim], src[kDim];
-    ld5(S.W32, fp, f, w);
+    ld5(stage_input<STAGE>(S), fp, f, w);
     source_f32(w, fcn32, fpc::d2f(acc0), P, src);
     // the FP32 increment (flux sum + dt source, one rounding) is added to
     // the FP64 state; U0 stays in S.U until stage 2 overwrites it
@@ -644,7 +741,7 @@ __device__ __forceinline__ void update_body(const DevGeomMixed& G, const DevStat
     if (P.solver == kSolverIsoHLLE) {
       u[4] = 0.0;
       float vm, dm;
-      iso_w32_candidates(u, fcn32, S.W32, fp, f, vm, dm);
+      iso_w32_candidates(u, fcn32, stage_output<STAGE>(S), fp, f, vm, dm);
       if (STAGE == 2) {
 #pragma unroll
         for (int k = 0; k < kDim; ++k) S.U[k * fp + f] = u[k];
@@ -653,7 +750,7 @@ __device__ __forceinline__ void update_body(const DevGeomMixed& G, const DevStat
       }
     } else {
       float w32[kDim];
-      store_face_state(S.W32, fp, f, u, fcn32, fcn_lo, P, w32);
+      store_face_state(stage_output<STAGE>(S), fp, f, u, fcn32, fcn_lo, P, w32);
       if (STAGE == 2) {
 #pragma unroll
         for (int k = 0; k < kDim; ++k) S.U[k * fp + f] = u[k];
@@ -726,6 +823,101 @@ __global__ void __launch_bounds__(kBlock) ens_update_kernel(const EnsInstance* _
   const int2 t = tiles[tile];
   const EnsInstance& I = inst[t.x];
   update_body<STAGE>(I.G, I.S, I.P, t.y + (threadIdx.x & 31));
+}
+
+// ---- the ensemble as one persistent launch
+// One cooperative launch runs n_steps steps of every member: per step the
+// per-member dt clip, then edge and update of each stage, the phases
+// separated by a grid-wide barrier instead of launch boundaries.  Every
+// block is resident (the grid is sized to the occupancy), warps take the
+// same (member, tile) pairs in the same order as the five-launch schedule
+// and call the same bodies, so each member's arithmetic is that of a
+// standalone solver.
+
+// ld.acquire at GPU scope (the barrier's generation word)
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Grid-wide barrier: thread 0 of every block adds itself to bar[0]; the
+// last to arrive restarts the count and advances the generation bar[1]; the
+// others wait for the generation to move, at most kBarrierSpins polls of
+// ~64 ns (about a quarter of a second, against phases of well under a
+// millisecond), after which they set kEnsBarrierTimeout in *status and the
+// launch returns early.  The GPU-scope fences around the arrival make every
+// write of a phase visible to the loads of the next one, like a launch
+// boundary.  All threads of the block call it; false when the wait ran out.
+constexpr long long kBarrierSpins = 1ll << 22;
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned* status) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ok = 1;
+    const unsigned gen = ld_acquire_gpu(bar + 1);
+    __threadfence();
+    if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      long long spins = 0;
+      while (ld_acquire_gpu(bar + 1) == gen) {
+        if (++spins > kBarrierSpins) {
+          atomicOr(status, kEnsBarrierTimeout);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// at most 72 registers like the edge launches (their bodies dominate)
+__global__ void __launch_bounds__(kBlock, 7)
+    ens_persistent_kernel(const EnsInstance* __restrict__ inst, int n_inst, const int2* __restrict__ ftiles,
+                          int n_ftiles, const int2* __restrict__ etiles, int n_etiles, double dt0, int n_steps,
+                          unsigned* bar, unsigned* status) {
+  const int warps = gridDim.x * kWarpTiles;
+  const int wid = blockIdx.x * kWarpTiles + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  for (int s = 0; s < n_steps; ++s) {
+    // each member's dt from its keys, then fresh keys (the finalize launch)
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_inst; i += gridDim.x * blockDim.x) {
+      publish_dt(inst[i].S, clip_dt(inst[i].S.keys, inst[i].P, dt0), dt0);
+      restart_keys(inst[i].S.keys);
+    }
+    if (!grid_barrier(bar, status)) return;
+    for (int t = wid; t < n_etiles; t += warps) {
+      const int2 tt = etiles[t];
+      const EnsInstance& I = inst[tt.x];
+      edge_body<1, false>(I.G, I.S, I.P, tt.y + lane, 0.0, 0.f);
+    }
+    if (!grid_barrier(bar, status)) return;
+    for (int t = wid; t < n_ftiles; t += warps) {
+      const int2 tt = ftiles[t];
+      const EnsInstance& I = inst[tt.x];
+      update_body<1>(I.G, I.S, I.P, tt.y + lane);
+    }
+    if (!grid_barrier(bar, status)) return;
+    for (int t = wid; t < n_etiles; t += warps) {
+      const int2 tt = etiles[t];
+      const EnsInstance& I = inst[tt.x];
+      edge_body<2, false>(I.G, I.S, I.P, tt.y + lane, 0.0, 0.f);
+    }
+    if (!grid_barrier(bar, status)) return;
+    for (int t = wid; t < n_ftiles; t += warps) {
+      const int2 tt = ftiles[t];
+      const EnsInstance& I = inst[tt.x];
+      update_body<2>(I.G, I.S, I.P, tt.y + lane);
+    }
+    if (s + 1 < n_steps && !grid_barrier(bar, status)) return;
+  }
 }
 
 inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
@@ -812,5 +1004,40 @@ cudaError_t ensemble_step(const EnsInstance* inst, int n_inst, const int2* ftile
 }
 
 const void* ensemble_finalize_kernel_ptr() { return (const void*)mx::ens_finalize_kernel; }
+
+cudaError_t mixed_edge_states(const DevGeomMixed& G, const DevState& S, const PhysParams& P, cudaStream_t st) {
+  mx::edge_states_kernel<<<mx::blocks_for(G.n_edges), mx::kBlock, 0, st>>>(G, S, P);
+  return cudaGetLastError();
+}
+
+int ensemble_persistent_grid(int device) {
+  int per_sm = 0, sms = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mx::ens_persistent_kernel, mx::kBlock, 0) !=
+      cudaSuccess)
+    return 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
+  return per_sm * sms;
+}
+
+cudaError_t ensemble_persistent(const EnsInstance* inst, int n_inst, const int2* ftiles, int n_ftiles,
+                                const int2* etiles, int n_etiles, double dt0, int n_steps, unsigned* bar,
+                                unsigned* status, int grid, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), st);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(mx::kBlock);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, mx::ens_persistent_kernel, inst, n_inst, ftiles, n_ftiles, etiles, n_etiles,
+                            dt0, n_steps, bar, status);
+}
+
+const void* ensemble_persistent_kernel_ptr() { return (const void*)mx::ens_persistent_kernel; }
 
 }  // namespace splash

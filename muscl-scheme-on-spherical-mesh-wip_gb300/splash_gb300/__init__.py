@@ -57,10 +57,12 @@ EXPORTED = (
     "splash_ensemble_create", "splash_ensemble_destroy", "splash_ensemble_do_steps",
     "splash_ensemble_synchronize", "splash_ensemble_stream", "splash_ensemble_get_state",
     "splash_ensemble_member_info", "splash_ensemble_schedule", "splash_ensemble_size",
+    "splash_ensemble_set_schedule",
     "splash_cfl_dt_noalloc",
     "splash_adjoint_create", "splash_adjoint_destroy", "splash_adjoint_forward",
     "splash_adjoint_backward", "splash_adjoint_run", "splash_tlm_run", "splash_adjoint_info",
     "splash_adjoint_error_word", "splash_adjoint_dt_schedule", "splash_face_geometry",
+    "splash_adjoint_branch_tape",
 )
 
 
@@ -141,12 +143,14 @@ def library(path: str | os.PathLike | None = None) -> C.CDLL:
         "splash_ensemble_member_info": [vp, C.c_int, dp, C.POINTER(C.c_uint32)],
         "splash_ensemble_schedule": [vp, ip, ip, dp],
         "splash_ensemble_size": [vp, ip, C.POINTER(C.c_int64)],
+        "splash_ensemble_set_schedule": [vp, C.c_int, C.c_int],
         "splash_adjoint_create": [vp, C.c_int, C.POINTER(vp)],
         "splash_adjoint_destroy": [vp],
         "splash_adjoint_forward": [vp, dp, dp, C.c_int, C.c_double, dp],
         "splash_adjoint_backward": [vp, dp, dp, dp],
         "splash_adjoint_run": [vp, dp, dp, C.c_int, C.c_double, dp, dp, dp, dp],
         "splash_tlm_run": [vp, dp, dp, dp, dp, C.c_int, C.c_double, dp, dp],
+        "splash_adjoint_branch_tape": [vp, dp, dp, C.c_int, C.c_int, dp, C.POINTER(C.c_int64)],
         "splash_adjoint_info": [vp, dp],
         "splash_adjoint_error_word": [vp, C.POINTER(C.c_uint32)],
         "splash_adjoint_dt_schedule": [vp, dp, C.c_int],
@@ -558,12 +562,23 @@ class Ensemble:
         return {"t": out[0], "dt": out[1], "max_vel": out[2], "extra_dt": out[3], "err": int(err.value)}
 
     def schedule(self) -> dict:
+        """The schedule in use: tile order, edge block width (0: the
+        persistent launch), and the autotuner's ms per step of every
+        candidate (five-launch rows by order x {32, 64, 128} threads, and
+        the persistent launch by order)."""
         o = C.c_int()
         w = C.c_int()
-        ms = np.zeros(9)
+        ms = np.zeros(12)
         _check(self._lib.splash_ensemble_schedule(self.handle, C.byref(o), C.byref(w), _dptr(ms)))
         return {"order": ["member", "largest-first", "round-robin"][o.value], "recon_width": w.value,
-                "trial_ms": ms.reshape(3, 3).tolist()}
+                "persistent": w.value == 0, "trial_ms": ms[:9].reshape(3, 3).tolist(),
+                "trial_ms_persistent": ms[9:].tolist()}
+
+    def set_schedule(self, order: int, edge_block: int) -> None:
+        """order 0..2 (member, largest first, round-robin); edge_block 32,
+        64 or 128 threads (five launches per step) or 0 (one persistent
+        launch per do_steps call)."""
+        _check(self._lib.splash_ensemble_set_schedule(self.handle, order, edge_block))
 
     def size(self) -> tuple[int, int]:
         n = C.c_int()
@@ -648,6 +663,24 @@ class Adjoint:
         _check(self._lib.splash_tlm_run(self.handle, _dptr(U0), self._p(th), self._p(dU), self._p(dth), n_steps,
                                         dt0, _dptr(U), _dptr(dUf)))
         return U, dUf
+
+    _TAPE_MODES = {"replay": 0, "record": 1, "compare": 2}
+
+    def branch_tape(self, U0, theta, n_steps: int, mode: str) -> tuple[np.ndarray, int]:
+        """The FP64 forward on the last forward run's dt schedule with its
+        branch decisions taped (validation only): mode "record" records them,
+        "replay" replays the recording (the branch-frozen map the adjoint
+        differentiates; count = replayed decisions the run's own values would
+        have taken otherwise), "compare" runs the plain forward and counts
+        the (face, launch) evaluations whose branch path departs from the
+        recording.  Returns (U_final, count)."""
+        U0 = self._arr(U0, (self.n_faces, 5))
+        th = self._arr(theta, (3,))
+        out = np.empty((self.n_faces, 5))
+        count = C.c_int64(0)
+        _check(self._lib.splash_adjoint_branch_tape(self.handle, _dptr(U0), self._p(th), n_steps,
+                                                    self._TAPE_MODES[mode], _dptr(out), C.byref(count)))
+        return out, count.value
 
     def info(self) -> dict:
         o = np.zeros(8)

@@ -155,3 +155,87 @@ def test_batched_workload_members_match_oracle():
         assert abs(info["t"] - o.info()["t"]) <= 1e-6 * o.info()["t"], (d["index"], info["t"], o.info()["t"])
     assert sum(1 for i in range(len(sub)) if ens.member_info(i)["err"]) == 3
     ens.close()
+
+
+@pytest.mark.parametrize("order", [0, 1, 2])
+def test_persistent_launch_equals_standalone_solvers(order):
+    """The persistent schedule (one cooperative launch per do_steps call,
+    grid barriers between the phases) computes exactly what the standalone
+    mixed solvers compute, for every tile order; 25 steps in one launch
+    equal five launches of 5 steps and the five-launch schedule."""
+    import splash_gb300 as sg
+
+    ms = members(seed=13)
+    ens = sg.Ensemble(ms, autotune=False)
+    ens.set_schedule(order, 0)
+    assert ens.schedule()["persistent"]
+    ens.do_steps(25, 1e-2)
+    ens.synchronize()
+    for i, m in enumerate(ms):
+        s = sg.Solver(m["mesh"], m["U_in"], m["U_in"].shape[1], m["gam"], 0.0, True, params=m["params"],
+                      solver=m["solver"], precision=sg.PREC_MIXED)
+        s.do_steps(25, 1e-2)
+        info = ens.member_info(i)
+        assert np.array_equal(ens.get_state(i), s.get_state()), (order, i)
+        assert info["t"] == s.time() and info["dt"] == s.last_dt() and info["err"] == s.error_word()
+        s.close()
+    pieces = sg.Ensemble(ms, autotune=False)
+    pieces.set_schedule(order, 0)
+    for _ in range(5):
+        pieces.do_steps(5, 1e-2)
+    five = sg.Ensemble(ms, autotune=False)
+    five.set_schedule(order, 64)
+    assert not five.schedule()["persistent"]
+    five.do_steps(25, 1e-2)
+    for i in range(len(ms)):
+        assert np.array_equal(pieces.get_state(i), ens.get_state(i))
+        assert np.array_equal(five.get_state(i), ens.get_state(i))
+    for e in (ens, pieces, five):
+        e.close()
+
+
+def test_full_batched_workload_matches_oracle_record():
+    """All 512 members of the batched workload (503 steps, own CFL dt)
+    against the oracle's record (tests/golden/ensemble_oracle_c3.json, made
+    by gen_ensemble_oracle.py: every member run on the FP64 oracle): every
+    member's stop bits equal the oracle's, each latched within one step of
+    the oracle's first, the times agree to 1e-6 and the total mass (energy)
+    to 1e-7 (1e-6) relative."""
+    import json
+
+    import splash_gb300 as sg
+    from splash_gb300 import workloads
+
+    from helpers import GOLDEN
+
+    rec = json.loads((GOLDEN / "ensemble_oracle_c3.json").read_text())
+    draws = workloads.ensemble_draws(512, 3)
+    members = workloads.ensemble_members(sg, draws)
+    ens = sg.Ensemble(members, autotune=False)
+    first = [None] * len(draws)
+    for k in range(rec["steps"]):
+        ens.do_steps(1, rec["dt0"])
+        if k >= 400:  # the recorded latches come late in the run
+            for r in rec["members"]:
+                i = r["index"]
+                if r["bits"] and first[i] is None and ens.member_info(i)["err"]:
+                    first[i] = k + 1
+    geoms = {}
+    for r in rec["members"]:
+        i = r["index"]
+        info = ens.member_info(i)
+        assert info["err"] == r["bits"], (i, info["err"], r["bits"])
+        for bit, step in r["first_step"].items():
+            assert first[i] is not None and abs(first[i] - step) <= 1, (i, first[i], step)
+        assert abs(info["t"] - r["t"]) <= 1e-6 * r["t"], (i, info["t"], r["t"])
+        lv = r["level"]
+        if lv not in geoms:
+            geoms[lv] = sg.Geometry(sg.icosphere_hex(lv))["area"]
+        U = ens.get_state(i)
+        mass = float(np.sum(geoms[lv] * U[:, 0]))
+        assert abs(mass - r["mass"]) <= 1e-7 * abs(r["mass"]), (i, mass, r["mass"])
+        if r["dim"] == 5:
+            en = float(np.sum(geoms[lv] * U[:, 4]))
+            assert abs(en - r["energy"]) <= 1e-6 * abs(r["energy"]), (i, en, r["energy"])
+    assert sum(1 for r in rec["members"] if r["bits"]) == 3
+    ens.close()
