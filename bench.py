@@ -213,22 +213,20 @@ def pinned_like(torch, a):
 
 
 def time_e2e(sg, solver, U_host, steps, flush=None, torch=None):
-    """Through the C ABI with host buffers: set_state (H2D), do_step,
-    get_state (D2H) per step, wall clock.  With `flush`, the L2 is flushed
-    before every step outside the timed intervals."""
+    """Through the C ABI with host buffers, wall clock per step: the state
+    uploaded from the host array (H2D), one do_step, the state read back
+    (D2H), as one splash_do_steps_host call (one synchronisation per step).
+    With `flush`, the L2 is flushed before every step outside the timed
+    intervals."""
     out = np.empty_like(U_host) if torch is None else pinned_like(torch, np.zeros_like(U_host))
-    solver.set_state(U_host)
-    solver.do_step(DT0)
-    solver.get_state(out)
+    solver.do_steps_host(U_host, 1, DT0, out)
     total = 0.0
     for _ in range(steps):
         if flush is not None:
             flush(torch)
             solver.synchronize()
         t0 = time.perf_counter()
-        solver.set_state(U_host)
-        solver.do_step(DT0)
-        solver.get_state(out)
+        solver.do_steps_host(U_host, 1, DT0, out)
         total += time.perf_counter() - t0
     return total
 
@@ -518,9 +516,16 @@ def adjoint_workload(sg, torch, steps=1000, checkpoint_every=50, level=6, seed=4
     tape_ms = (time.perf_counter() - t0) * 1e3  # wall clock, including the state upload
     evaluations = base.n_faces * (1 + 4 * steps)
     rows_j = fd_check(adj, U0, theta, gU, gth, target, area, steps, dt0, joint[:n_joint], h)
-    rows_p = fd_check(adj, U0, theta, gU, gth, target, area, steps, dt0,
-                      [(np.zeros_like(U0), d) for d in params], h)
+    pdirs = [(np.zeros_like(U0), d) for d in params]
+    rows_p = fd_check(adj, U0, theta, gU, gth, target, area, steps, dt0, pdirs, h)
     rows_l = fd_check(adj, U0, theta, gU, gth, target, area, steps, dt0, local, h)
+    # smaller steps straddle fewer kinks (the error follows the crossings, not
+    # h^2: fourth-order differences do no better), until round-off sets in
+    sweep = {f"{hs:.0e}": {"parameter": fd_summary(fd_check(adj, U0, theta, gU, gth, target, area, steps, dt0,
+                                                             pdirs, hs), evaluations),
+                           "core_state": fd_summary(fd_check(adj, U0, theta, gU, gth, target, area, steps, dt0,
+                                                              local, hs), evaluations)}
+             for hs in (1e-7, 1e-8)}
     out = {"workload": f"icosphere_hex({level}) {base.n_faces} faces, HLLC, FP64, {steps} steps dt0={dt0}, "
                        f"checkpoints every {checkpoint_every}",
            "forward_ms": fwd_ms, "gradient_forward_ms": info["ms_forward"],
@@ -532,6 +537,7 @@ def adjoint_workload(sg, torch, steps=1000, checkpoint_every=50, level=6, seed=4
            "fd_parameter": fd_summary(rows_p, evaluations), "fd_core_state": fd_summary(rows_l, evaluations),
            "fd_joint": fd_summary(rows_j, evaluations),
            "fd_rows": {"joint": rows_j, "parameter": rows_p, "core_state": rows_l},
+           "fd_smaller_h": sweep,
            "core_faces": int(core.sum()),
            "branch_tape_record_ms": tape_ms,
            "fd_note": "central differences of the FP64 forward at h; crossings: (face, launch) evaluations whose "
@@ -744,7 +750,8 @@ def run_ours(args):
                    "working_set_mb": round((geo_b + st_b) / 1e6, 1)},
         "gpu_launches": 4 * args.steps,
         "e2e": {"value": F * e2e_steps / e2e_secs, "unit": METRIC, "h2d_bytes_per_step": bytes_io,
-                "d2h_bytes_per_step": bytes_io, "host_buffers": "pinned (page-locked) FP64 [F][5] arrays"},
+                "d2h_bytes_per_step": bytes_io, "host_buffers": "pinned (page-locked) FP64 [F][5] arrays",
+                "call": "splash_do_steps_host(s, U_in, 1, dt0, U_out) per step"},
         "fp64": {"value": value64, "ms_per_step": secs64 / args.steps * 1e3, "kernel_ms": kern64,
                  "fp64_pipe_busy": fp64_pipe_busy()},
         "back_to_back": {"value": F * args.steps / secs_bb, "ms_per_step": secs_bb / args.steps * 1e3,

@@ -189,6 +189,12 @@ SPLASH_API int splash_dim(splash_solver* s, int* dim);
  * the staging path.  Both are synchronous and give identical states. */
 SPLASH_API int splash_get_state(splash_solver* s, double* U);
 SPLASH_API int splash_set_state(splash_solver* s, const double* U);
+/* set_state(U_in), n do_step(dt0) calls and get_state(U_out) as one call
+ * with one synchronisation, at the end (either state pointer may be NULL;
+ * U_in may equal U_out): for a coupling code that owns the state in host
+ * memory and hands it over every step.  The same states as the three calls.
+ * No counterpart in the reference (its state stays in the solver object). */
+SPLASH_API int splash_do_steps_host(splash_solver* s, const double* U_in, int n, double dt0, double* U_out);
 /* Per-step diagnostics of MUSCL_base.hpp:187-214 for the current state:
  * out[0] = sum Sigma*A, out[1..3] = sum l*A, out[4] = sum E*A. */
 SPLASH_API int splash_diagnostics(splash_solver* s, double out[5]);

@@ -585,6 +585,20 @@ int splash_do_steps(splash_solver* h, int n, double dt0) {
   return s->steps_n(n, dt0);
 }
 
+int splash_do_steps_host(splash_solver* h, const double* U_in, int n, double dt0, double* U_out) {
+  GET_SOLVER(h);
+  if (n < 0) return fail(SPLASH_E_INVALID, "n < 0");
+  if (U_in) {
+    const int rc = s->upload_state(U_in);
+    if (rc) return rc;
+  }
+  const int rc = s->steps_n(n, dt0);
+  if (rc) return rc;
+  if (U_out) return s->download_state(U_out);  // synchronises the stream
+  SPLASH_CUDA(cudaStreamSynchronize(s->stream));  // U_in has been read
+  return SPLASH_OK;
+}
+
 int splash_stream(splash_solver* h, void** stream) {
   Solver* s = reinterpret_cast<Solver*>(h);
   if (!s || !stream) return fail(SPLASH_E_INVALID, "NULL argument");

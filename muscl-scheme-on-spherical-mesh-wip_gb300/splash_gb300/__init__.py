@@ -46,7 +46,7 @@ STOP_NEG_EXTRA_DT = 8
 # every entry point declared in include/splash_gb300.h
 EXPORTED = (
     "splash_last_error", "splash_version", "splash_create", "splash_destroy",
-    "splash_do_step", "splash_do_steps", "splash_synchronize", "splash_time",
+    "splash_do_step", "splash_do_steps", "splash_do_steps_host", "splash_synchronize", "splash_time",
     "splash_stop_check", "splash_error_word", "splash_last_dt", "splash_steps",
     "splash_n_faces", "splash_dim", "splash_get_state", "splash_set_state",
     "splash_diagnostics", "splash_get_permutation", "splash_write_t_rho",
@@ -119,6 +119,7 @@ def library(path: str | os.PathLike | None = None) -> C.CDLL:
     for name, args in {
         "splash_destroy": [vp], "splash_do_step": [vp, C.c_double],
         "splash_do_steps": [vp, C.c_int, C.c_double], "splash_synchronize": [vp],
+        "splash_do_steps_host": [vp, dp, C.c_int, C.c_double, dp],
         "splash_time": [vp, dp], "splash_stop_check": [vp, ip],
         "splash_error_word": [vp, C.POINTER(C.c_uint32)], "splash_last_dt": [vp, dp],
         "splash_steps": [vp, C.POINTER(C.c_int64)], "splash_n_faces": [vp, ip],
@@ -356,6 +357,16 @@ class Solver:
 
     def do_steps(self, n: int, dt0: float) -> None:
         _check(self._lib.splash_do_steps(self.handle, n, dt0))
+
+    def do_steps_host(self, U_in, n: int, dt0: float, out: np.ndarray | None = None) -> np.ndarray:
+        """set_state(U_in), n steps and get_state() in one synchronising
+        call (U_in None: continue from the current state)."""
+        if out is None:
+            out = np.empty((self.n_faces, self.dim))
+        src = None if U_in is None else np.ascontiguousarray(U_in, dtype=np.float64)
+        _check(self._lib.splash_do_steps_host(self.handle, None if src is None else _dptr(src), n, dt0,
+                                              _dptr(out)))
+        return out
 
     def synchronize(self) -> None:
         _check(self._lib.splash_synchronize(self.handle))

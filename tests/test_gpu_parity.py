@@ -221,3 +221,30 @@ def test_device_diagnostics_and_light_curves(precision):
     seen = [(phi < np.pi / 2) & (phi > -np.pi / 2), fcn @ obs[1] > 0, theta < np.pi / 2, theta > np.pi / 2]
     ref = [np.sum((PI * (np.abs(fcn @ o) / np.linalg.norm(o)) * area)[m]) for o, m in zip(obs, seen)]
     assert np.allclose(s.get_light_curves(), ref, rtol=1e-12, atol=0)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_do_steps_host_equals_separate_calls(precision):
+    """splash_do_steps_host (upload, n steps, download, one synchronisation)
+    gives exactly the states of set_state + do_steps + get_state, with the
+    input and output arrays distinct or the same; NULL input continues."""
+    import splash_gb300 as sg
+
+    mesh = mesh_of("hex", 4)
+    g = sg.Geometry(mesh)
+    gam = sg.initial_conditions.gam2d(4 / 3)
+    U0 = sg.initial_conditions.rotating_blob(g.unit_face_centers(), gam, seed=21)
+    a = sg.MUSCL_HLLCplus(mesh, U0, 5, gam, 0.0, True, precision=precision)
+    b = sg.MUSCL_HLLCplus(mesh, U0, 5, gam, 0.0, True, precision=precision)
+    U1 = U0.copy()
+    U1[:, 0] *= 1.001
+    a.set_state(U1)
+    a.do_steps(3, 1e-3)
+    ref = a.get_state()
+    out = b.do_steps_host(U1, 3, 1e-3)
+    assert np.array_equal(out, ref)
+    a.do_steps(2, 1e-3)
+    assert np.array_equal(b.do_steps_host(None, 2, 1e-3), a.get_state())
+    inout = U1.copy()
+    b.do_steps_host(inout, 3, 1e-3, out=inout)
+    assert np.array_equal(inout, ref)
