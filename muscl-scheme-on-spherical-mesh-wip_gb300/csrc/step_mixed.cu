@@ -675,7 +675,7 @@ __global__ void __launch_bounds__(kBlock, 7) edge_kernel(DevGeomMixed G, DevStat
 // BLOCK_FOLD: kBlock-thread launches of one solver; RESTART_KEYS: the
 // stage-1 update of one solver gives the keys a fresh start (the stage-1
 // edge launch that read them has completed)
-template <int STAGE, bool BLOCK_FOLD = false, bool RESTART_KEYS = false>
+template <int STAGE, int MAXS = kMaxFaceSlots, bool BLOCK_FOLD = false, bool RESTART_KEYS = false>
 __device__ __forceinline__ void update_body(const DevGeomMixed& G, const DevState& S, const PhysParams& P,
                                             int f) {
   const int fp = G.fpad;
@@ -684,8 +684,8 @@ __device__ __forceinline__ void update_body(const DevGeomMixed& G, const DevStat
   double acc0 = 0.0;
   int n = 0;
   // the slots' edges and flux coefficients: geometry, loaded before the wait
-  int se[kMaxFaceSlots];
-  float co[kMaxFaceSlots];
+  int se[MAXS];
+  float co[MAXS];
   if (live) {
     fcn32 = plane3f(G.fcn32, fp, f);
     acc0 = G.acc_src[f];
@@ -693,7 +693,7 @@ __device__ __forceinline__ void update_body(const DevGeomMixed& G, const DevStat
     n = G.nslots[f];
   }
 #pragma unroll
-  for (int j = 0; j < kMaxFaceSlots; ++j) {
+  for (int j = 0; j < MAXS; ++j) {
     se[j] = (j < n) ? G.slot_edge[j * fp + f] : 0;
     co[j] = (j < n) ? G.coef[j * fp + f] : 0.f;
   }
@@ -709,7 +709,7 @@ __device__ __forceinline__ void update_body(const DevGeomMixed& G, const DevStat
     // unrolled over the slot bound so that every slot's gather is in flight
     // before the first is summed; the sum stays in slot order
 #pragma unroll
-    for (int j = 0; j < kMaxFaceSlots; ++j) {
+    for (int j = 0; j < MAXS; ++j) {
       if (j < n) {
         const float cf = dtf * co[j];
         // -cf F with F = Fe on the owner side and -Fe on the reverse side
@@ -766,10 +766,13 @@ __device__ __forceinline__ void update_body(const DevGeomMixed& G, const DevStat
   }
 }
 
-template <int STAGE>
+// MAXS: the mesh's largest face degree rounded up to 4, 6 or 8 (the slot
+// loop is unrolled to it; slots past a face's own count are predicated off
+// but still issued)
+template <int STAGE, int MAXS>
 __global__ void __launch_bounds__(kBlock) update_kernel(DevGeomMixed G, DevState S, PhysParams P) {
   griddep_launch_dependents();
-  update_body<STAGE, true, STAGE == 1>(G, S, P, blockIdx.x * blockDim.x + threadIdx.x);
+  update_body<STAGE, MAXS, true, STAGE == 1>(G, S, P, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // ---------------------------------------------------------------- ensemble
@@ -968,13 +971,22 @@ cudaError_t mixed_step(const DevGeomMixed& G, const DevState& S, const PhysParam
   if (ev) cudaEventRecord(ev[0], st);
   if (ev) cudaEventRecord(ev[1], st);
   const float dt0f = fpc::d2f(dt0);
+  void (*upd1)(DevGeomMixed, DevState, PhysParams) = mx::update_kernel<1, 8>;
+  void (*upd2)(DevGeomMixed, DevState, PhysParams) = mx::update_kernel<2, 8>;
+  if (G.max_slots <= 4) {
+    upd1 = mx::update_kernel<1, 4>;
+    upd2 = mx::update_kernel<2, 4>;
+  } else if (G.max_slots <= 6) {
+    upd1 = mx::update_kernel<1, 6>;
+    upd2 = mx::update_kernel<2, 6>;
+  }
   chk(launch_pdl(mx::edge_kernel<1>, egrid, dim3(mx::kBlock), st, G, S, P, dt0, dt0f));
   if (ev) cudaEventRecord(ev[2], st);
-  chk(launch_pdl(mx::update_kernel<1>, ugrid, dim3(mx::kBlock), st, G, S, P));
+  chk(launch_pdl(upd1, ugrid, dim3(mx::kBlock), st, G, S, P));
   if (ev) cudaEventRecord(ev[3], st);
   chk(launch_pdl(mx::edge_kernel<2>, egrid, dim3(mx::kBlock), st, G, S, P, dt0, dt0f));
   if (ev) cudaEventRecord(ev[4], st);
-  chk(launch_pdl(mx::update_kernel<2>, ugrid, dim3(mx::kBlock), st, G, S, P));
+  chk(launch_pdl(upd2, ugrid, dim3(mx::kBlock), st, G, S, P));
   if (ev) cudaEventRecord(ev[5], st);
   return e != cudaSuccess ? e : cudaGetLastError();
 }
