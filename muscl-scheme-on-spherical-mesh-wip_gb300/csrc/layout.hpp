@@ -111,7 +111,7 @@ struct DevGeomMixed {
   const double* acc_src;  // accretion mass source, FP64
   const float* coef;      // per slot: round_diff * chord / area
   const int* slot_edge;   // per slot: its edge, bit 31 set on the edge's reverse side
-  // interior edges, each once, in owner order; records of four interleaved
+  // interior edges, each once, face-major (owner face, then slot); records of four interleaved
   // values (read as one int4 / float4 each), see MixedPlanes
   int n_edges;
   int epad;               // n_edges rounded up to 32

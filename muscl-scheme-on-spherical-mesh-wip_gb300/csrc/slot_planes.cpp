@@ -205,9 +205,9 @@ MixedPlanes make_mixed_planes(const SlotPlanes& sp) {
       mp.coef[q] = (float)(sp.round_diff * sp.chord[q] / sp.area[i]);
     }
   if (sp.n_faces >= (1 << 28)) throw std::runtime_error("too many faces for the edge records");
-  // Edges in ascending owner order (plane-major, faces ascending within a
-  // plane, i.e. ascending slot-plane index): edge e is the e-th owner slot,
-  // its index an exclusive prefix sum of the owner flags.
+  // Owner slots: of the two slots of an edge, the one with the smaller
+  // slot-plane index.  Edge e is the e-th owner slot in the visiting order
+  // below, its index an exclusive prefix sum of the owner flags.
   std::vector<unsigned char> is_own(PS, 0);
   bool lonely = false;
 #pragma omp parallel for schedule(static) reduction(|| : lonely)
@@ -219,13 +219,23 @@ MixedPlanes make_mixed_planes(const SlotPlanes& sp) {
     is_own[q] = (int)q < r;
   }
   if (lonely) throw std::runtime_error("slot without a neighbour");
-  // prefix sum over fixed chunks: counts per chunk, then offsets
-  const long long nchunk = 256, clen = ((long long)PS + nchunk - 1) / nchunk;
+  // Edges numbered face-major: the owner face's internal (Hilbert) index,
+  // then its slot, so that the edges of a run of faces form one compact
+  // range (the update's flux gathers stay local; measured 1% faster per step
+  // on hex(7) than ascending slot-plane order).  Prefix sum over fixed chunks
+  // of faces: counts per chunk, then offsets.
+  const long long nvisit = (long long)sp.n_faces;
+  const int ms = sp.max_slots, fp = sp.fpad;
+  auto visit = [&](long long v, auto&& fn) {  // the owner-candidate slots of face v, in slot order
+    for (int j = 0; j < ms; ++j) fn((long long)j * fp + v);
+  };
+  const long long nchunk = 256, clen = (nvisit + nchunk - 1) / nchunk;
   std::vector<long long> base(nchunk + 1, 0);
 #pragma omp parallel for schedule(static)
   for (long long c = 0; c < nchunk; ++c) {
     long long cnt = 0;
-    for (long long q = c * clen; q < std::min((long long)PS, (c + 1) * clen); ++q) cnt += is_own[q];
+    for (long long v = c * clen; v < std::min(nvisit, (c + 1) * clen); ++v)
+      visit(v, [&](long long q) { cnt += is_own[q]; });
     base[c + 1] = cnt;
   }
   for (long long c = 0; c < nchunk; ++c) base[c + 1] += base[c];
@@ -235,15 +245,16 @@ MixedPlanes make_mixed_planes(const SlotPlanes& sp) {
 #pragma omp parallel for schedule(static)
   for (long long c = 0; c < nchunk; ++c) {
     long long e = base[c];
-    for (long long q = c * clen; q < std::min((long long)PS, (c + 1) * clen); ++q) {
-      if (!is_own[q]) continue;
-      const int r = sp.rev[q];
-      own[e] = (int)q;
-      nbr[e] = r;
-      mp.slot_edge[q] = (int)e;
-      mp.slot_edge[r] = (int)((unsigned)e | 0x80000000u);
-      ++e;
-    }
+    for (long long v = c * clen; v < std::min(nvisit, (c + 1) * clen); ++v)
+      visit(v, [&](long long q) {
+        if (!is_own[q]) return;
+        const int r = sp.rev[q];
+        own[e] = (int)q;
+        nbr[e] = r;
+        mp.slot_edge[q] = (int)e;
+        mp.slot_edge[r] = (int)((unsigned)e | 0x80000000u);
+        ++e;
+      });
   }
   const int ep = mp.epad = (mp.n_edges + 31) / 32 * 32;
   mp.e_ids.assign(4 * (size_t)ep, 0);

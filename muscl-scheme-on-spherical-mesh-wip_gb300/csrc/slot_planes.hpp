@@ -51,7 +51,7 @@ std::vector<double> accretion_source_fcn(const std::vector<double>& fcn, int n_f
 // one thread reconstructs the edge states of the edge's two slots (owner:
 // the slot with the smaller slot-plane index; reverse: the other) and
 // evaluates the Riemann flux once, in the owner's orientation.  Edges are
-// numbered in owner order; slot_edge maps every slot to its edge, with bit
+// numbered face-major; slot_edge maps every slot to its edge, with bit
 // 31 set on the reverse side, whose flux is the owner's with the sign
 // flipped (every Riemann solver here satisfies F(uR, uL, -n) = -F(uL, uR, n)).
 // The two sides share the edge centre (the same two vertices) and have
