@@ -161,7 +161,7 @@ struct Ensemble {
   }
 
   cudaError_t launch_step(double dt0) {
-    return ensemble_step(d_inst, n, d_ftiles, n_ftiles, d_etiles, n_etiles, recon_width, dt0, stream);
+    return ensemble_step(d_inst, n, d_ftiles, n_ftiles, d_etiles, n_etiles, recon_width, max_slots, dt0, stream);
   }
   cudaError_t launch_persistent(double dt0, int steps) {
     return ensemble_persistent(d_inst, n, d_ftiles, n_ftiles, d_etiles, n_etiles, dt0, steps, d_bar, d_bar + 2,

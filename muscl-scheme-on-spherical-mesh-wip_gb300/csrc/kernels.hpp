@@ -52,11 +52,13 @@ cudaError_t mixed_scatter_prepare(const double* aos, const int* iperm, const Dev
 // ---- ensemble (step_mixed.cu): batched launches over instances ----
 // ftiles: (instance, first face) of 32-face tiles; etiles: (instance,
 // first edge) of 32-edge tiles; edge_block: threads per block of the
-// reconstruction + edge-flux launch (a multiple of 32; one tile per warp).
+// reconstruction + edge-flux launch (a multiple of 32; one tile per warp);
+// max_slots: the largest face degree over the members' meshes.
 cudaError_t ensemble_prepare(const EnsInstance* inst, int n_inst, const int2* ftiles, int n_ftiles,
                              cudaStream_t st);
 cudaError_t ensemble_step(const EnsInstance* inst, int n_inst, const int2* ftiles, int n_ftiles,
-                          const int2* etiles, int n_etiles, int edge_block, double dt0, cudaStream_t st);
+                          const int2* etiles, int n_etiles, int edge_block, int max_slots, double dt0,
+                          cudaStream_t st);
 const void* ensemble_finalize_kernel_ptr();
 // The same n_steps steps as one cooperative launch of `grid` resident blocks
 // (ensemble_persistent_grid: the occupancy of the current device, 0 if it

@@ -816,8 +816,9 @@ __global__ void __launch_bounds__(kBlock, 7) ens_edge_kernel(const EnsInstance* 
   edge_body<STAGE, false>(I.G, I.S, I.P, t.y + (threadIdx.x & 31), 0.0, 0.f);
 }
 
-// update: one 32-face tile per warp
-template <int STAGE>
+// update: one 32-face tile per warp; MAXS as update_kernel, over every
+// member's mesh
+template <int STAGE, int MAXS>
 __global__ void __launch_bounds__(kBlock) ens_update_kernel(const EnsInstance* __restrict__ inst,
                                                             const int2* __restrict__ tiles, int n_tiles) {
   griddep_launch_dependents();
@@ -825,7 +826,7 @@ __global__ void __launch_bounds__(kBlock) ens_update_kernel(const EnsInstance* _
   if (tile >= n_tiles) return;  // whole warps: the candidates fold per warp
   const int2 t = tiles[tile];
   const EnsInstance& I = inst[t.x];
-  update_body<STAGE>(I.G, I.S, I.P, t.y + (threadIdx.x & 31));
+  update_body<STAGE, MAXS>(I.G, I.S, I.P, t.y + (threadIdx.x & 31));
 }
 
 // ---- the ensemble as one persistent launch
@@ -999,7 +1000,8 @@ cudaError_t ensemble_prepare(const EnsInstance* inst, int n_inst, const int2* ft
 }
 
 cudaError_t ensemble_step(const EnsInstance* inst, int n_inst, const int2* ftiles, int n_ftiles,
-                          const int2* etiles, int n_etiles, int edge_block, double dt0, cudaStream_t st) {
+                          const int2* etiles, int n_etiles, int edge_block, int max_slots, double dt0,
+                          cudaStream_t st) {
   const int wpb = edge_block / 32;
   const dim3 egrid((n_etiles + wpb - 1) / wpb);
   const dim3 ugrid((n_ftiles + mx::kWarpTiles - 1) / mx::kWarpTiles);
@@ -1007,11 +1009,20 @@ cudaError_t ensemble_step(const EnsInstance* inst, int n_inst, const int2* ftile
   auto chk = [&](cudaError_t r) {
     if (e == cudaSuccess) e = r;
   };
+  void (*upd1)(const EnsInstance*, const int2*, int) = mx::ens_update_kernel<1, 8>;
+  void (*upd2)(const EnsInstance*, const int2*, int) = mx::ens_update_kernel<2, 8>;
+  if (max_slots <= 4) {
+    upd1 = mx::ens_update_kernel<1, 4>;
+    upd2 = mx::ens_update_kernel<2, 4>;
+  } else if (max_slots <= 6) {
+    upd1 = mx::ens_update_kernel<1, 6>;
+    upd2 = mx::ens_update_kernel<2, 6>;
+  }
   chk(launch_pdl(mx::ens_finalize_kernel, dim3((n_inst + 127) / 128), dim3(128), st, inst, n_inst, dt0));
   chk(launch_pdl(mx::ens_edge_kernel<1>, egrid, dim3(edge_block), st, inst, etiles, n_etiles));
-  chk(launch_pdl(mx::ens_update_kernel<1>, ugrid, dim3(mx::kBlock), st, inst, ftiles, n_ftiles));
+  chk(launch_pdl(upd1, ugrid, dim3(mx::kBlock), st, inst, ftiles, n_ftiles));
   chk(launch_pdl(mx::ens_edge_kernel<2>, egrid, dim3(edge_block), st, inst, etiles, n_etiles));
-  chk(launch_pdl(mx::ens_update_kernel<2>, ugrid, dim3(mx::kBlock), st, inst, ftiles, n_ftiles));
+  chk(launch_pdl(upd2, ugrid, dim3(mx::kBlock), st, inst, ftiles, n_ftiles));
   return e != cudaSuccess ? e : cudaGetLastError();
 }
 
