@@ -674,8 +674,12 @@ __global__ void __launch_bounds__(kBlock, 7) edge_kernel(DevGeomMixed G, DevStat
 // must call it (the candidates fold per warp).
 // BLOCK_FOLD: kBlock-thread launches of one solver; RESTART_KEYS: the
 // stage-1 update of one solver gives the keys a fresh start (the stage-1
-// edge launch that read them has completed)
-template <int STAGE, int MAXS = kMaxFaceSlots, bool BLOCK_FOLD = false, bool RESTART_KEYS = false>
+// edge launch that read them has completed); EARLY_STATE: the face's own
+// FP32 and FP64 states are loaded right after the dependency wait, in
+// flight with the flux gathers (one memory round trip less per thread, at
+// more registers: for the one-wave launches of one solver)
+template <int STAGE, int MAXS = kMaxFaceSlots, bool BLOCK_FOLD = false, bool RESTART_KEYS = false,
+          bool EARLY_STATE = false>
 __device__ __forceinline__ void update_body(const DevGeomMixed& G, const DevState& S, const PhysParams& P,
                                             int f) {
   const int fp = G.fpad;
@@ -701,6 +705,13 @@ __device__ __forceinline__ void update_body(const DevGeomMixed& G, const DevStat
   if (RESTART_KEYS && f == 0) restart_keys(S.keys);
   float vmax = 0.f, dmin = kNoBound;
   if (live) {
+    float w[kDim];
+    double u0[kDim];
+    if (EARLY_STATE) {
+      ld5(stage_input<STAGE>(S), fp, f, w);
+#pragma unroll
+      for (int k = 0; k < kDim; ++k) u0[k] = S.U[k * fp + f];
+    }
     const float2 dtf2 = *reinterpret_cast<const float2*>(S.scal + kScDtF);
     const float dtf = (STAGE == 1) ? dtf2.y : dtf2.x;
     // fields 0-1 and 2-3 accumulate in packed pairs, field 4 alone
@@ -725,14 +736,15 @@ __device__ __forceinline__ void update_body(const DevGeomMixed& G, const DevStat
     }
     const Acc acc[kDim] = {{a01.hi.x, a01.lo.x}, {a01.hi.y, a01.lo.y}, {a23.hi.x, a23.lo.x},
                            {a23.hi.y, a23.lo.y}, a4};
-    float w[kDim], src[kDim];
-    ld5(stage_input<STAGE>(S), fp, f, w);
+    float src[kDim];
+    if (!EARLY_STATE) ld5(stage_input<STAGE>(S), fp, f, w);
     source_f32(w, fcn32, fpc::d2f(acc0), P, src);
     // the FP32 increment (flux sum + dt source, one rounding) is added to
     // the FP64 state; U0 stays in S.U until stage 2 overwrites it
     double u[kDim];
 #pragma unroll
-    for (int k = 0; k < kDim; ++k) u[k] = S.U[k * fp + f] + fpc::f2d((acc[k].hi + acc[k].lo) + dtf * src[k]);
+    for (int k = 0; k < kDim; ++k)
+      u[k] = (EARLY_STATE ? u0[k] : S.U[k * fp + f]) + fpc::f2d((acc[k].hi + acc[k].lo) + dtf * src[k]);
     if (P.accretion_on) {  // accretion mass source in FP64
       const double dt_here = S.scal[(STAGE == 1) ? kScDtHalf : kScDt];
       u[0] += dt_here * acc0;
@@ -773,6 +785,14 @@ template <int STAGE, int MAXS>
 __global__ void __launch_bounds__(kBlock) update_kernel(DevGeomMixed G, DevState S, PhysParams P) {
   griddep_launch_dependents();
   update_body<STAGE, MAXS, true, STAGE == 1>(G, S, P, blockIdx.x * blockDim.x + threadIdx.x);
+}
+// the same with the early state loads of update_body, at most 56 registers
+// (9 blocks of 128 per SM; uncapped they take 63-72 registers and the
+// hex(7) grid two waves, 1-4 us slower per launch)
+template <int STAGE, int MAXS>
+__global__ void __launch_bounds__(kBlock, 9) update_early_kernel(DevGeomMixed G, DevState S, PhysParams P) {
+  griddep_launch_dependents();
+  update_body<STAGE, MAXS, true, STAGE == 1, true>(G, S, P, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // ---------------------------------------------------------------- ensemble
@@ -972,14 +992,24 @@ cudaError_t mixed_step(const DevGeomMixed& G, const DevState& S, const PhysParam
   if (ev) cudaEventRecord(ev[0], st);
   if (ev) cudaEventRecord(ev[1], st);
   const float dt0f = fpc::d2f(dt0);
+  // The update variant: the early state loads for meshes of at most 6-gons
+  // whose update grid nearly fills the GPU in one wave at 9 blocks per SM
+  // (more than 6, at most 9 blocks per SM).  Measured per step against the
+  // plain update: hex(7) (8.4 blocks per SM) 1.2% faster; hex(5) (0.5 per
+  // SM) 2.5% slower back to back; hex(8) (34 per SM) 0.8% slower; hex(9)
+  // equal; quad(7) with the 4-slot copy 3% slower (a larger spill).
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    sms = 0;
+  const bool early = G.max_slots > 4 && G.max_slots <= 6 && (int)ugrid.x > 6 * sms && (int)ugrid.x <= 9 * sms;
   void (*upd1)(DevGeomMixed, DevState, PhysParams) = mx::update_kernel<1, 8>;
   void (*upd2)(DevGeomMixed, DevState, PhysParams) = mx::update_kernel<2, 8>;
   if (G.max_slots <= 4) {
     upd1 = mx::update_kernel<1, 4>;
     upd2 = mx::update_kernel<2, 4>;
   } else if (G.max_slots <= 6) {
-    upd1 = mx::update_kernel<1, 6>;
-    upd2 = mx::update_kernel<2, 6>;
+    upd1 = early ? mx::update_early_kernel<1, 6> : mx::update_kernel<1, 6>;
+    upd2 = early ? mx::update_early_kernel<2, 6> : mx::update_kernel<2, 6>;
   }
   chk(launch_pdl(mx::edge_kernel<1>, egrid, dim3(mx::kBlock), st, G, S, P, dt0, dt0f));
   if (ev) cudaEventRecord(ev[2], st);
