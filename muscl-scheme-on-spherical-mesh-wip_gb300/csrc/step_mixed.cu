@@ -591,26 +591,56 @@ __device__ __forceinline__ void load_edge(const DevGeomMixed& G, int e, bool liv
     ce = ld_rec_f4(G.e_ec, e);
     ne = ld_rec_f4(G.e_en, e);
     r.so.st = ld_rec_i4(G.e_sten, e);
-    r.sr.st = ld_rec_i4(G.e_sten, ep + e);
     r.so.bt = ld_rec_f4(G.e_beta, e);
-    r.sr.bt = ld_rec_f4(G.e_beta, ep + e);
     r.so.hh = ld_rec_f4(G.e_h, e);
-    r.sr.hh = ld_rec_f4(G.e_h, ep + e);
+    // the reverse slot's constants are loaded once the owner slot's edge
+    // state is done (recon_edge); their lines are fetched into L2 now
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(G.e_sten + 4 * (ep + e)));
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(G.e_beta + 4 * (ep + e)));
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(G.e_h + 4 * (ep + e)));
   }
   r.so.eta_p = __fdividef(1.0f, r.so.hh.x * r.so.hh.z);
   r.so.eta_m = __fdividef(1.0f, r.so.hh.y * r.so.hh.z);
-  r.sr.eta_p = __fdividef(1.0f, r.sr.hh.x * r.sr.hh.z);
-  r.sr.eta_m = __fdividef(1.0f, r.sr.hh.y * r.sr.hh.z);
   r.g.ec = f3(ce.x, ce.y, ce.z);
   r.g.en = f3(ne.x, ne.y, ne.z);
   r.g.nxr = f3(ce.w, ne.w, __int_as_float(r.ids.z));
 }
 
-// the edge states of both slots of an edge from the face states W: the
+// The reverse slot's record entries, loaded after the owner slot's edge
+// state: volatile with a memory clobber, so that neither the compiler nor
+// the barrier before them moves them up into the owner slot, where they
+// would hold 14 registers through its reconstruction (measured on hex(7):
+// 72 registers with a 16-byte spill at 7 blocks per SM before; 64 without
+// a spill at 8 blocks per SM after, 0.0704 -> 0.0667 ms per step flushed).
+__device__ __forceinline__ int4 ld_rec_i4_late(const int* base, size_t i) {
+  int4 v;
+  asm volatile("ld.global.nc.L1::no_allocate.v4.s32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+               : "l"(base + 4 * i)
+               : "memory");
+  return v;
+}
+__device__ __forceinline__ float4 ld_rec_f4_late(const float* base, size_t i) {
+  float4 v;
+  asm volatile("ld.global.nc.L1::no_allocate.v4.f32 {%0, %1, %2, %3}, [%4];"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "l"(base + 4 * i)
+               : "memory");
+  return v;
+}
+
+// the edge states of both slots of edge e from the face states W: the
 // owner slot (face f) and the reverse slot (face g, negated normal)
-__device__ __forceinline__ void recon_edge(const float* W, const DevGeomMixed& G, const PhysParams& P,
-                                           const EdgeRec& r, float dt, float* uL, float* uR) {
+__device__ __forceinline__ void recon_edge(const float* W, const DevGeomMixed& G, const PhysParams& P, EdgeRec& r,
+                                           int e, float dt, float* uL, float* uR) {
   recon_slot(W, G.fpad, r.ids.x & 0x0fffffff, r.ids.x >> 28, r.so, r.g.ec, r.g.en, dt, P, uL);
+  asm volatile("" ::: "memory");
+  const size_t ep = (size_t)G.epad;
+  r.sr.st = ld_rec_i4_late(G.e_sten, ep + e);
+  r.sr.bt = ld_rec_f4_late(G.e_beta, ep + e);
+  r.sr.hh = ld_rec_f4_late(G.e_h, ep + e);
+  r.sr.eta_p = __fdividef(1.0f, r.sr.hh.x * r.sr.hh.z);
+  r.sr.eta_m = __fdividef(1.0f, r.sr.hh.y * r.sr.hh.z);
   recon_slot(W, G.fpad, r.ids.y & 0x0fffffff, r.ids.y >> 28, r.sr, r.g.ec, f3(-r.g.en.x, -r.g.en.y, -r.g.en.z),
              dt, P, uR);
 }
@@ -647,7 +677,7 @@ __device__ __forceinline__ void edge_body(const DevGeomMixed& G, const DevState&
   unsigned bits = 0;
   if (live) {
     float uL[kDim], uR[kDim], F[kDim] = {0.f, 0.f, 0.f, 0.f, 0.f};
-    recon_edge(stage_input<STAGE>(S), G, P, r, dt, uL, uR);
+    recon_edge(stage_input<STAGE>(S), G, P, r, e, dt, uL, uR);
     bits = (P.solver == kSolverIsoHLLE) ? iso_flux_star(uL, uR, r.g, F)
                                         : flux_star(uL, uR, r.g, P.gam_f, P.solver, F);
 #pragma unroll
@@ -670,15 +700,15 @@ __global__ void __launch_bounds__(kBlock) edge_states_kernel(DevGeomMixed G, Dev
   load_edge(G, e, true, r);
   const float dt = reinterpret_cast<const float2*>(S.scal + kScDtF)->x;
   float uL[kDim], uR[kDim];
-  recon_edge(stage_input<2>(S), G, P, r, dt, uL, uR);
+  recon_edge(stage_input<2>(S), G, P, r, e, dt, uL, uR);
   st5(S.uplus32, 2 * G.epad, e, uL);
   st5(S.uplus32, 2 * G.epad, G.epad + e, uR);
 }
 
-// at most 73 registers (7 blocks of 128 per SM; a small spill, measured best
-// of 5 to 8 blocks)
+// at most 64 registers (8 blocks of 128 per SM, no spill; measured best of
+// 7 to 9 blocks)
 template <int STAGE>
-__global__ void __launch_bounds__(kBlock, 7) edge_kernel(DevGeomMixed G, DevState S, PhysParams P, double dt0,
+__global__ void __launch_bounds__(kBlock, 8) edge_kernel(DevGeomMixed G, DevState S, PhysParams P, double dt0,
                                                          float dt0f) {
   griddep_launch_dependents();
   edge_body<STAGE, STAGE == 1>(G, S, P, blockIdx.x * blockDim.x + threadIdx.x, dt0, dt0f);
@@ -844,10 +874,10 @@ __global__ void ens_finalize_kernel(const EnsInstance* __restrict__ inst, int n,
 // reconstruction + edge fluxes: one 32-edge tile per warp (tiles hold
 // (instance, first edge))
 constexpr int kWarpTiles = kBlock / 32;
-// at most 73 registers like the single-solver edge launch (blocks of at
-// most 128 threads)
+// at most 64 registers like the single-solver edge launch (blocks of at
+// most 128 threads; 1% faster per ensemble step than 72 registers)
 template <int STAGE>
-__global__ void __launch_bounds__(kBlock, 7) ens_edge_kernel(const EnsInstance* __restrict__ inst,
+__global__ void __launch_bounds__(kBlock, 8) ens_edge_kernel(const EnsInstance* __restrict__ inst,
                                                        const int2* __restrict__ tiles, int n_tiles) {
   griddep_launch_dependents();
   const int tile = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -923,7 +953,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned* status) {
   return ok != 0;
 }
 
-// at most 72 registers like the edge launches (their bodies dominate)
+// at most 72 registers (7 blocks of 128 per SM)
 __global__ void __launch_bounds__(kBlock, 7)
     ens_persistent_kernel(const EnsInstance* __restrict__ inst, int n_inst, const int2* __restrict__ ftiles,
                           int n_ftiles, const int2* __restrict__ etiles, int n_etiles, double dt0, int n_steps,
