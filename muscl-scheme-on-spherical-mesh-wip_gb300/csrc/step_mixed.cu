@@ -630,10 +630,19 @@ __device__ __forceinline__ float4 ld_rec_f4_late(const float* base, size_t i) {
 }
 
 // the edge states of both slots of edge e from the face states W: the
-// owner slot (face f) and the reverse slot (face g, negated normal)
+// owner slot (face f) and the reverse slot (face g, negated normal).  PARK
+// (blocks of at most kBlock threads): the owner slot's edge state waits in
+// shared memory while the reverse slot is reconstructed (5 registers fewer
+// at the peak: on hex(7) 0.0672 -> 0.0665 ms per step flushed)
+template <bool PARK = false>
 __device__ __forceinline__ void recon_edge(const float* W, const DevGeomMixed& G, const PhysParams& P, EdgeRec& r,
                                            int e, float dt, float* uL, float* uR) {
   recon_slot(W, G.fpad, r.ids.x & 0x0fffffff, r.ids.x >> 28, r.so, r.g.ec, r.g.en, dt, P, uL);
+  __shared__ float park[PARK ? kDim : 1][PARK ? kBlock : 1];
+  if (PARK) {
+#pragma unroll
+    for (int k = 0; k < kDim; ++k) park[k][threadIdx.x] = uL[k];
+  }
   asm volatile("" ::: "memory");
   const size_t ep = (size_t)G.epad;
   r.sr.st = ld_rec_i4_late(G.e_sten, ep + e);
@@ -643,6 +652,11 @@ __device__ __forceinline__ void recon_edge(const float* W, const DevGeomMixed& G
   r.sr.eta_m = __fdividef(1.0f, r.sr.hh.y * r.sr.hh.z);
   recon_slot(W, G.fpad, r.ids.y & 0x0fffffff, r.ids.y >> 28, r.sr, r.g.ec, f3(-r.g.en.x, -r.g.en.y, -r.g.en.z),
              dt, P, uR);
+  if (PARK) {
+    asm volatile("" ::: "memory");
+#pragma unroll
+    for (int k = 0; k < kDim; ++k) uL[k] = park[k][threadIdx.x];
+  }
 }
 
 // The stage's input face states: W32 in stage 1 (written by set_state and
@@ -660,7 +674,9 @@ __device__ __forceinline__ float* stage_output(const DevState& S) {
   return STAGE == 1 ? S.W32b : S.W32;
 }
 
-template <int STAGE, bool OWN_DT>
+// PARK: recon_edge parks the owner slot's edge state in shared memory (the
+// single-solver edge launches; the batched ones measured 3% slower with it)
+template <int STAGE, bool OWN_DT, bool PARK = false>
 __device__ __forceinline__ void edge_body(const DevGeomMixed& G, const DevState& S, const PhysParams& P, int e,
                                           double dt0, float dt0f) {
   const bool live = e < G.n_edges;
@@ -677,7 +693,7 @@ __device__ __forceinline__ void edge_body(const DevGeomMixed& G, const DevState&
   unsigned bits = 0;
   if (live) {
     float uL[kDim], uR[kDim], F[kDim] = {0.f, 0.f, 0.f, 0.f, 0.f};
-    recon_edge(stage_input<STAGE>(S), G, P, r, e, dt, uL, uR);
+    recon_edge<PARK>(stage_input<STAGE>(S), G, P, r, e, dt, uL, uR);
     bits = (P.solver == kSolverIsoHLLE) ? iso_flux_star(uL, uR, r.g, F)
                                         : flux_star(uL, uR, r.g, P.gam_f, P.solver, F);
 #pragma unroll
@@ -711,7 +727,7 @@ template <int STAGE>
 __global__ void __launch_bounds__(kBlock, 8) edge_kernel(DevGeomMixed G, DevState S, PhysParams P, double dt0,
                                                          float dt0f) {
   griddep_launch_dependents();
-  edge_body<STAGE, STAGE == 1>(G, S, P, blockIdx.x * blockDim.x + threadIdx.x, dt0, dt0f);
+  edge_body<STAGE, STAGE == 1, true>(G, S, P, blockIdx.x * blockDim.x + threadIdx.x, dt0, dt0f);
 }
 
 // res2d + RK combine (MUSCL_base.hpp:238-276, 124-161) of face f: the
