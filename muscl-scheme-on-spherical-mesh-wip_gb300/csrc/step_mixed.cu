@@ -197,16 +197,34 @@ __device__ __forceinline__ void fold_candidates_block(float vmax2, float dmin, u
 }
 
 // The FP32 face state (Sigma, l, Pi) of the FP64 state u of face f, stored
-// to W32 and returned in w: the pressure recovery Pi = (E - |r x l|^2 /
-// (2 Sigma)) (gam - 1), floored at 1e-16 (MUSCL_base.hpp:538), runs in
-// double-word FP32 arithmetic (dword.cuh), accurate to the FP32 rounding of
-// Pi down to kinetic energies within 1e-5 of E, instead of on the FP64 pipe
-// (about 2 lanes per SM per clock here); lo holds the FP32 residuals of the
-// unit centre r32.
+// to W32 and returned in w: (Sigma, l) rounded to the nearest float and the
+// pressure recovery Pi = (E - |r x l|^2 / (2 Sigma)) (gam - 1), floored at
+// 1e-16 (MUSCL_base.hpp:538).  Where the kinetic term cancels part of E
+// (above E / 8: low density, fast flow) the recovery runs in double-word
+// FP32 arithmetic (dword.cuh), accurate to the FP32 rounding of Pi down to
+// kinetic energies within 1e-5 of E, instead of on the FP64 pipe (about 2
+// lanes per SM per clock here); lo holds the FP32 residuals of the unit
+// centre r32.  Below E / 8 the subtraction loses at most a factor 8/7, so
+// plain FP32 gives Pi to a few units in the last place of its float (the
+// rounding of E, an error of a few ulp in the kinetic term, which enters at
+// most 1/7 of the result, and two roundings): measured on hex(7), the
+// same density L1 error against FP64 after 200 steps (6.0e-8) with both
+// update launches at 12.3 us instead of 12.4 / 14.3 us.
 __device__ __forceinline__ void store_face_state(float* W32, int fp, int f, const double* u, F3 r32, F3 lo,
                                                  const PhysParams& P, float* w) {
-  const dw::DW r[3] = {{r32.x, lo.x}, {r32.y, lo.y}, {r32.z, lo.z}};
-  dw::face_state_dw(u, r, dw::DW{P.gam_m1_h, P.gam_m1_l}, w);
+  w[0] = fpc::d2f(u[0]);
+  w[1] = fpc::d2f(u[1]);
+  w[2] = fpc::d2f(u[2]);
+  w[3] = fpc::d2f(u[3]);
+  const float E = fpc::d2f(u[4]);
+  const F3 c = cross3(r32, f3(w[1], w[2], w[3]));
+  const float ke = 0.5f * __fdividef(dot3(c, c), w[0]);
+  if (ke <= 0.125f * E) {  // false for NaN operands (a zero density) and E < 0
+    w[4] = fmaxf((E - ke) * P.gam_m1_h, 1e-16f);
+  } else {
+    const dw::DW r[3] = {{r32.x, lo.x}, {r32.y, lo.y}, {r32.z, lo.z}};
+    dw::face_state_dw(u, r, dw::DW{P.gam_m1_h, P.gam_m1_l}, w);
+  }
   st5(W32, fp, f, w);
 }
 
