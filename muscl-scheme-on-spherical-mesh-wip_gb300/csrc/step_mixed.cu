@@ -205,9 +205,10 @@ __device__ __forceinline__ void fold_candidates_block(float vmax2, float dmin, u
 // kinetic energies within 1e-5 of E, instead of on the FP64 pipe (about 2
 // lanes per SM per clock here); lo holds the FP32 residuals of the unit
 // centre r32.  Below E / 8 the subtraction loses at most a factor 8/7, so
-// plain FP32 gives Pi to a few units in the last place of its float (the
-// rounding of E, an error of a few ulp in the kinetic term, which enters at
-// most 1/7 of the result, and two roundings): measured on hex(7), the
+// plain FP32 gives Pi within about 2 units in the last place of its float
+// (the rounding of E, a few ulp in the kinetic term, which enters at most
+// 1/7 of the result, and two roundings; 2.1 ulp at worst on 10^6 states
+// just below E / 8, 1.0 when the kinetic term is negligible): on hex(7) the
 // same density L1 error against FP64 after 200 steps (6.0e-8) with both
 // update launches at 12.3 us instead of 12.4 / 14.3 us.
 __device__ __forceinline__ void store_face_state(float* W32, int fp, int f, const double* u, F3 r32, F3 lo,
