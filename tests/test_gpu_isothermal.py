@@ -95,3 +95,25 @@ def test_isothermal_mixed_close_to_fp64():
     assert mom < 1e-4, mom
     assert abs(b.time() - a.time()) <= 1e-6 * a.time()
     assert not a.get_stop_check() and not b.get_stop_check()
+
+
+def test_isothermal_mixed_hex7_close_to_fp64():
+    """The isothermal solver on icosphere_hex(7), whose update grid (1,281
+    blocks of 128) is about one wave on a 152-SM GB300: the mixed path runs
+    its early-state update launches there.  Rotating blob, 50 steps, against
+    the FP64 isothermal path."""
+    import splash_gb300 as sg
+
+    mesh = mesh_of("hex", 7)
+    g = sg.Geometry(mesh)
+    U0 = _state(g, "blob", 7)
+    a = sg.MUSCL_HLLE(mesh, U0, 4, GAM)
+    b = sg.MUSCL_HLLE(mesh, U0, 4, GAM, precision=sg.PREC_MIXED)
+    a.do_steps(50, 1e-3)
+    b.do_steps(50, 1e-3)
+    Ua, Ub = a.get_state(), b.get_state()
+    area = g["area"]
+    l1 = np.sum(area * np.abs(Ub[:, 0] - Ua[:, 0])) / np.sum(area * np.abs(Ua[:, 0]))
+    assert l1 < 1e-6, l1
+    assert abs(b.time() - a.time()) <= 1e-6 * a.time()
+    assert not a.get_stop_check() and not b.get_stop_check()
