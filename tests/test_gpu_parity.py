@@ -105,6 +105,34 @@ def test_fp64_mid_size_workload_100_steps():
     s.close()
 
 
+@pytest.mark.parametrize("solver", [1, 2])
+def test_fp64_mid_size_workload_other_solvers(solver):
+    """The same hex(7) accreting workload (quiet noise of seed 1, dt0 = 2e-4,
+    100 steps) with MUSCL_HLLE_p and MUSCL_HLLC: the GPU FP64 state against
+    the oracle on every face at 1e-10 relative L-infinity per field, dt, t
+    and the stop flag equal."""
+    import splash_gb300 as sg
+
+    c = load("state_c1_hex7_hllcp.npz")
+    g = sg.Geometry(mesh_of(str(c["mesh"]), int(c["level"])))
+    U0 = sg.initial_conditions.quiet_noise(g.unit_face_centers(), float(c["gam"]), seed=int(c["seed"]))
+    case = {k: c[k] for k in ("gam", "accretion_on", "mesh", "level", "params")}
+    case["U0"] = U0
+    case["solver"] = solver
+    nsteps, dt0 = int(c["steps"]), float(c["dt0"])
+    s = gpu_solver(case)
+    s.do_steps(nsteps, dt0)
+    o = make_oracle(g, case)
+    o.do_steps(nsteps, dt0)
+    err = rel_linf(s.get_state(), o.get_state())
+    assert np.all(err < TOL), (solver, err)
+    info = o.info()
+    assert abs(s.last_dt() - info["dt"]) <= 1e-13 * info["dt"]
+    assert abs(s.time() - info["t"]) <= 1e-12 * info["t"]
+    assert s.get_stop_check() == info["stop"]
+    s.close()
+
+
 def test_step_is_deterministic_and_graph_replay_equals_single_steps():
     c = load("state_hex3_hllcp_acc.npz")
     a = gpu_solver(c)
