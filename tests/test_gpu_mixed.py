@@ -242,3 +242,26 @@ def test_nan_input_stop_flag_mixed_like_fp64(field):
     assert out[0][0] == out[1][0] == (field == 0)
     if field == 4:
         assert np.array_equal(out[0][1], out[1][1])
+
+
+def test_mixed_quad7_shear_close_to_fp64():
+    """quad_sphere(7) (98,304 faces, four slots per face: the 4-slot update
+    launches), MUSCL_HLLC, the shear layer of seed 2, 200 steps of dt0 = 1e-4:
+    the mixed state against the FP64 state, relative L1 per field."""
+    import splash_gb300 as sg
+
+    mesh = mesh_of("quad", 7)
+    g = sg.Geometry(mesh)
+    gam = sg.initial_conditions.gam2d(4 / 3)
+    U0 = sg.initial_conditions.shear_layer(g.unit_face_centers(), gam, seed=2)
+    a = sg.MUSCL_HLLC(mesh, U0, 5, gam, 0.0, False)
+    b = sg.MUSCL_HLLC(mesh, U0, 5, gam, 0.0, False, precision=sg.PREC_MIXED)
+    a.do_steps(200, 1e-4)
+    b.do_steps(200, 1e-4)
+    Ua, Ub = a.get_state(), b.get_state()
+    area = g["area"][:, None]
+    l1 = np.sum(area * np.abs(Ub - Ua), axis=0) / np.sum(area * np.abs(Ua), axis=0)
+    assert l1[0] < 1e-6 and l1[4] < 1e-6, l1
+    assert np.all(l1[1:4] < 1e-5), l1
+    assert abs(b.time() - a.time()) <= 1e-6 * a.time()
+    assert a.get_stop_check() == b.get_stop_check()
