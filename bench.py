@@ -519,13 +519,14 @@ def adjoint_workload(sg, torch, steps=1000, checkpoint_every=50, level=6, seed=4
     pdirs = [(np.zeros_like(U0), d) for d in params]
     rows_p = fd_check(adj, U0, theta, gU, gth, target, area, steps, dt0, pdirs, h)
     rows_l = fd_check(adj, U0, theta, gU, gth, target, area, steps, dt0, local, h)
-    # smaller steps straddle fewer kinks (the error follows the crossings, not
-    # h^2: fourth-order differences do no better), until round-off sets in
+    # other steps straddle other kinks (the error follows the crossings, not
+    # h^2: fourth-order differences do no better; it is not monotone in h),
+    # until round-off sets in below about 3e-8
     sweep = {f"{hs:.0e}": {"parameter": fd_summary(fd_check(adj, U0, theta, gU, gth, target, area, steps, dt0,
                                                              pdirs, hs), evaluations),
                            "core_state": fd_summary(fd_check(adj, U0, theta, gU, gth, target, area, steps, dt0,
                                                               local, hs), evaluations)}
-             for hs in (1e-7, 1e-8)}
+             for hs in (2e-7, 1e-7, 1e-8)}
     out = {"workload": f"icosphere_hex({level}) {base.n_faces} faces, HLLC, FP64, {steps} steps dt0={dt0}, "
                        f"checkpoints every {checkpoint_every}",
            "forward_ms": fwd_ms, "gradient_forward_ms": info["ms_forward"],
